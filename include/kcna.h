@@ -1,0 +1,196 @@
+/*
+ * kcna.h - C ABI of the GB300 (sm_103a) FastKCNA graph-construction library.
+ *
+ * This is the drop-in boundary for FastKCNA's build path.  The reference
+ * exposes a C++ virtual interface (kgraph::KGraph in src/kgraph.h:113-304)
+ * whose data enters through the IndexOracle plugin (src/kgraph.h:63-81) over a
+ * caller-owned Matrix<float> (src/kgraph-data.h:97-288).  Every entry point
+ * below is plain C: pointers, sizes and status codes, no C++ or torch types, so
+ * that a C++ facade (kgraph_gb300.h), a ctypes stub or any other FFI can bind
+ * it.  Each function names the reference interface it replaces.
+ *
+ * Threading: one context per host thread.  A context owns one CUDA stream on
+ * one device and all device memory of one build.
+ * Errors: every call returns kcna_status; kcna_last_error() gives the text.
+ */
+#ifndef KCNA_H
+#define KCNA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    KCNA_OK = 0,
+    KCNA_E_ARG = 1,     /* maps to kgraph::invalid_argument (src/kgraph.h:363-366) */
+    KCNA_E_OOM = 2,     /* device or host allocation failed */
+    KCNA_E_CUDA = 3,    /* a CUDA call failed; maps to kgraph::runtime_error */
+    KCNA_E_TIMEOUT = 4, /* a bounded device-side wait gave up (error flag set) */
+    KCNA_E_IO = 5,      /* maps to kgraph::io_error (src/kgraph.h:373-376) */
+    KCNA_E_STATE = 6    /* call order violated (e.g. prune before build) */
+} kcna_status;
+
+/* Graph kinds.  The numbers equal the reference's PG_type column of the run CSV
+ * (src/kgraph.cpp:3757 HNSW=2, :3816 NSG=1, :3874 TauMNG=3, :3931 AlphaPG=4). */
+typedef enum {
+    KCNA_NSG = 1,
+    KCNA_HNSW_LAYER = 2, /* NSG-style layer without tree_grow (buildHNSWLayer, :2326-2337) */
+    KCNA_TAUMNG = 3,
+    KCNA_ALPHAPG = 4
+} kcna_kind;
+
+/* Distance screening forms for the local join and the P2K join. */
+typedef enum {
+    KCNA_SCREEN_FP32 = 0, /* plain FP32, the drop-in */
+    KCNA_SCREEN_BF16 = 1  /* BF16 tensor-core Gram screen + FP32 re-rank of survivors */
+} kcna_screen;
+
+/* Build parameters.  Field meaning and defaults follow kgraph::KGraph::IndexParams
+ * (src/kgraph.h:116-170, defaults :12-40) and the CLI flags (src/fastnsg.cpp:53-94). */
+typedef struct {
+    uint32_t K;          /* -K, default 25 */
+    uint32_t L;          /* -L, default 100 */
+    uint32_t S;          /* -S, default 10 */
+    uint32_t R;          /* -R, default 100 */
+    uint32_t iterations; /* -I, default 30 */
+    uint32_t controls;   /* --controls, default 100 */
+    uint32_t seed;       /* --seed, default 2024 */
+    uint32_t nthreads;   /* --nthreads (host threads of CPU helpers) */
+    float delta;         /* --delta, default 0.002 */
+    float recall;        /* --recall, default 0.95 */
+    uint32_t nsg_R;      /* --nsg_R, default 50 */
+    uint32_t search_L;   /* --search_L, default 40 */
+    uint32_t search_K;   /* --search_K, default 500 */
+    uint32_t step;       /* --step, default 10 */
+    uint32_t massq_S;    /* --massq_S, default 10 */
+    uint32_t loop_i;     /* --loop_i, default 2 */
+    float tau;           /* --tau, default 0 */
+    float angle;         /* --angle (degrees), default 60 */
+    /* GB300 extensions (no counterpart in the reference) */
+    uint32_t screen;     /* kcna_screen */
+    uint32_t learned_seed; /* 1: seed NN-descent from learned codes (kcna_seed_learned) */
+    uint32_t verbosity;  /* 0 silent, 1 per-phase lines on stderr */
+    uint32_t reserved[5];
+} kcna_params;
+
+/* Fills p with the reference defaults (src/kgraph.h:12-40). */
+void kcna_params_default(kcna_params *p);
+
+/* Statistics of one build.  Key names follow the reference's run CSV
+ * (SaveResult, src/kgraph.cpp:1725-1807) and IndexInfo (src/kgraph.h:186-198). */
+#define KCNA_MAX_ITERS 64
+#define KCNA_MAX_LOOPS 16
+typedef struct {
+    uint32_t iterations;       /* NN-descent iterations run */
+    uint32_t stop_condition;   /* 0 ITERATION, 1 DELTA, 2 RECALL (IndexInfo::StopCondition) */
+    uint32_t maxl;             /* candidate pool size MAXL = max(L,K,search_L,search_K) */
+    uint32_t loops;            /* prune/P2K loops run (loop_i+1) */
+    float iter_recall[KCNA_MAX_ITERS]; /* control recall@K after each join */
+    float iter_delta[KCNA_MAX_ITERS];
+    double iter_time[KCNA_MAX_ITERS];  /* seconds since build start ("kgraph time") */
+    uint64_t iter_cand_overflow[KCNA_MAX_ITERS]; /* candidates dropped by full buffers */
+    float loop_recall[KCNA_MAX_LOOPS + 1]; /* evaluate(): control recall@MAXL, [0] after NN-descent */
+    double prune_time[KCNA_MAX_LOOPS];
+    double inter_time[KCNA_MAX_LOOPS];
+    double tree_grow_time[KCNA_MAX_LOOPS];
+    double buildnsg_time[KCNA_MAX_LOOPS];
+    double search_time[KCNA_MAX_LOOPS];   /* P2K (BridgeView) seconds per loop */
+    double con_time[KCNA_MAX_LOOPS];      /* seconds since start after each loop */
+    double nndescent_time;
+    double total_time;
+    uint64_t n_comps;          /* NN-descent join distance evaluations (kgraph.cpp:1116) */
+    uint64_t prune_comps;      /* prune distance evaluations */
+    uint64_t bridge_comps;     /* P2K join distance evaluations */
+    uint64_t screened_pairs;   /* pairs screened in BF16 (0 in FP32 mode) */
+    uint64_t rescored_pairs;   /* screened pairs recomputed in FP32 */
+    uint32_t ep;               /* entry point */
+    uint32_t width;            /* max out-degree */
+    uint32_t aod;              /* average out-degree (CalculateNSG, :2273-2293) */
+    uint32_t min_degree, max_degree;
+    uint32_t reserved[3];
+} kcna_stats;
+
+typedef struct kcna_ctx kcna_ctx;
+
+/* Context on CUDA device `device`.  Replaces KGraph::create (src/kgraph.cpp:3968-3971). */
+kcna_status kcna_create(kcna_ctx **out, int device);
+void kcna_destroy(kcna_ctx *ctx);
+const char *kcna_last_error(const kcna_ctx *ctx);
+const char *kcna_version(void); /* replaces KGraph::version (src/kgraph.cpp:3973) */
+
+/* Copies n rows of d floats (row pitch stride_bytes) from HOST memory into the
+ * context.  Replaces constructing MatrixOracle over a Matrix<float>
+ * (src/kgraph-data.h:349-384; src/fastnsg.cpp:193). */
+kcna_status kcna_upload(kcna_ctx *ctx, const float *rows, uint32_t n, uint32_t d, uint64_t stride_bytes);
+/* Same, from DEVICE memory of the context's device (no host copy). */
+kcna_status kcna_upload_device(kcna_ctx *ctx, const float *dev_rows, uint32_t n, uint32_t d, uint64_t stride_bytes);
+/* Restricts every following call to the first n_prefix rows.
+ * Replaces IndexOracle::set_size (src/kgraph.h:80, src/kgraph-data.h:372-382). */
+kcna_status kcna_set_size(kcna_ctx *ctx, uint32_t n_prefix);
+
+/* Exact k-NN of m base rows (ids) against all rows, self excluded; ties broken by
+ * lower id.  Replaces LinearSearch (src/kgraph.cpp:309-330).  Host outputs m*k. */
+kcna_status kcna_knn_exact(kcna_ctx *ctx, const uint32_t *ids, uint32_t m, uint32_t k,
+                           uint32_t *out_ids, float *out_dists);
+/* Exact k-NN of m host query vectors (pitch q_stride_bytes) against all rows.
+ * Replaces SearchOracle::search (src/kgraph.cpp:332-361). */
+kcna_status kcna_knn_queries(kcna_ctx *ctx, const float *queries, uint32_t m, uint64_t q_stride_bytes,
+                             uint32_t k, uint32_t *out_ids, float *out_dists);
+
+/* Full build of one graph kind: NN-descent, then loop_i+1 rounds of
+ * {prune+link, entry point, [tree_grow], UpdateNhoods, [P2K refinement]}.
+ * Replaces KGraph::buildFastNSG / buildFastTauMNG / buildFastAlphaPG
+ * (src/kgraph.h:230-232; src/kgraph.cpp:3796-3966) and the per-layer part of
+ * buildFastHNSW (src/kgraph.h:233; src/kgraph.cpp:3720-3795). */
+kcna_status kcna_build(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind, kcna_stats *stats);
+
+/* NN-descent only (the KGraphConstructor constructor, src/kgraph.cpp:1281-1459),
+ * leaving the pools in the context. */
+kcna_status kcna_nndescent(kcna_ctx *ctx, const kcna_params *params, kcna_stats *stats);
+
+/* Graph after a build: ids is n*width (rows padded with 0xFFFFFFFF), degrees n.
+ * Pass NULL ids to query width only.  Replaces reading nn_nsg as SaveNsg does
+ * (src/kgraph.cpp:1704-1724) and SwapPGraph (:2296-2311). */
+kcna_status kcna_get_graph(kcna_ctx *ctx, uint32_t *ids, uint32_t *degrees, uint32_t *ep, uint32_t *width);
+
+/* Candidate pools (sorted by distance): ids/dists n*cap, counts n.  cap must be
+ * >= the pool capacity reported by kcna_pool_capacity. */
+kcna_status kcna_pool_capacity(kcna_ctx *ctx, uint32_t *cap);
+kcna_status kcna_get_pools(kcna_ctx *ctx, uint32_t *ids, float *dists, uint32_t *counts, uint32_t cap);
+/* Installs caller pools (each sorted ascending by distance, no duplicate ids)
+ * so that prune/link can be run on an identical input KNN graph. */
+kcna_status kcna_set_pools(kcna_ctx *ctx, const kcna_params *params, const uint32_t *ids, const float *dists,
+                           const uint32_t *counts, uint32_t cap);
+
+/* Occlusion prune of every pool into the graph (kind NSG/HNSW_LAYER: RNG,
+ * TAUMNG: tau, ALPHAPG: angle).  Replaces nsg_sync_prune (src/kgraph.cpp:1809-1851),
+ * taumg_sync_prune (:2833-2876) and alphapg_sync_prune (:3157-3203). */
+kcna_status kcna_prune(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind);
+/* Prune + reverse-edge insert + re-prune of over-full nodes.  Replaces
+ * nsg_Link / taumg_Link / alphapg_Link (src/kgraph.cpp:2087-2143, 3085-3141, 3424-3480). */
+kcna_status kcna_link(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind);
+/* Installs a caller graph (ids n*width padded with 0xFFFFFFFF, degrees n). */
+kcna_status kcna_set_graph(kcna_ctx *ctx, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep);
+
+/* Greedy beam search of m host queries over the context graph, beam width L,
+ * starting from init_ids (m*L host ids, or NULL: entry point + its graph
+ * neighbours).  Outputs the best k (m*k).  Replaces get_neighbors
+ * (src/kgraph.cpp:1560-1623) and serves the query-time recall@10 evaluator. */
+kcna_status kcna_search(kcna_ctx *ctx, const float *queries, uint32_t m, uint64_t q_stride_bytes,
+                        const uint32_t *init_ids, uint32_t L, uint32_t k,
+                        uint32_t *out_ids, float *out_dists);
+
+/* Number of kernels this context has launched so far. */
+uint64_t kcna_kernel_launches(const kcna_ctx *ctx);
+
+/* Writes the graph in the NSG/efanna format written by SaveNsg
+ * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */
+kcna_status kcna_write_nsg(kcna_ctx *ctx, const char *path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KCNA_H */

@@ -1,0 +1,276 @@
+// ref_harness.cpp - TEST INFRASTRUCTURE, not product code.
+//
+// Compiles the reference's own src/kgraph.cpp, unmodified, into this
+// translation unit (read from the reference tree by oracle/build_ref.sh,
+// never copied into this repository) against the self-written Boost-subset
+// shim in oracle/compat, and exposes its build-path functions through a small
+// C interface so that tests can pin the oracle restatement
+// (oracle/kcna_oracle.cpp) and generate golden fixtures from the reference
+// itself.  `class` is defined to `struct` around the include only to give this
+// harness access to KGraphConstructor's internals (pools, nn_nsg lists).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <limits>
+#include <malloc.h>
+#include <mutex>
+#include <queue>
+#include <random>
+#include <stack>
+#include <stdexcept>
+#include <unordered_set>
+#include <vector>
+#include <sys/resource.h>
+#include <omp.h>
+#include <boost/timer/timer.hpp>
+#include <boost/progress.hpp>
+#include <boost/dynamic_bitset.hpp>
+#include <boost/accumulators/accumulators.hpp>
+#include <boost/accumulators/statistics/stats.hpp>
+#include <boost/accumulators/statistics/mean.hpp>
+#include <boost/accumulators/statistics/moment.hpp>
+#include <boost/smart_ptr/detail/spinlock.hpp>
+#include <boost/assert.hpp>
+
+#define class struct
+#include "kgraph.cpp"
+#undef class
+#include "kgraph-data.h"
+
+#include "kcna.h"
+
+using namespace kgraph;
+typedef MatrixOracle<float, metric::l2sqr> RefOracle;
+
+namespace {
+
+struct Quiet { // the reference prints progress to stdout; silence it in tests
+    std::streambuf *old;
+    Quiet() : old(std::cout.rdbuf(nullptr)) {}
+    ~Quiet() { std::cout.rdbuf(old); }
+};
+
+void fill(Matrix<float> &M, const float *X, uint64_t stride, unsigned n, unsigned d) {
+    M.resize(n, d);
+    M.zero();
+    for (unsigned i = 0; i < n; ++i) std::memcpy(M[i], X + (uint64_t)i * stride, sizeof(float) * d);
+}
+
+KGraph::IndexParams to_params(const kcna_params *p) {
+    KGraph::IndexParams q;
+    q.K = p->K;
+    q.L = p->L;
+    q.S = p->S;
+    q.R = p->R;
+    q.iterations = p->iterations;
+    q.controls = p->controls;
+    q.seed = p->seed;
+    q.nthreads = p->nthreads;
+    q.delta = p->delta;
+    q.recall = p->recall;
+    q.nsg_R = p->nsg_R;
+    q.search_L = p->search_L;
+    q.search_K = p->search_K;
+    q.step = p->step;
+    q.massq_S = p->massq_S;
+    q.loop_i = p->loop_i;
+    q.tau = p->tau;
+    q.angle = p->angle;
+    q.prune = 0;
+    q.reverse = 0;
+    return q;
+}
+
+// A constructor that runs no NN-descent iteration: used to hold given pools.
+KGraphConstructor *empty_constructor(RefOracle &O, const kcna_params *p, const uint32_t *pid, const float *pd,
+                                     const uint32_t *pcnt, uint32_t cap) {
+    KGraph::IndexParams q = to_params(p);
+    q.iterations = 0;
+    q.controls = 1;
+    KGraph::IndexInfo info;
+    KGraphConstructor *con = new KGraphConstructor(O, q, &info);
+    con->init_nhoods();
+    unsigned n = O.size();
+    for (unsigned i = 0; i < n && pid; ++i) {
+        auto &h = con->nhoods[i];
+        h.pool.assign(std::max<size_t>(h.pool.size(), cap + 1), Neighbor());
+        h.L = std::min<unsigned>(pcnt[i], cap);
+        for (unsigned j = 0; j < h.L; ++j) {
+            Neighbor nb(pid[(uint64_t)i * cap + j], pd[(uint64_t)i * cap + j], false);
+            h.pool[j] = nb;
+        }
+    }
+    return con;
+}
+
+void store_graph(KGraphConstructor *con, unsigned n, uint32_t *out_ids, float *out_d, uint32_t *out_deg,
+                 uint32_t width) {
+    for (unsigned i = 0; i < n; ++i) {
+        auto &g = con->nhoods[i].nn_nsg;
+        out_deg[i] = (uint32_t)g.size();
+        for (uint32_t j = 0; j < width; ++j) {
+            out_ids[(uint64_t)i * width + j] = j < g.size() ? g[j].id : 0xFFFFFFFFu;
+            if (out_d) out_d[(uint64_t)i * width + j] = j < g.size() ? g[j].dist : 0.f;
+        }
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+float kref_l2(const float *a, const float *b, uint32_t d) { return metric::l2sqr::apply<float>(a, b, d); }
+
+int kref_linear_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, const uint32_t *ids, uint32_t m,
+                       uint32_t k, uint32_t *out_ids, float *out_d) {
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < (int)m; ++i) {
+        std::vector<Neighbor> nns;
+        LinearSearch(O, ids[i], k, &nns);
+        for (uint32_t j = 0; j < k; ++j) {
+            out_ids[(uint64_t)i * k + j] = nns[j].id;
+            out_d[(uint64_t)i * k + j] = nns[j].dist;
+        }
+    }
+    return 0;
+}
+
+int kref_nndescent(const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p, int nthreads,
+                   uint32_t *pool_ids, float *pool_d, uint32_t *pool_cnt, uint32_t cap, float *iter_recall,
+                   uint32_t *iters, float *final_recall) {
+    Quiet quiet;
+    omp_set_num_threads(nthreads);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraph::IndexParams q = to_params(p);
+    KGraph::IndexInfo info;
+    KGraphConstructor con(O, q, &info);
+    *iters = (uint32_t)con.allrecall.size();
+    for (size_t i = 0; i < con.allrecall.size() && i < KCNA_MAX_ITERS; ++i) iter_recall[i] = con.allrecall[i];
+    *final_recall = con.evaluate();
+    for (unsigned i = 0; i < n && pool_ids; ++i) {
+        auto &h = con.nhoods[i];
+        pool_cnt[i] = std::min<uint32_t>(h.L, cap);
+        for (unsigned j = 0; j < cap; ++j) {
+            pool_ids[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].id : 0xFFFFFFFFu;
+            pool_d[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].dist : INFINITY;
+        }
+    }
+    return 0;
+}
+
+int kref_prune(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p,
+               const uint32_t *pid, const float *pd, const uint32_t *pcnt, uint32_t cap, uint32_t *out_ids,
+               float *out_d, uint32_t *out_deg, uint32_t width) {
+    Quiet quiet;
+    omp_set_num_threads(1);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraphConstructor *con = empty_constructor(O, p, pid, pd, pcnt, cap);
+    for (unsigned q = 0; q < n; ++q) {
+        if (kind == KCNA_TAUMNG)
+            con->taumg_sync_prune(q);
+        else if (kind == KCNA_ALPHAPG)
+            con->alphapg_sync_prune(q);
+        else
+            con->nsg_sync_prune(q);
+    }
+    store_graph(con, n, out_ids, out_d, out_deg, width);
+    delete con;
+    return 0;
+}
+
+int kref_link(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p,
+              const uint32_t *pid, const float *pd, const uint32_t *pcnt, uint32_t cap, uint32_t *out_ids,
+              float *out_d, uint32_t *out_deg, uint32_t width) {
+    Quiet quiet;
+    omp_set_num_threads(1);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraphConstructor *con = empty_constructor(O, p, pid, pd, pcnt, cap);
+    con->pruneAgain.resize(n);
+    con->pruneAgain.set();
+    if (kind == KCNA_TAUMNG)
+        con->taumg_Link();
+    else if (kind == KCNA_ALPHAPG)
+        con->alphapg_Link();
+    else
+        con->nsg_Link();
+    store_graph(con, n, out_ids, out_d, out_deg, width);
+    delete con;
+    return 0;
+}
+
+int kref_beam_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, const uint32_t *g_ids,
+                     const uint32_t *g_deg, uint32_t width, const float *Q, uint64_t qstride, uint32_t m,
+                     const uint32_t *init_ids, uint32_t L, uint32_t k, uint32_t *out_ids, float *out_d) {
+    Quiet quiet;
+    omp_set_num_threads(1);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    kcna_params p;
+    std::memset(&p, 0, sizeof p);
+    p.K = p.L = p.search_K = std::max<uint32_t>(L, 2);
+    p.S = 1;
+    p.search_L = L;
+    p.nsg_R = width;
+    KGraphConstructor *con = empty_constructor(O, &p, nullptr, nullptr, nullptr, 0);
+    for (unsigned i = 0; i < n; ++i) {
+        con->nhoods[i].nn_nsg.clear();
+        for (unsigned j = 0; j < std::min(g_deg[i], width); ++j)
+            con->nhoods[i].nn_nsg.push_back(Neighbor(g_ids[(uint64_t)i * width + j], 0.f, false));
+    }
+    auto &seed_pool = con->nhoods[0].pool;
+    if (seed_pool.size() < L + 1) seed_pool.resize(L + 1);
+    for (uint32_t i = 0; i < m; ++i) {
+        for (uint32_t j = 0; j < L; ++j) seed_pool[j].id = init_ids[(uint64_t)i * L + j];
+        std::vector<Neighbor> pool;
+        con->get_neighbors(Q + (uint64_t)i * qstride, 0, L, pool);
+        for (uint32_t j = 0; j < k; ++j) {
+            out_ids[(uint64_t)i * k + j] = pool[j].id;
+            out_d[(uint64_t)i * k + j] = pool[j].dist;
+        }
+    }
+    delete con;
+    return 0;
+}
+
+// Full reference build through its public API (KGraph::create + buildFast*),
+// writing the NSG-format index and the run CSV to the given paths.
+int kref_build(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p, int nthreads,
+               const char *index_path, const char *csv_path, int quiet) {
+    std::streambuf *old = quiet ? std::cout.rdbuf(nullptr) : nullptr;
+    omp_set_num_threads(nthreads);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraph::IndexParams q = to_params(p);
+    KGraph::IndexInfo info;
+    KGraph *kg = KGraph::create();
+    if (kind == KCNA_TAUMNG)
+        kg->buildFastTauMNG(O, q, &info, index_path, csv_path);
+    else if (kind == KCNA_ALPHAPG)
+        kg->buildFastAlphaPG(O, q, &info, index_path, csv_path);
+    else
+        kg->buildFastNSG(O, q, &info, index_path, csv_path);
+    delete kg;
+    if (quiet) std::cout.rdbuf(old);
+    return 0;
+}
+
+} // extern "C"
