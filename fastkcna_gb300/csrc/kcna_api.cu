@@ -1,0 +1,578 @@
+// kcna_api.cu - C ABI, context and build driver of the GB300 FastKCNA library.
+//
+// The build driver follows KGraphImpl::buildFastNSG / buildFastTauMNG /
+// buildFastAlphaPG (src/kgraph.cpp:3796-3966) and the per-layer part of
+// buildFastHNSW (:3720-3795): NN-descent, evaluate, then loop_i+1 rounds of
+// {link, ComputeEp, [tree_grow], UpdateNhoods} with a P2K refinement
+// (BridgeView) and evaluate between rounds.  All compute runs in the CUDA
+// kernels of kcna_knn.cu, kcna_nnd.cu and kcna_graph.cu; the host only
+// sequences phases, reads counters and moves data across the boundary.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <random>
+#include <set>
+#include <vector>
+
+#include "kcna_internal.h"
+
+#ifndef KCNA_VERSION_STRING
+#define KCNA_VERSION_STRING "kcna-gb300 0.1 (sm_103a)"
+#endif
+
+double kcna_now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+kcna_status kcna_fail(kcna_ctx *c, kcna_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+kcna_status kcna_cuda_check(kcna_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return KCNA_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return kcna_fail(c, KCNA_E_OOM, m);
+    return kcna_fail(c, KCNA_E_CUDA, m);
+}
+
+kcna_status kcna_check_device_err(kcna_ctx *c, const char *phase) {
+    int h = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->d_err, 4, cudaMemcpyDeviceToHost, c->stream), "err d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "err sync"));
+    if (h == 0) return KCNA_OK;
+    cudaMemsetAsync(c->d_err, 0, 4, c->stream);
+    cudaStreamSynchronize(c->stream);
+    const char *what = h == 1 ? "index outside its buffer (access skipped)"
+                       : h == 2 ? "bounded wait gave up"
+                       : h == 3 ? "graph row ran out of slots"
+                                : "unknown";
+    return kcna_fail(c, h == 2 ? KCNA_E_TIMEOUT : KCNA_E_CUDA, std::string(phase) + ": device error: " + what);
+}
+
+static kcna_status grow(kcna_ctx *c, void **p, size_t *cur, size_t bytes) {
+    if (*cur >= bytes && *p) return KCNA_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cur = 0;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        *p = nullptr;
+        return kcna_fail(c, KCNA_E_OOM, "scratch allocation failed");
+    }
+    *cur = bytes;
+    return KCNA_OK;
+}
+kcna_status kcna_scratch(kcna_ctx *c, size_t bytes, void **out) {
+    KCNA_TRY(grow(c, &c->scratch, &c->scratch_bytes, bytes));
+    *out = c->scratch;
+    return KCNA_OK;
+}
+kcna_status kcna_scratch2(kcna_ctx *c, size_t bytes, void **out) {
+    KCNA_TRY(grow(c, &c->scratch2, &c->scratch2_bytes, bytes));
+    *out = c->scratch2;
+    return KCNA_OK;
+}
+
+void kcna_log(kcna_ctx *c, const kcna_params *p, const char *fmt, ...) {
+    (void)c;
+    if (!p || !p->verbosity) return;
+    va_list ap;
+    va_start(ap, fmt);
+    fprintf(stderr, "[kcna] ");
+    vfprintf(stderr, fmt, ap);
+    fprintf(stderr, "\n");
+    va_end(ap);
+}
+
+static void free_state(kcna_ctx *c) {
+    void *bufs[] = {c->pool, c->pool_cnt, c->radius, c->M, c->radiusM, c->found, c->fwd_new, c->fwd_new_cnt,
+                    c->fwd_old, c->fwd_old_cnt, c->rnew, c->rnew_cnt, c->rold, c->rold_cnt, c->cand, c->cand_cnt,
+                    c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
+                    c->d_control_knn};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    c->pool = nullptr;
+    c->pool_cnt = nullptr;
+    c->radius = nullptr;
+    c->M = nullptr;
+    c->radiusM = nullptr;
+    c->found = nullptr;
+    c->fwd_new = c->fwd_new_cnt = c->fwd_old = c->fwd_old_cnt = nullptr;
+    c->rnew = c->rnew_cnt = c->rold = c->rold_cnt = nullptr;
+    c->cand = nullptr;
+    c->cand_cnt = nullptr;
+    c->g_ids = c->g_deg = c->g_old = c->g_old_deg = nullptr;
+    c->g_dist = nullptr;
+    c->g_isnew = nullptr;
+    c->d_controls = c->d_control_knn = nullptr;
+    c->W = 0;
+    c->cap = 0;
+    c->has_graph = c->has_pools = false;
+}
+
+static kcna_status bind(kcna_ctx *c) { return kcna_cuda_check(c, cudaSetDevice(c->device), "cudaSetDevice"); }
+
+extern "C" {
+
+void kcna_params_default(kcna_params *p) {
+    memset(p, 0, sizeof *p);
+    p->K = 25;
+    p->L = 100;
+    p->S = 10;
+    p->R = 100;
+    p->iterations = 30;
+    p->controls = 100;
+    p->seed = 2024;
+    p->nthreads = 40;
+    p->delta = 0.002f;
+    p->recall = 0.95f;
+    p->nsg_R = 50;
+    p->search_L = 40;
+    p->search_K = 500;
+    p->step = 10;
+    p->massq_S = 10;
+    p->loop_i = 2;
+    p->tau = 0.f;
+    p->angle = 60.f;
+}
+
+const char *kcna_version(void) { return KCNA_VERSION_STRING; }
+
+kcna_status kcna_create(kcna_ctx **out, int device) {
+    if (!out) return KCNA_E_ARG;
+    *out = nullptr;
+    kcna_ctx *c = new kcna_ctx();
+    c->device = device;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || device < 0 || device >= count) {
+        (void)cudaGetLastError();
+        delete c;
+        return KCNA_E_CUDA;
+    }
+    kcna_status s = bind(c);
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device), "attr");
+    if (s == KCNA_OK) s = kcna_alloc(c, &c->d_err, 1, "error word");
+    if (s == KCNA_OK) s = kcna_alloc(c, &c->counters, 64, "counters");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaMemset(c->d_err, 0, 4), "memset");
+    if (s != KCNA_OK) {
+        kcna_destroy(c);
+        return s;
+    }
+    *out = c;
+    return KCNA_OK;
+}
+
+void kcna_destroy(kcna_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_state(c);
+    if (c->X) cudaFree(c->X);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->scratch2) cudaFree(c->scratch2);
+    if (c->d_err) cudaFree(c->d_err);
+    if (c->counters) cudaFree(c->counters);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *kcna_last_error(const kcna_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+uint64_t kcna_kernel_launches(const kcna_ctx *c) { return c ? c->launches : 0; }
+
+static kcna_status upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d, uint64_t stride, cudaMemcpyKind kind) {
+    if (!c) return KCNA_E_ARG;
+    if (!rows || n < 2 || d == 0 || stride < (uint64_t)d * 4 || n > KCNA_MAX_ID)
+        return kcna_fail(c, KCNA_E_ARG, "upload: need rows, n >= 2, d >= 1, stride >= 4*d, n < 2^30");
+    KCNA_TRY(bind(c));
+    free_state(c);
+    if (c->X) cudaFree(c->X);
+    c->X = nullptr;
+    c->d = d;
+    c->ld = (d + 3) & ~3u;
+    c->n_total = c->n = n;
+    KCNA_TRY(kcna_alloc(c, &c->X, (size_t)n * c->ld, "rows"));
+    if (c->ld != d) KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->X, 0, (size_t)n * c->ld * 4, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpy2DAsync(c->X, (size_t)c->ld * 4, rows, stride, (size_t)d * 4, n, kind, c->stream),
+                             "upload copy"));
+    return kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "upload sync");
+}
+
+kcna_status kcna_upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d, uint64_t stride_bytes) {
+    return upload(c, rows, n, d, stride_bytes, cudaMemcpyHostToDevice);
+}
+kcna_status kcna_upload_device(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d, uint64_t stride_bytes) {
+    return upload(c, rows, n, d, stride_bytes, cudaMemcpyDeviceToDevice);
+}
+
+kcna_status kcna_set_size(kcna_ctx *c, uint32_t n_prefix) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "set_size: no rows");
+    if (n_prefix < 2) return kcna_fail(c, KCNA_E_ARG, "set_size: need at least 2 rows");
+    KCNA_TRY(bind(c));
+    free_state(c);
+    c->n = std::min(n_prefix, c->n_total); // IndexOracle::set_size clamps (src/kgraph-data.h:372-382)
+    return KCNA_OK;
+}
+
+static kcna_status to_device_rows(kcna_ctx *c, const float *q, uint32_t m, uint64_t stride, float **out) {
+    float *dq = nullptr;
+    KCNA_TRY(kcna_alloc(c, &dq, (size_t)m * c->ld, "query rows"));
+    kcna_status s = KCNA_OK;
+    if (c->ld != c->d) s = kcna_cuda_check(c, cudaMemsetAsync(dq, 0, (size_t)m * c->ld * 4, c->stream), "memset");
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpy2DAsync(dq, (size_t)c->ld * 4, q, stride, (size_t)c->d * 4, m,
+                                                 cudaMemcpyHostToDevice, c->stream),
+                            "query copy");
+    if (s != KCNA_OK) {
+        cudaFree(dq);
+        return s;
+    }
+    *out = dq;
+    return KCNA_OK;
+}
+
+kcna_status kcna_knn_exact(kcna_ctx *c, const uint32_t *ids, uint32_t m, uint32_t k, uint32_t *out_ids,
+                           float *out_dists) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "knn_exact: no rows");
+    if (!ids || !out_ids || !out_dists || m == 0) return kcna_fail(c, KCNA_E_ARG, "knn_exact: null argument");
+    for (uint32_t i = 0; i < m; ++i)
+        if (ids[i] >= c->n) return kcna_fail(c, KCNA_E_ARG, "knn_exact: id out of range");
+    KCNA_TRY(bind(c));
+    uint32_t *did = nullptr, *oid = nullptr;
+    float *rows = nullptr, *od = nullptr;
+    kcna_status s = kcna_alloc(c, &did, m, "ids");
+    if (s == KCNA_OK) s = kcna_alloc(c, &rows, (size_t)m * c->ld, "rows");
+    if (s == KCNA_OK) s = kcna_alloc(c, &oid, (size_t)m * k, "out ids");
+    if (s == KCNA_OK) s = kcna_alloc(c, &od, (size_t)m * k, "out dists");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaMemcpyAsync(did, ids, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    if (s == KCNA_OK) s = kcna_gather_rows(c, did, m, rows);
+    if (s == KCNA_OK) s = kcna_knn_device(c, rows, m, did, k, oid, od);
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_ids, oid, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "knn sync");
+    cudaFree(did);
+    cudaFree(rows);
+    cudaFree(oid);
+    cudaFree(od);
+    return s == KCNA_OK ? kcna_check_device_err(c, "knn_exact") : s;
+}
+
+kcna_status kcna_knn_queries(kcna_ctx *c, const float *queries, uint32_t m, uint64_t q_stride, uint32_t k,
+                             uint32_t *out_ids, float *out_dists) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "knn_queries: no rows");
+    if (!queries || !out_ids || !out_dists || m == 0 || q_stride < (uint64_t)c->d * 4)
+        return kcna_fail(c, KCNA_E_ARG, "knn_queries: bad argument");
+    KCNA_TRY(bind(c));
+    float *dq = nullptr, *od = nullptr;
+    uint32_t *oid = nullptr;
+    kcna_status s = to_device_rows(c, queries, m, q_stride, &dq);
+    if (s == KCNA_OK) s = kcna_alloc(c, &oid, (size_t)m * k, "out ids");
+    if (s == KCNA_OK) s = kcna_alloc(c, &od, (size_t)m * k, "out dists");
+    if (s == KCNA_OK) s = kcna_knn_device(c, dq, m, nullptr, k, oid, od);
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_ids, oid, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "knn sync");
+    cudaFree(dq);
+    cudaFree(oid);
+    cudaFree(od);
+    return s == KCNA_OK ? kcna_check_device_err(c, "knn_queries") : s;
+}
+
+kcna_status kcna_nndescent(kcna_ctx *c, const kcna_params *p, kcna_stats *st) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "nndescent: no rows");
+    if (!p) return kcna_fail(c, KCNA_E_ARG, "nndescent: null params");
+    KCNA_TRY(bind(c));
+    kcna_stats local;
+    if (!st) st = &local;
+    memset(st, 0, sizeof *st);
+    free_state(c);
+    c->t0 = kcna_now();
+    KCNA_TRY(kcna_nndescent_run(c, p, st));
+    float r = 0;
+    KCNA_TRY(kcna_control_recall(c, c->cap, &r));
+    st->loop_recall[0] = r;
+    st->nndescent_time = kcna_now() - c->t0;
+    st->total_time = st->nndescent_time;
+    return kcna_check_device_err(c, "nndescent");
+}
+
+static kcna_status degree_stats(kcna_ctx *c, kcna_stats *st) {
+    std::vector<uint32_t> deg(c->n);
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(deg.data(), c->g_deg, (size_t)c->n * 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));
+    uint64_t sum = 0;
+    uint32_t mx = 0, mn = ~0u;
+    for (uint32_t d : deg) {
+        sum += d;
+        mx = std::max(mx, d);
+        mn = std::min(mn, d);
+    }
+    c->width = mx;
+    st->width = mx;
+    st->max_degree = mx;
+    st->min_degree = mn;
+    st->aod = (uint32_t)(sum / std::max<uint32_t>(1, c->n)); // CalculateNSG (src/kgraph.cpp:2273-2293)
+    st->ep = c->ep;
+    return KCNA_OK;
+}
+
+kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_stats *st) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "build: no rows");
+    if (!p) return kcna_fail(c, KCNA_E_ARG, "build: null params");
+    if (kind != KCNA_NSG && kind != KCNA_HNSW_LAYER && kind != KCNA_TAUMNG && kind != KCNA_ALPHAPG)
+        return kcna_fail(c, KCNA_E_ARG, "build: unknown kind");
+    KCNA_TRY(bind(c));
+    kcna_stats local;
+    if (!st) st = &local;
+    memset(st, 0, sizeof *st);
+    free_state(c);
+    c->t0 = kcna_now();
+    kcna_params P = *p;
+    KCNA_TRY(kcna_nndescent_run(c, &P, st));
+    const uint32_t maxl = c->cap;
+    if (c->n <= P.K) P.loop_i = 0; // clamping of src/kgraph.cpp:1320-1327
+    float r = 0;
+    KCNA_TRY(kcna_control_recall(c, maxl, &r));
+    st->loop_recall[0] = r;
+    st->nndescent_time = kcna_now() - c->t0;
+    kcna_log(c, &P, "nndescent done: recall@MAXL %.4f t %.3f", r, st->nndescent_time);
+    KCNA_TRY(kcna_graph_alloc(c, P.nsg_R + 8));
+    KCNA_TRY(kcna_pools_set_radius(c, maxl)); // init_nhoods: pools grow to MAXL (:1462-1496)
+    uint64_t prune_comps = 0, bridge_comps = 0;
+    int loopcount = 0;
+    const uint32_t iters = P.loop_i + 1;
+    for (uint32_t iter = 1; iter <= iters; ++iter) {
+        double a = kcna_now();
+        uint64_t pc = 0;
+        KCNA_TRY(kcna_link_all(c, &P, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &pc));
+        prune_comps += pc;
+        double b = kcna_now();
+        KCNA_TRY(kcna_compute_ep(c, &P, (uint64_t)P.seed * 1000003ull + iter));
+        double e = kcna_now();
+        if (kind != KCNA_HNSW_LAYER) KCNA_TRY(kcna_tree_grow(c, &P, (uint64_t)P.seed * 7919ull + iter));
+        double f = kcna_now();
+        KCNA_TRY(kcna_update_nhoods(c, loopcount));
+        KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "loop sync"));
+        if (loopcount < KCNA_MAX_LOOPS) {
+            st->prune_time[loopcount] = b - a;
+            st->inter_time[loopcount] = 0;
+            st->tree_grow_time[loopcount] = f - e;
+            st->buildnsg_time[loopcount] = kcna_now() - a;
+            st->con_time[loopcount] = kcna_now() - c->t0;
+        }
+        kcna_log(c, &P, "loop %u: link %.3f ep %.3f tree_grow %.3f", iter, b - a, e - b, f - e);
+        loopcount++;
+        if (iter == iters) break;
+        double s0 = kcna_now();
+        uint64_t bc = 0;
+        KCNA_TRY(kcna_bridge_view(c, &P, maxl, loopcount, &bc));
+        bridge_comps += bc;
+        KCNA_TRY(kcna_control_recall(c, maxl, &r));
+        if (loopcount - 1 < KCNA_MAX_LOOPS) st->search_time[loopcount - 1] = kcna_now() - s0;
+        if (loopcount <= KCNA_MAX_LOOPS) st->loop_recall[loopcount] = r;
+        kcna_log(c, &P, "P2K %d: recall@MAXL %.4f t %.3f", loopcount, r, kcna_now() - s0);
+    }
+    st->loops = (uint32_t)loopcount;
+    st->prune_comps = prune_comps;
+    st->bridge_comps = bridge_comps;
+    KCNA_TRY(degree_stats(c, st));
+    st->total_time = kcna_now() - c->t0;
+    return kcna_check_device_err(c, "build");
+}
+
+kcna_status kcna_get_graph(kcna_ctx *c, uint32_t *ids, uint32_t *degrees, uint32_t *ep, uint32_t *width) {
+    if (!c || !c->has_graph) return kcna_fail(c, KCNA_E_STATE, "get_graph: no graph");
+    KCNA_TRY(bind(c));
+    if (width) *width = c->W;
+    if (ep) *ep = c->ep;
+    if (ids)
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(ids, c->g_ids, (size_t)c->n * c->W * 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    if (degrees)
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(degrees, c->g_deg, (size_t)c->n * 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    return kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "get_graph sync");
+}
+
+kcna_status kcna_pool_capacity(kcna_ctx *c, uint32_t *cap) {
+    if (!c || !c->has_pools) return kcna_fail(c, KCNA_E_STATE, "no pools");
+    *cap = c->cap;
+    return KCNA_OK;
+}
+
+kcna_status kcna_get_pools(kcna_ctx *c, uint32_t *ids, float *dists, uint32_t *counts, uint32_t cap) {
+    if (!c || !c->has_pools) return kcna_fail(c, KCNA_E_STATE, "get_pools: no pools");
+    if (cap < c->cap) return kcna_fail(c, KCNA_E_ARG, "get_pools: cap below the pool capacity");
+    KCNA_TRY(bind(c));
+    std::vector<uint64_t> keys((size_t)c->n * c->cap);
+    std::vector<uint32_t> cnt(c->n);
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(keys.data(), c->pool, keys.size() * 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(cnt.data(), c->pool_cnt, (size_t)c->n * 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));
+    for (uint32_t i = 0; i < c->n; ++i) {
+        uint32_t k = std::min(cnt[i], c->cap);
+        if (counts) counts[i] = k;
+        for (uint32_t j = 0; j < cap; ++j) {
+            uint64_t key = j < k ? keys[(size_t)i * c->cap + j] : KCNA_EMPTY_KEY_H;
+            if (ids) ids[(size_t)i * cap + j] = j < k ? (uint32_t)(key & 0xFFFFFFFFull) >> 2 : 0xFFFFFFFFu;
+            if (dists) {
+                uint32_t bits = (uint32_t)(key >> 32);
+                float f;
+                memcpy(&f, &bits, 4);
+                dists[(size_t)i * cap + j] = j < k ? f : INFINITY;
+            }
+        }
+    }
+    return KCNA_OK;
+}
+
+kcna_status kcna_set_pools(kcna_ctx *c, const kcna_params *p, const uint32_t *ids, const float *dists,
+                           const uint32_t *counts, uint32_t cap) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "set_pools: no rows");
+    if (!p || !ids || !dists || !counts || cap == 0) return kcna_fail(c, KCNA_E_ARG, "set_pools: null argument");
+    KCNA_TRY(bind(c));
+    free_state(c);
+    const uint32_t maxl = std::max(std::max(std::max(p->L, p->K), std::max(p->search_L, p->search_K)), cap);
+    if (maxl > 1024) return kcna_fail(c, KCNA_E_ARG, "set_pools: capacity above 1024");
+    c->cap = maxl;
+    std::vector<uint64_t> keys((size_t)c->n * maxl, KCNA_EMPTY_KEY_H);
+    std::vector<uint32_t> cnt(c->n);
+    for (uint32_t i = 0; i < c->n; ++i) {
+        uint32_t k = std::min(counts[i], cap);
+        cnt[i] = k;
+        for (uint32_t j = 0; j < k; ++j) {
+            uint32_t id = ids[(size_t)i * cap + j];
+            if (id >= c->n) return kcna_fail(c, KCNA_E_ARG, "set_pools: id out of range");
+            float f = dists[(size_t)i * cap + j];
+            uint32_t bits;
+            memcpy(&bits, &f, 4);
+            keys[(size_t)i * maxl + j] = ((uint64_t)bits << 32) | ((uint64_t)id << 2);
+        }
+    }
+    KCNA_TRY(kcna_alloc(c, &c->pool, keys.size(), "pool"));
+    KCNA_TRY(kcna_alloc(c, &c->pool_cnt, c->n, "pool_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->radius, c->n, "radius"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->pool, keys.data(), keys.size() * 8, cudaMemcpyHostToDevice, c->stream), "h2d"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->pool_cnt, cnt.data(), (size_t)c->n * 4, cudaMemcpyHostToDevice, c->stream), "h2d"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));
+    c->has_pools = true;
+    return kcna_pools_set_radius(c, maxl);
+}
+
+kcna_status kcna_prune(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
+    if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "prune: null argument");
+    KCNA_TRY(bind(c));
+    uint64_t comps = 0;
+    KCNA_TRY(kcna_prune_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
+    return kcna_check_device_err(c, "prune");
+}
+
+kcna_status kcna_link(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
+    if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "link: null argument");
+    KCNA_TRY(bind(c));
+    uint64_t comps = 0;
+    KCNA_TRY(kcna_link_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
+    return kcna_check_device_err(c, "link");
+}
+
+kcna_status kcna_set_graph(kcna_ctx *c, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep) {
+    if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "set_graph: no rows");
+    if (!ids || !degrees || width == 0 || width > 4096 || ep >= c->n) return kcna_fail(c, KCNA_E_ARG, "set_graph: bad argument");
+    KCNA_TRY(bind(c));
+    for (uint32_t i = 0; i < c->n; ++i)
+        if (degrees[i] > width) return kcna_fail(c, KCNA_E_ARG, "set_graph: degree above width");
+    if (c->W != width) {
+        c->W = 0;
+        if (c->g_ids) {
+            cudaFree(c->g_ids);
+            c->g_ids = nullptr;
+        }
+    }
+    KCNA_TRY(kcna_graph_alloc(c, width));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->g_ids, ids, (size_t)c->n * width * 4, cudaMemcpyHostToDevice, c->stream), "h2d"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->g_deg, degrees, (size_t)c->n * 4, cudaMemcpyHostToDevice, c->stream), "h2d"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));
+    c->ep = ep;
+    c->has_graph = true;
+    return KCNA_OK;
+}
+
+kcna_status kcna_search(kcna_ctx *c, const float *queries, uint32_t m, uint64_t q_stride, const uint32_t *init_ids,
+                        uint32_t L, uint32_t k, uint32_t *out_ids, float *out_dists) {
+    if (!c || !c->has_graph) return kcna_fail(c, KCNA_E_STATE, "search: no graph");
+    if (!queries || !out_ids || !out_dists || m == 0 || q_stride < (uint64_t)c->d * 4)
+        return kcna_fail(c, KCNA_E_ARG, "search: bad argument");
+    if (L == 0 || L > std::min<uint32_t>(2048, c->n) || k == 0 || k > L)
+        return kcna_fail(c, KCNA_E_ARG, "search: need 0 < k <= L <= min(2048, n)");
+    KCNA_TRY(bind(c));
+    std::vector<uint32_t> init;
+    if (init_ids) {
+        init.assign(init_ids, init_ids + (size_t)m * L);
+    } else {
+        // entry point, its graph neighbours, then seeded random distinct ids
+        std::vector<uint32_t> row(c->W), one;
+        uint32_t dg = 0;
+        cudaMemcpy(row.data(), c->g_ids + (size_t)c->ep * c->W, c->W * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&dg, c->g_deg + c->ep, 4, cudaMemcpyDeviceToHost);
+        std::set<uint32_t> seen;
+        one.push_back(c->ep);
+        seen.insert(c->ep);
+        for (uint32_t j = 0; j < std::min(dg, c->W) && one.size() < L; ++j)
+            if (row[j] < c->n && seen.insert(row[j]).second) one.push_back(row[j]);
+        std::mt19937 rng(2024);
+        while (one.size() < L) {
+            uint32_t id = rng() % c->n;
+            if (seen.insert(id).second) one.push_back(id);
+        }
+        init.resize((size_t)m * L);
+        for (uint32_t i = 0; i < m; ++i) std::copy(one.begin(), one.end(), init.begin() + (size_t)i * L);
+    }
+    float *dq = nullptr, *od = nullptr;
+    uint32_t *di = nullptr, *oid = nullptr;
+    kcna_status s = to_device_rows(c, queries, m, q_stride, &dq);
+    if (s == KCNA_OK) s = kcna_alloc(c, &di, init.size(), "init ids");
+    if (s == KCNA_OK) s = kcna_alloc(c, &oid, (size_t)m * k, "out ids");
+    if (s == KCNA_OK) s = kcna_alloc(c, &od, (size_t)m * k, "out dists");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaMemcpyAsync(di, init.data(), init.size() * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    if (s == KCNA_OK) s = kcna_search_device(c, dq, m, di, L, k, oid, od);
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_ids, oid, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "search sync");
+    cudaFree(dq);
+    cudaFree(di);
+    cudaFree(oid);
+    cudaFree(od);
+    return s == KCNA_OK ? kcna_check_device_err(c, "search") : s;
+}
+
+kcna_status kcna_write_nsg(kcna_ctx *c, const char *path) {
+    if (!c || !c->has_graph) return kcna_fail(c, KCNA_E_STATE, "write_nsg: no graph");
+    if (!path) return kcna_fail(c, KCNA_E_ARG, "write_nsg: null path");
+    std::vector<uint32_t> ids((size_t)c->n * c->W), deg(c->n);
+    uint32_t ep = 0, W = 0;
+    KCNA_TRY(kcna_get_graph(c, ids.data(), deg.data(), &ep, &W));
+    uint32_t width = 0;
+    for (uint32_t d : deg) width = std::max(width, d);
+    FILE *f = fopen(path, "wb");
+    if (!f) return kcna_fail(c, KCNA_E_IO, std::string("write_nsg: cannot open ") + path);
+    bool ok = fwrite(&width, 4, 1, f) == 1 && fwrite(&ep, 4, 1, f) == 1;
+    for (uint32_t i = 0; ok && i < c->n; ++i) {
+        uint32_t gk = std::min(deg[i], W);
+        ok = fwrite(&gk, 4, 1, f) == 1 && (gk == 0 || fwrite(ids.data() + (size_t)i * W, 4, gk, f) == gk);
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? KCNA_OK : kcna_fail(c, KCNA_E_IO, std::string("write_nsg: write failed for ") + path);
+}
+
+} // extern "C"

@@ -1,0 +1,1152 @@
+// kcna_graph.cu - occlusion prune, link, entry point, connectivity, P2K
+// refinement and beam search on the GPU.
+//
+// Reference functions replaced (src/kgraph.cpp):
+//   nsg_sync_prune :1809-1851, taumg_sync_prune :2833-2876,
+//   alphapg_sync_prune :3157-3203          -> prune_kernel (warp per node)
+//   InterInsert :2051-2084 + *_reversed_prune :2012-2048/:3038-3083/:3374-3422
+//   inside nsg_Link :2087-2143 (and the tau / angle twins) -> link kernels
+//   ComputeEp :1528-1536, Calcenter (src/kgraph-data.h:413-428),
+//   get_neighbors :1560-1623               -> centroid + beam_search_kernel
+//   tree_grow :2145-2172, findroot :2174-2236, DFS :2238-2270 -> BFS + attach
+//   UpdateNhoods :3537-3584                -> update_nhoods_kernel
+//   BridgeView :2478-2663                  -> bridge_* kernels + the shared merge
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <set>
+
+#include "kcna_internal.h"
+#include "kcna_sort.cuh"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264;
+
+struct PruneRule {
+    int kind;
+    float t3;  // 3 * tau (FP32, src/kgraph.cpp:2859)
+    float thr; // cos(angle) as the reference computes it (src/kgraph.cpp:3161)
+};
+
+// Occlusion of candidate p (distance pd to the node) by kept t (distance td to
+// the node) at distance djk between them.
+__device__ __forceinline__ bool occludes(const PruneRule &r, float td, float djk, float pd) {
+    if (r.kind == KCNA_TAUMNG) return djk < __fsub_rn(pd, r.t3);
+    if (r.kind == KCNA_ALPHAPG) {
+        float num = __fdiv_rn(__fsub_rn(__fadd_rn(td, djk), pd), 2.0f);
+        float cs = __fdiv_rn(num, __fsqrt_rn(__fmul_rn(td, djk)));
+        return djk < pd && cs < r.thr;
+    }
+    return djk < pd;
+}
+
+// Prune of one candidate list by one warp.  cand ids/dists are read through
+// get(i); the kept list (ids, dists) lives in shared memory.  Candidates are
+// taken 32 at a time: each lane tests its candidate against the kept list, then
+// the batch is resolved in order (the first unoccluded lane is kept and tests
+// the later lanes), which gives exactly the sequential result.
+template <typename GetFn>
+__device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle, const PruneRule &rule,
+                          uint32_t self, int first, int lim, int range, GetFn get, uint32_t *kid, float *kd,
+                          unsigned long long *comps) {
+    const int lane = kcna_lane();
+    if (first >= lim || range <= 0) return 0;
+    int nk = 0;
+    {
+        uint32_t id0;
+        float d0;
+        get(first, id0, d0);
+        if (lane == 0) {
+            kid[0] = id0;
+            kd[0] = d0;
+        }
+        nk = 1;
+    }
+    __syncwarp();
+    unsigned long long cc = 0;
+    for (int base = first + 1; base < lim && nk < range; base += 32) {
+        const int i = base + lane;
+        uint32_t id = KCNA_NONE;
+        float pd = 0.f;
+        bool live = false;
+        if (i < lim) {
+            get(i, id, pd);
+            live = id < n_oracle; // src/kgraph.cpp:1822 `if (p.id >= oracle.size()) continue;`
+        }
+        const float *prow = X + (uint64_t)(live ? id : 0) * ld;
+        bool occ = false;
+        if (live) {
+            for (int t = 0; t < nk; ++t) {
+                uint32_t tid = kid[t];
+                if (tid == id) {
+                    occ = true;
+                    break;
+                }
+                ++cc;
+                float djk = kcna_l2_ldg(X + (uint64_t)tid * ld, prow, ld);
+                if (occludes(rule, kd[t], djk, pd)) {
+                    occ = true;
+                    break;
+                }
+            }
+        }
+        unsigned rem = __ballot_sync(KCNA_FULL, live && !occ);
+        while (rem && nk < range) {
+            const int a = __ffs(rem) - 1;
+            const uint32_t aid = __shfl_sync(KCNA_FULL, id, a);
+            const float ad = __shfl_sync(KCNA_FULL, pd, a);
+            if (lane == 0) {
+                kid[nk] = aid;
+                kd[nk] = ad;
+            }
+            ++nk;
+            __syncwarp();
+            rem &= ~((2u << a) - 1u); // lanes after a
+            bool mine = (rem >> lane) & 1u;
+            bool o2 = false;
+            if (mine) {
+                if (aid == id) {
+                    o2 = true;
+                } else {
+                    ++cc;
+                    float djk = kcna_l2_ldg(X + (uint64_t)aid * ld, prow, ld);
+                    o2 = occludes(rule, ad, djk, pd);
+                }
+            }
+            rem &= ~__ballot_sync(KCNA_FULL, o2);
+        }
+    }
+    cc = kcna_warp_sum(cc);
+    if (lane == 0 && comps && cc) atomicAdd(comps, cc);
+    __syncwarp();
+    return nk;
+}
+
+constexpr int PW = 4; // warps per prune block
+
+__global__ void __launch_bounds__(PW * 32) prune_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                        const uint64_t *__restrict__ pool,
+                                                        const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                                        PruneRule rule, int range, int maxc, uint32_t *__restrict__ g_ids,
+                                                        float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
+                                                        uint32_t W, unsigned long long *comps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    uint32_t *kid = reinterpret_cast<uint32_t *>(smem) + w * 2 * range;
+    float *kd = reinterpret_cast<float *>(kid + range);
+    const uint32_t q = blockIdx.x * PW + w;
+    if (q >= N) return;
+    const uint64_t *pr = pool + (uint64_t)q * cap;
+    const int cnt = (int)pool_cnt[q];
+    int first = 0;
+    if (cnt > 0 && kcna_key_id(pr[0]) == q) first = 1;
+    const int lim = min(cnt, maxc);
+    auto get = [&](int i, uint32_t &id, float &dd) {
+        uint64_t k = pr[i];
+        id = kcna_key_id(k);
+        dd = kcna_key_dist(k);
+    };
+    int nk = (first < cnt) ? warp_prune(X, ld, N, rule, q, first, max(lim, first + 1), range, get, kid, kd, comps) : 0;
+    for (int j = lane; j < (int)W; j += 32) {
+        g_ids[(uint64_t)q * W + j] = j < nk ? kid[j] : KCNA_NONE;
+        g_dist[(uint64_t)q * W + j] = j < nk ? kd[j] : 0.f;
+    }
+    if (lane == 0) g_deg[q] = nk;
+}
+
+// ---- link: reverse edges -------------------------------------------------
+__global__ void rev_count_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg, uint32_t N,
+                                 uint32_t W, uint32_t *__restrict__ indeg) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)N * W) return;
+    uint32_t n = (uint32_t)(t / W), j = (uint32_t)(t % W);
+    if (j >= g_deg[n]) return;
+    uint32_t des = g_ids[t];
+    if (des < N) atomicAdd(indeg + des, 1u);
+}
+__global__ void rev_fill_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg, uint32_t N,
+                                uint32_t W, const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                                uint32_t *__restrict__ rev) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)N * W) return;
+    uint32_t n = (uint32_t)(t / W), j = (uint32_t)(t % W);
+    if (j >= g_deg[n]) return;
+    uint32_t des = g_ids[t];
+    if (des >= N) return;
+    uint32_t p = atomicAdd(cursor + des, 1u);
+    rev[off[des] + p] = n;
+}
+
+// exclusive scan of u32 counts into u64 offsets (3 phases)
+constexpr int SCAN_T = 1024, SCAN_E = 4;
+__global__ void scan_block_sums(const uint32_t *__restrict__ in, uint64_t n, uint64_t *__restrict__ sums) {
+    __shared__ uint64_t s[SCAN_T / 32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_T * SCAN_E;
+    uint64_t v = 0;
+    for (int e = 0; e < SCAN_E; ++e) {
+        uint64_t i = base + (uint64_t)e * SCAN_T + threadIdx.x;
+        if (i < n) v += in[i];
+    }
+    v = kcna_warp_sum(v);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (int i = 0; i < SCAN_T / 32; ++i) t += s[i];
+        sums[blockIdx.x] = t;
+    }
+}
+__global__ void scan_sums_serial(uint64_t *sums, uint32_t nb, uint64_t *total) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint64_t run = 0;
+    for (uint32_t i = 0; i < nb; ++i) {
+        uint64_t t = sums[i];
+        sums[i] = run;
+        run += t;
+    }
+    *total = run;
+}
+__global__ void scan_apply(const uint32_t *__restrict__ in, uint64_t n, const uint64_t *__restrict__ sums,
+                           uint64_t *__restrict__ out) {
+    __shared__ uint64_t s[SCAN_T];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_T * SCAN_E;
+    uint64_t run = sums[blockIdx.x];
+    for (int e = 0; e < SCAN_E; ++e) {
+        uint64_t i = base + (uint64_t)e * SCAN_T + threadIdx.x;
+        uint64_t v = i < n ? in[i] : 0;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < SCAN_T; o <<= 1) {
+            uint64_t u = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
+            __syncthreads();
+            s[threadIdx.x] += u;
+            __syncthreads();
+        }
+        if (i < n) out[i] = run + s[threadIdx.x] - v;
+        uint64_t tot = s[SCAN_T - 1];
+        __syncthreads();
+        run += tot;
+    }
+}
+
+// Per node: pruned list + reverse sources (sorted by id, not already present),
+// then the reversed prune when the list exceeds range.
+constexpr int LT = 128;
+constexpr int LCAP = 4096; // merged-list capacity per node in shared memory
+
+__global__ void __launch_bounds__(LT) link_merge_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                       PruneRule rule, int range, uint32_t *__restrict__ g_ids,
+                                                       float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
+                                                       uint32_t W, const uint64_t *__restrict__ off,
+                                                       const uint32_t *__restrict__ rev,
+                                                       unsigned long long *comps, int *err) {
+    __shared__ uint64_t s_key[LCAP];   // sorting keys (rev ids; later (dist, position))
+    __shared__ uint32_t s_id[LCAP];
+    __shared__ float s_d[LCAP];
+    __shared__ uint32_t s_kid[128];
+    __shared__ float s_kd[128];
+    __shared__ uint32_t s_warp[LT / 32];
+    __shared__ int s_nk;
+    const uint32_t q = blockIdx.x;
+    const int deg = (int)g_deg[q];
+    const uint64_t r0 = off[q], r1 = off[q + 1];
+    const uint64_t room = (uint64_t)(LCAP - deg);
+    int nin = (int)((r1 - r0) < room ? (r1 - r0) : room);
+    if ((uint64_t)nin < r1 - r0) kcna_set_err(err, KCNA_DERR_BOUNDS);
+    // pruned entries first, in order
+    for (int j = threadIdx.x; j < deg; j += LT) {
+        s_id[j] = g_ids[(uint64_t)q * W + j];
+        s_d[j] = g_dist[(uint64_t)q * W + j];
+    }
+    // reverse sources sorted by id
+    const int np2 = kcna_pow2_ceil_d(max(nin, 1));
+    for (int j = threadIdx.x; j < np2; j += LT) s_key[j] = j < nin ? (uint64_t)rev[r0 + j] : KCNA_EMPTY_KEY;
+    kcna_cta_bitonic(s_key, np2);
+    // keep sources not in the pruned list (InterInsert dup check, :2064-2071)
+    int keep_local = 0;
+    const int per = (nin + LT - 1) / LT;
+    const int b = threadIdx.x * per;
+    uint32_t flags = 0;
+    for (int e = 0; e < per && b + e < nin; ++e) {
+        uint32_t src = (uint32_t)s_key[b + e];
+        bool dup = false;
+        for (int j = 0; j < deg; ++j)
+            if (s_id[j] == src) {
+                dup = true;
+                break;
+            }
+        if (!dup) {
+            flags |= 1u << e;
+            ++keep_local;
+        }
+    }
+    // block exclusive scan of keep counts
+    int incl = keep_local;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(KCNA_FULL, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < LT / 32; ++i) {
+            uint32_t t = s_warp[i];
+            s_warp[i] = run;
+            run += t;
+        }
+        s_nk = (int)run;
+    }
+    __syncthreads();
+    int pos = deg + (int)s_warp[w] + incl - keep_local;
+    for (int e = 0; e < per && b + e < nin; ++e)
+        if (flags & (1u << e)) {
+            uint32_t src = (uint32_t)s_key[b + e];
+            s_id[pos] = src;
+            s_d[pos] = kcna_l2_ldg(X + (uint64_t)src * ld, X + (uint64_t)q * ld, ld); // oracle(n, des)
+            ++pos;
+        }
+    const int total = deg + s_nk;
+    __syncthreads();
+    if (total <= range) {
+        for (int j = threadIdx.x; j < (int)W; j += LT) {
+            g_ids[(uint64_t)q * W + j] = j < total ? s_id[j] : KCNA_NONE;
+            g_dist[(uint64_t)q * W + j] = j < total ? s_d[j] : 0.f;
+        }
+        if (threadIdx.x == 0) g_deg[q] = total;
+        return;
+    }
+    // reversed prune: stable sort by distance, then the occlusion scan without the search_K cap
+    const int tp = kcna_pow2_ceil_d(total);
+    for (int j = threadIdx.x; j < tp; j += LT)
+        s_key[j] = j < total ? (((uint64_t)__float_as_uint(s_d[j]) << 32) | (uint32_t)j) : KCNA_EMPTY_KEY;
+    kcna_cta_bitonic(s_key, tp);
+    if (threadIdx.x < 32) {
+        auto get = [&](int i, uint32_t &id, float &dd) {
+            uint32_t p = (uint32_t)s_key[i];
+            id = s_id[p];
+            dd = s_d[p];
+        };
+        int first = 0;
+        {
+            uint32_t id0;
+            float d0;
+            get(0, id0, d0);
+            if (id0 == q) first = 1;
+        }
+        int nk = warp_prune(X, ld, 0xFFFFFFFFu, rule, q, first, total, range, get, s_kid, s_kd, comps);
+        for (int j = lane; j < (int)W; j += 32) {
+            g_ids[(uint64_t)q * W + j] = j < nk ? s_kid[j] : KCNA_NONE;
+            g_dist[(uint64_t)q * W + j] = j < nk ? s_kd[j] : 0.f;
+        }
+        if (lane == 0) g_deg[q] = nk;
+    }
+}
+
+// ---- entry point: centroid + beam search --------------------------------
+constexpr int CB_ROWS = 1024;
+__global__ void centroid_partial_kernel(const float *__restrict__ X, int ld, uint32_t n, int d,
+                                        double *__restrict__ part) {
+    const uint32_t r0 = blockIdx.x * CB_ROWS, r1 = min(n, r0 + CB_ROWS);
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+        double s = 0;
+        for (uint32_t r = r0; r < r1; ++r) s += X[(uint64_t)r * ld + j];
+        part[(uint64_t)blockIdx.x * d + j] = s;
+    }
+}
+__global__ void centroid_final_kernel(const double *__restrict__ part, uint32_t nb, int d, int ld, uint32_t n,
+                                      float *__restrict__ center) {
+    for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+        double s = 0;
+        for (uint32_t b = 0; b < nb; ++b) s += j < d ? part[(uint64_t)b * d + j] : 0.0;
+        center[j] = j < d ? (float)(s / n) : 0.f;
+    }
+}
+
+// Beam search of one query per warp (get_neighbors semantics).  Pool of L+1
+// keys in shared memory; bit 0 of a key = not yet expanded.  visited: one
+// bitmap of N bits per resident warp slot in global memory.
+constexpr int BW = 4;
+
+// InsertIntoPool (src/kgraph.cpp:261-298) on keys ordered by distance only.
+__device__ int pool_insert_pos(const uint64_t *pool, int K, float dist, uint32_t id) {
+    int left = 0, right = K - 1;
+    if (kcna_key_dist(pool[left]) > dist) return -1; // insert at 0
+    if (kcna_key_dist(pool[right]) < dist) return K; // append
+    while (left < right - 1) {
+        int mid = (left + right) / 2;
+        if (kcna_key_dist(pool[mid]) > dist)
+            right = mid;
+        else
+            left = mid;
+    }
+    while (left > 0) {
+        if (kcna_key_dist(pool[left]) < dist) break;
+        if (kcna_key_id(pool[left]) == id) return K + 1;
+        left--;
+    }
+    if (kcna_key_id(pool[left]) == id || kcna_key_id(pool[right]) == id) return K + 1;
+    return right;
+}
+
+__global__ void __launch_bounds__(BW * 32) beam_search_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                              const uint32_t *__restrict__ g_ids,
+                                                              const uint32_t *__restrict__ g_deg, uint32_t W,
+                                                              const float *__restrict__ Q, uint32_t m,
+                                                              const uint32_t *__restrict__ init_ids, int L, int k,
+                                                              uint32_t *__restrict__ visited, uint32_t vwords,
+                                                              uint32_t *__restrict__ out_ids,
+                                                              float *__restrict__ out_d) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    uint64_t *pool = reinterpret_cast<uint64_t *>(smem) + (uint64_t)w * (L + 1);
+    const uint32_t slot = blockIdx.x * BW + w;
+    uint32_t *vis = visited + (uint64_t)slot * vwords;
+    const uint32_t nslots = gridDim.x * BW;
+    for (uint32_t qi = slot; qi < m; qi += nslots) {
+        for (uint32_t i = lane; i < vwords; i += 32) vis[i] = 0;
+        __syncwarp();
+        const float *qrow = Q + (uint64_t)qi * ld;
+        const uint32_t *init = init_ids + (uint64_t)qi * L;
+        // init: mark, compute, sort
+        for (int i = lane; i < L; i += 32) {
+            uint32_t id = init[i];
+            if (id < N) atomicOr(vis + (id >> 5), 1u << (id & 31));
+        }
+        __syncwarp();
+        int Lc = 0;
+        for (int b0 = 0; b0 < L; b0 += 32) {
+            int i = b0 + lane;
+            uint32_t id = i < L ? init[i] : KCNA_NONE;
+            bool ok = id < N;
+            uint64_t key = KCNA_EMPTY_KEY;
+            if (ok) key = kcna_key(kcna_l2_ldg(qrow, X + (uint64_t)id * ld, ld), id, 1u);
+            unsigned mk = __ballot_sync(KCNA_FULL, ok);
+            if (ok) pool[Lc + __popc(mk & kcna_lanemask_lt())] = key;
+            Lc += __popc(mk);
+        }
+        const int p2 = kcna_pow2_ceil_d(max(Lc, 1));
+        // sort pool[0..Lc) (pad into the free slots beyond L with care: use a local sort)
+        if (p2 <= L + 1) {
+            for (int i = Lc + lane; i < p2; i += 32) pool[i] = KCNA_EMPTY_KEY;
+            kcna_warp_bitonic(pool, p2);
+        } else if (lane == 0) { // insertion sort (Lc > (L+1)/2 and not a power of two)
+            for (int i = 1; i < Lc; ++i) {
+                uint64_t v = pool[i];
+                int j = i - 1;
+                while (j >= 0 && pool[j] > v) {
+                    pool[j + 1] = pool[j];
+                    --j;
+                }
+                pool[j + 1] = v;
+            }
+        }
+        __syncwarp();
+        int kk = 0;
+        while (kk < Lc) {
+            int nk = Lc;
+            uint64_t cur = pool[kk];
+            if (cur & 1ull) {
+                __syncwarp();
+                if (lane == 0) pool[kk] = cur & ~1ull;
+                __syncwarp();
+                const uint32_t nid = kcna_key_id(cur);
+                const int deg = (int)min(g_deg[nid], W);
+                for (int b0 = 0; b0 < deg; b0 += 32) {
+                    int j = b0 + lane;
+                    uint32_t id = j < deg ? g_ids[(uint64_t)nid * W + j] : KCNA_NONE;
+                    bool fresh = false;
+                    if (id < N) {
+                        uint32_t old = atomicOr(vis + (id >> 5), 1u << (id & 31));
+                        fresh = !(old & (1u << (id & 31)));
+                    }
+                    float dist = fresh ? kcna_l2_ldg(qrow, X + (uint64_t)id * ld, ld) : 0.f;
+                    unsigned mk = __ballot_sync(KCNA_FULL, fresh);
+                    // apply in neighbour order, as the reference does
+                    while (mk) {
+                        int src = __ffs(mk) - 1;
+                        mk &= mk - 1;
+                        uint32_t cid = __shfl_sync(KCNA_FULL, id, src);
+                        float cd = __shfl_sync(KCNA_FULL, dist, src);
+                        if (cd >= kcna_key_dist(pool[Lc - 1])) continue;
+                        int r = 0;
+                        if (lane == 0) r = pool_insert_pos(pool, Lc, cd, cid);
+                        r = __shfl_sync(KCNA_FULL, r, 0);
+                        if (r == Lc + 1) continue; // duplicate: InsertIntoPool returns K+1, L still grows below
+                        int at = r < 0 ? 0 : r;
+                        __syncwarp();
+                        if (lane == 0) {
+                            for (int t = Lc; t > at; --t) pool[t] = pool[t - 1];
+                            pool[at] = kcna_key(cd, cid, 1u);
+                        }
+                        __syncwarp();
+                        if (Lc < L) ++Lc;
+                        if (at < nk) nk = at;
+                    }
+                }
+            }
+            if (nk <= kk)
+                kk = nk;
+            else
+                ++kk;
+        }
+        for (int i = lane; i < k; i += 32) {
+            uint64_t key = i < Lc ? pool[i] : KCNA_EMPTY_KEY;
+            out_ids[(uint64_t)qi * k + i] = i < Lc ? kcna_key_id(key) : KCNA_NONE;
+            out_d[(uint64_t)qi * k + i] = i < Lc ? kcna_key_dist(key) : __uint_as_float(0x7F800000u);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- tree_grow: BFS reachability + attach --------------------------------
+__global__ void bfs_expand_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg, uint32_t W,
+                                  uint32_t N, const uint32_t *__restrict__ frontier, uint32_t nf,
+                                  uint32_t *__restrict__ visited, uint32_t *__restrict__ next,
+                                  uint32_t *__restrict__ next_cnt) {
+    const uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (wi >= nf) return;
+    const uint32_t u = frontier[wi];
+    const int deg = (int)min(g_deg[u], W);
+    for (int j = lane; j < deg; j += 32) {
+        uint32_t v = g_ids[(uint64_t)u * W + j];
+        if (v >= N) continue;
+        uint32_t old = atomicOr(visited + (v >> 5), 1u << (v & 31));
+        if (!(old & (1u << (v & 31)))) next[atomicAdd(next_cnt, 1u)] = v;
+    }
+}
+
+// Attach loop in one block: smallest unreached id u; first reached node r in
+// u's pool with degree < nsg_R (else a random reached node with degree <
+// nsg_R * factor); edge r -> u; block-level BFS from u.  Every round visits
+// at least u, so the loop ends after at most N rounds.
+constexpr int AT = 1024;
+__global__ void __launch_bounds__(AT) attach_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                    const uint64_t *__restrict__ pool,
+                                                    const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                                    uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
+                                                    uint32_t *__restrict__ g_deg, uint32_t W, uint32_t nsg_R,
+                                                    uint32_t *__restrict__ visited, uint32_t *__restrict__ qa,
+                                                    uint32_t *__restrict__ qb, uint64_t seed, int *err,
+                                                    unsigned long long *attached) {
+    __shared__ uint32_t s_u, s_root, s_na, s_nb;
+    __shared__ int s_found;
+    const uint32_t words = (N + 31) / 32;
+    uint32_t start_word = 0;
+    for (uint32_t round = 0; round < N; ++round) {
+        // smallest unreached id
+        if (threadIdx.x == 0) s_u = KCNA_NONE;
+        __syncthreads();
+        for (uint32_t wbase = start_word; wbase < words; wbase += AT) {
+            uint32_t wd = wbase + threadIdx.x;
+            if (wd < words) {
+                uint32_t v = visited[wd];
+                uint32_t valid = (wd == words - 1 && (N & 31)) ? ((1u << (N & 31)) - 1u) : 0xFFFFFFFFu;
+                uint32_t miss = ~v & valid;
+                if (miss) atomicMin(&s_u, wd * 32 + (__ffs(miss) - 1));
+            }
+            __syncthreads();
+            if (s_u != KCNA_NONE) break;
+            __syncthreads();
+        }
+        const uint32_t u = s_u;
+        if (u == KCNA_NONE) return;
+        start_word = u >> 5;
+        // attach point: first reached pool entry of u with degree < nsg_R
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            const uint32_t cnt = pool_cnt[u];
+            uint32_t root = KCNA_NONE;
+            for (uint32_t b0 = 0; b0 < cnt && root == KCNA_NONE; b0 += 32) {
+                uint32_t i = b0 + lane;
+                bool ok = false;
+                uint32_t cid = 0;
+                if (i < cnt) {
+                    cid = kcna_key_id(pool[(uint64_t)u * cap + i]);
+                    ok = cid < N && ((visited[cid >> 5] >> (cid & 31)) & 1u) && g_deg[cid] < nsg_R;
+                }
+                unsigned mk = __ballot_sync(KCNA_FULL, ok);
+                if (mk) root = __shfl_sync(KCNA_FULL, cid, __ffs(mk) - 1);
+            }
+            if (lane == 0) {
+                if (root == KCNA_NONE) { // random reached node, src/kgraph.cpp:2216-2230
+                    for (uint64_t t = 1; t <= 64ull * N + 64; ++t) {
+                        uint32_t factor = (uint32_t)(t / N) + 1;
+                        uint32_t rid = kcna_rand32(seed, u, t) % N;
+                        if (((visited[rid >> 5] >> (rid & 31)) & 1u) && g_deg[rid] < nsg_R * factor) {
+                            root = rid;
+                            break;
+                        }
+                    }
+                }
+                s_found = root != KCNA_NONE;
+                s_root = root;
+                if (root != KCNA_NONE) {
+                    uint32_t dg = g_deg[root];
+                    if (dg < W) {
+                        g_ids[(uint64_t)root * W + dg] = u;
+                        g_dist[(uint64_t)root * W + dg] = kcna_l2(X + (uint64_t)root * ld, X + (uint64_t)u * ld, ld);
+                        g_deg[root] = dg + 1;
+                    } else {
+                        kcna_set_err(err, KCNA_DERR_DEGREE);
+                    }
+                    atomicAdd(attached, 1ull);
+                } else {
+                    kcna_set_err(err, KCNA_DERR_SPIN);
+                }
+                visited[u >> 5] |= 1u << (u & 31);
+                qa[0] = u;
+                s_na = 1;
+            }
+        }
+        __syncthreads();
+        if (!s_found) return;
+        // block BFS from u
+        uint32_t *cur = qa, *nxt = qb;
+        while (s_na > 0) {
+            if (threadIdx.x == 0) s_nb = 0;
+            __syncthreads();
+            const uint32_t na = s_na;
+            for (uint32_t t = threadIdx.x; t < na * 64u; t += AT) {
+                uint32_t f = t / 64u, j = t % 64u;
+                uint32_t x = cur[f];
+                if (j >= min(g_deg[x], W)) continue;
+                uint32_t v = g_ids[(uint64_t)x * W + j];
+                if (v >= N) continue;
+                uint32_t old = atomicOr(visited + (v >> 5), 1u << (v & 31));
+                if (!(old & (1u << (v & 31)))) nxt[atomicAdd(&s_nb, 1u)] = v;
+            }
+            // degrees above 64: second pass
+            for (uint32_t t = threadIdx.x; t < na; t += AT) {
+                uint32_t x = cur[t];
+                for (uint32_t j = 64; j < min(g_deg[x], W); ++j) {
+                    uint32_t v = g_ids[(uint64_t)x * W + j];
+                    if (v >= N) continue;
+                    uint32_t old = atomicOr(visited + (v >> 5), 1u << (v & 31));
+                    if (!(old & (1u << (v & 31)))) nxt[atomicAdd(&s_nb, 1u)] = v;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) s_na = s_nb;
+            uint32_t *tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void degree_stats_kernel(const uint32_t *__restrict__ g_deg, uint32_t N, unsigned long long *out) {
+    // out[0] sum, out[1] max, out[2] min
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    uint32_t d = g_deg[i];
+    atomicAdd(out + 0, (unsigned long long)d);
+    atomicMax(out + 1, (unsigned long long)d);
+    atomicMin(out + 2, (unsigned long long)d);
+}
+
+// ---- UpdateNhoods ---------------------------------------------------------
+__global__ void update_nhoods_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg,
+                                     uint32_t *__restrict__ g_old, uint32_t *__restrict__ g_old_deg,
+                                     uint8_t *__restrict__ g_isnew, uint32_t N, uint32_t W, int first) {
+    const uint32_t n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (n >= N) return;
+    const uint32_t deg = min(g_deg[n], W), odeg = first ? 0 : min(g_old_deg[n], W);
+    const uint32_t *cur = g_ids + (uint64_t)n * W;
+    uint32_t *old = g_old + (uint64_t)n * W;
+    uint8_t flags[2] = {1, 1};
+    uint32_t mine[2] = {KCNA_NONE, KCNA_NONE};
+    for (int h = 0; h < 2; ++h) {
+        uint32_t j = lane + 32 * h;
+        if (j < deg) {
+            mine[h] = cur[j];
+            bool found = false;
+            for (uint32_t t = 0; t < odeg; ++t)
+                if (old[t] == mine[h]) {
+                    found = true;
+                    break;
+                }
+            flags[h] = (first || !found) ? 1 : 0;
+        }
+    }
+    for (uint32_t j = 64 + lane; j < deg; j += 32) { // rows wider than 64
+        uint32_t id = cur[j];
+        bool found = false;
+        for (uint32_t t = 0; t < odeg; ++t)
+            if (old[t] == id) {
+                found = true;
+                break;
+            }
+        g_isnew[(uint64_t)n * W + j] = (first || !found) ? 1 : 0;
+    }
+    __syncwarp();
+    for (int h = 0; h < 2; ++h) {
+        uint32_t j = lane + 32 * h;
+        if (j < deg) g_isnew[(uint64_t)n * W + j] = flags[h];
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < W; j += 32) old[j] = j < deg ? cur[j] : KCNA_NONE;
+    if (lane == 0) g_old_deg[n] = deg;
+}
+
+// ---- BridgeView (P2K) -----------------------------------------------------
+__global__ void bridge_init_kernel(uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                   uint32_t N, int cur_loop, uint32_t pre_L, uint32_t cur_L) {
+    const uint32_t n = blockIdx.x;
+    const uint32_t cnt = pool_cnt[n];
+    uint64_t *pr = pool + (uint64_t)n * cap;
+    for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+        uint64_t k = pr[j] & ~3ull;
+        uint64_t f = pr[j] & KCNA_FLAG_NEW;
+        if (cur_loop == 0 || j < pre_L || j >= cur_L)
+            k |= KCNA_FLAG_NEW; // flag=true, isnew=false
+        else
+            k |= KCNA_FLAG_NEW | (f ? KCNA_FLAG_ISNEW : 0ull); // isnew = previous flag
+        pr[j] = k;
+    }
+}
+
+// count (pass 0) or emit (pass 1) the pushes of one update round
+__global__ void bridge_update_kernel(uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                     uint32_t N, uint32_t Lp, uint32_t S_, int capped, int emit,
+                                     uint32_t *__restrict__ tcount, uint64_t *__restrict__ pushes,
+                                     unsigned long long *__restrict__ npush, uint64_t push_cap) {
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (i >= N) return;
+    uint64_t *pr = pool + (uint64_t)i * cap;
+    const uint32_t lim = min(Lp, pool_cnt[i]);
+    uint32_t taken = 0;
+    for (uint32_t b0 = 0; b0 < lim && (!capped || taken < S_); b0 += 32) {
+        uint32_t j = b0 + lane;
+        uint64_t k = j < lim ? pr[j] : 0;
+        bool f = j < lim && (k & KCNA_FLAG_NEW);
+        unsigned mk = __ballot_sync(KCNA_FULL, f);
+        uint32_t rank = taken + __popc(mk & kcna_lanemask_lt());
+        bool take = f && (!capped || rank < S_);
+        if (take) {
+            uint32_t tgt = kcna_key_id(k);
+            if (!emit) {
+                atomicAdd(tcount + tgt, 1u);
+            } else {
+                unsigned long long p = atomicAdd(npush, 1ull);
+                if (p < push_cap)
+                    pushes[p] = ((uint64_t)tgt << 32) | i | ((k & KCNA_FLAG_ISNEW) ? 0x80000000ull : 0ull);
+                pr[j] = k & ~KCNA_FLAG_NEW;
+            }
+        }
+        taken += __popc(__ballot_sync(KCNA_FULL, take));
+    }
+}
+
+__global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint64_t np,
+                                      const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                                      uint32_t *__restrict__ rnn, uint32_t N) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np) return;
+    uint64_t v = pushes[t];
+    uint32_t tgt = (uint32_t)(v >> 32);
+    if (tgt >= N) return;
+    uint32_t p = atomicAdd(cursor + tgt, 1u);
+    if (off[tgt] + p < off[tgt + 1]) rnn[off[tgt] + p] = (uint32_t)v;
+}
+
+// P2K join: for q, each pusher u (with its isnew bit) against q's PG
+// neighbours w: d(u, w) -> candidate (w) for pool u.  Warp per (q, u).
+__global__ void bridge_join_kernel(const float *__restrict__ X, int ld, uint32_t N, const uint64_t *__restrict__ off,
+                                   const uint32_t *__restrict__ rnn, const uint32_t *__restrict__ g_ids,
+                                   const uint32_t *__restrict__ g_deg, const uint8_t *__restrict__ g_isnew,
+                                   uint32_t W, const float *__restrict__ radius, uint64_t *__restrict__ cand,
+                                   uint32_t *__restrict__ cand_cnt, uint32_t CB, unsigned long long *comps) {
+    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (q >= N) return;
+    const uint64_t r0 = off[q], r1 = off[q + 1];
+    if (r0 == r1) return;
+    const int deg = (int)min(g_deg[q], W);
+    uint32_t wid[2] = {KCNA_NONE, KCNA_NONE};
+    bool wnew[2] = {false, false};
+    for (int h = 0; h < 2; ++h) {
+        int j = lane + 32 * h;
+        if (j < deg) {
+            wid[h] = g_ids[(uint64_t)q * W + j];
+            wnew[h] = g_isnew[(uint64_t)q * W + j] != 0;
+        }
+    }
+    unsigned long long cc = 0;
+    for (uint64_t r = r0; r < r1; ++r) {
+        uint32_t v = rnn[r];
+        uint32_t u = v & 0x7FFFFFFFu;
+        bool ifnew = (v & 0x80000000u) != 0;
+        if (u >= N) continue;
+        const float rad = radius[u];
+        const float *urow = X + (uint64_t)u * ld;
+        uint64_t keys[2];
+        bool ok[2] = {false, false};
+        for (int h = 0; h < 2; ++h) {
+            uint32_t w = wid[h];
+            if (w >= N || w == u || (!ifnew && !wnew[h])) continue;
+            ++cc;
+            float dd = kcna_l2_ldg(urow, X + (uint64_t)w * ld, ld);
+            if (dd <= rad) {
+                ok[h] = true;
+                keys[h] = kcna_key(dd, w, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+            }
+        }
+        for (int j = 64 + lane; j < deg; j += 32) { // rows wider than 64: direct emission
+            uint32_t w = g_ids[(uint64_t)q * W + j];
+            bool wn = g_isnew[(uint64_t)q * W + j] != 0;
+            if (w >= N || w == u || (!ifnew && !wn)) continue;
+            ++cc;
+            float dd = kcna_l2_ldg(urow, X + (uint64_t)w * ld, ld);
+            if (dd <= rad) {
+                uint32_t p = atomicAdd(cand_cnt + u, 1u);
+                if (p < CB) cand[(uint64_t)u * CB + p] = kcna_key(dd, w, 3u);
+            }
+        }
+        unsigned m0 = __ballot_sync(KCNA_FULL, ok[0]), m1 = __ballot_sync(KCNA_FULL, ok[1]);
+        int cnt = __popc(m0) + __popc(m1);
+        if (!cnt) continue;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(cand_cnt + u, (uint32_t)cnt);
+        base = __shfl_sync(KCNA_FULL, base, 0);
+        uint64_t *dst = cand + (uint64_t)u * CB;
+        if (ok[0]) {
+            uint32_t p = base + __popc(m0 & kcna_lanemask_lt());
+            if (p < CB) dst[p] = keys[0];
+        }
+        if (ok[1]) {
+            uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
+            if (p < CB) dst[p] = keys[1];
+        }
+    }
+    cc = kcna_warp_sum(cc);
+    if (lane == 0 && cc) atomicAdd(comps, cc);
+}
+
+PruneRule make_rule(const kcna_params *p, int kind) {
+    PruneRule r;
+    r.kind = kind;
+    r.t3 = 3.0f * p->tau;
+    r.thr = (float)std::cos((double)(p->angle / 180.0f) * kPi);
+    return r;
+}
+
+kcna_status exclusive_scan(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t *out, uint64_t *total_h) {
+    // out has n+1 entries; out[n] = total
+    uint32_t nb = kcna_div_up(std::max<uint64_t>(n, 1), (uint64_t)SCAN_T * SCAN_E);
+    uint64_t *sums = nullptr;
+    KCNA_TRY(kcna_alloc(c, &sums, nb + 1, "scan sums"));
+    scan_block_sums<<<nb, SCAN_T, 0, c->stream>>>(in, n, sums);
+    scan_sums_serial<<<1, 1, 0, c->stream>>>(sums, nb, sums + nb);
+    scan_apply<<<nb, SCAN_T, 0, c->stream>>>(in, n, sums, out);
+    c->launches += 3;
+    kcna_status s = kcna_cuda_check(c, cudaMemcpyAsync(out + n, sums + nb, 8, cudaMemcpyDeviceToDevice, c->stream),
+                                    "scan total");
+    if (s == KCNA_OK && total_h)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(total_h, sums + nb, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "scan sync");
+    cudaFree(sums);
+    return s;
+}
+
+} // namespace
+
+kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W) {
+    const uint64_t N = c->n;
+    if (c->W == W && c->g_ids) return KCNA_OK;
+    c->W = W;
+    KCNA_TRY(kcna_alloc(c, &c->g_ids, N * W, "graph ids"));
+    KCNA_TRY(kcna_alloc(c, &c->g_dist, N * W, "graph dists"));
+    KCNA_TRY(kcna_alloc(c, &c->g_isnew, N * W, "graph flags"));
+    KCNA_TRY(kcna_alloc(c, &c->g_deg, N, "graph degrees"));
+    KCNA_TRY(kcna_alloc(c, &c->g_old, N * W, "previous graph"));
+    KCNA_TRY(kcna_alloc(c, &c->g_old_deg, N, "previous degrees"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->g_deg, 0, N * 4, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->g_old_deg, 0, N * 4, c->stream), "memset"));
+    if (!c->counters) KCNA_TRY(kcna_alloc(c, &c->counters, 64, "counters"));
+    return KCNA_OK;
+}
+
+kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps) {
+    if (!c->has_pools) return kcna_fail(c, KCNA_E_STATE, "prune: no pools (run NN-descent or set pools first)");
+    const uint32_t range = p->nsg_R;
+    if (range == 0 || range > 128) return kcna_fail(c, KCNA_E_ARG, "nsg_R must be in [1, 128]");
+    KCNA_TRY(kcna_graph_alloc(c, std::max<uint32_t>(c->W, range + 8)));
+    PruneRule rule = make_rule(p, kind);
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 16, 0, 8, c->stream), "memset"));
+    size_t sm = (size_t)PW * 2 * range * 4;
+    prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+        c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, (int)std::min(p->search_K, c->cap),
+        c->g_ids, c->g_dist, c->g_deg, c->W, c->counters + 16);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
+    unsigned long long h = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 16, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "prune sync"));
+    if (comps) *comps = h;
+    c->has_graph = true;
+    return KCNA_OK;
+}
+
+kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps) {
+    uint64_t pc = 0;
+    KCNA_TRY(kcna_prune_all(c, p, kind, &pc));
+    const uint64_t N = c->n;
+    const uint32_t W = c->W;
+    // reverse-edge CSR: in-degree count, scan, fill
+    uint32_t *indeg = nullptr, *cursor = nullptr, *rev = nullptr;
+    uint64_t *off = nullptr;
+    kcna_status s = KCNA_OK;
+    auto cleanup = [&]() {
+        cudaFree(indeg);
+        cudaFree(cursor);
+        cudaFree(rev);
+        cudaFree(off);
+    };
+    if ((s = kcna_alloc(c, &indeg, N, "indeg")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &off, N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
+    cudaMemsetAsync(indeg, 0, N * 4, c->stream);
+    cudaMemsetAsync(cursor, 0, N * 4, c->stream);
+    rev_count_kernel<<<kcna_div_up(N * W, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, (uint32_t)N, W, indeg);
+    KCNA_LAUNCHED(c);
+    uint64_t E = 0;
+    if ((s = exclusive_scan(c, indeg, N, off, &E)) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &rev, std::max<uint64_t>(E, 1), "reverse edges")) != KCNA_OK) return cleanup(), s;
+    rev_fill_kernel<<<kcna_div_up(N * W, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, (uint32_t)N, W, off, cursor,
+                                                                     rev);
+    KCNA_LAUNCHED(c);
+    PruneRule rule = make_rule(p, kind);
+    cudaMemsetAsync(c->counters + 17, 0, 8, c->stream);
+    link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(c->X, (int)c->ld, (uint32_t)N, rule, (int)p->nsg_R,
+                                                         c->g_ids, c->g_dist, c->g_deg, W, off, rev,
+                                                         c->counters + 17, c->d_err);
+    KCNA_LAUNCHED(c);
+    s = kcna_cuda_check(c, cudaGetLastError(), "link kernels");
+    unsigned long long h = 0;
+    if (s == KCNA_OK)
+        s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 17, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync");
+    cleanup();
+    if (comps) *comps = pc + h;
+    return s == KCNA_OK ? kcna_check_device_err(c, "link") : s;
+}
+
+kcna_status kcna_search_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint32_t *d_init, uint32_t L,
+                               uint32_t k, uint32_t *d_out_ids, float *d_out_d) {
+    if (!c->has_graph) return kcna_fail(c, KCNA_E_STATE, "search: no graph");
+    if (L == 0 || L > 2048 || k == 0 || k > L) return kcna_fail(c, KCNA_E_ARG, "search: need 0 < k <= L <= 2048");
+    const uint32_t vwords = (c->n + 31) / 32;
+    uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(kcna_div_up(m, BW), (uint32_t)c->num_sms * 4));
+    uint64_t slots = (uint64_t)blocks * BW;
+    void *vis = nullptr;
+    KCNA_TRY(kcna_scratch2(c, slots * vwords * 4, &vis));
+    size_t sm = (size_t)BW * (L + 1) * 8;
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(beam_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(sm, 48 * 1024)),
+                             "attr"));
+    beam_search_kernel<<<blocks, BW * 32, sm, c->stream>>>(c->X, (int)c->ld, c->n, c->g_ids, c->g_deg, c->W, dQ, m,
+                                                           d_init, (int)L, (int)k, (uint32_t *)vis, vwords, d_out_ids,
+                                                           d_out_d);
+    KCNA_LAUNCHED(c);
+    return kcna_cuda_check(c, cudaGetLastError(), "beam_search");
+}
+
+// ComputeEp (src/kgraph.cpp:1528-1536): centroid of all rows, beam search of
+// width search_L seeded with the pool of a random node and random fill.
+kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
+    const uint32_t d = c->d, ld = c->ld;
+    const uint32_t nrows = c->n_total;
+    const uint32_t nb = kcna_div_up(nrows, CB_ROWS);
+    double *part = nullptr;
+    float *center = nullptr;
+    uint32_t *init = nullptr, *oid = nullptr;
+    float *od = nullptr;
+    kcna_status s = KCNA_OK;
+    auto cleanup = [&]() {
+        cudaFree(part);
+        cudaFree(center);
+        cudaFree(init);
+        cudaFree(oid);
+        cudaFree(od);
+    };
+    const uint32_t Lw = std::max<uint32_t>(1, std::min<uint32_t>(p->search_L, c->n - 1));
+    if ((s = kcna_alloc(c, &part, (size_t)nb * d, "centroid")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &center, ld, "center")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &init, Lw, "init ids")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &oid, Lw, "ep ids")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &od, Lw, "ep dists")) != KCNA_OK) return cleanup(), s;
+    centroid_partial_kernel<<<nb, 128, 0, c->stream>>>(c->X, (int)ld, nrows, (int)d, part);
+    centroid_final_kernel<<<1, 128, 0, c->stream>>>(part, nb, (int)d, (int)ld, nrows, center);
+    c->launches += 2;
+    // init ids: first search_L pool entries of a random node, then random distinct ids
+    std::mt19937 rng((uint32_t)seed);
+    uint32_t init_point = rng() % c->n;
+    uint32_t cnt = 0;
+    std::vector<uint64_t> pk(Lw);
+    cudaMemcpyAsync(&cnt, c->pool_cnt + init_point, 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(pk.data(), c->pool + (uint64_t)init_point * c->cap, (size_t)std::min(Lw, c->cap) * 8,
+                    cudaMemcpyDeviceToHost, c->stream);
+    if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "ep d2h")) != KCNA_OK) return cleanup(), s;
+    std::vector<uint32_t> ids;
+    std::set<uint32_t> seen;
+    for (uint32_t i = 0; i < Lw && i < cnt && i < c->cap; ++i) {
+        uint32_t id = (uint32_t)(pk[i] & 0xFFFFFFFFull) >> 2;
+        if (id < c->n && seen.insert(id).second) ids.push_back(id);
+    }
+    while (ids.size() < Lw) {
+        uint32_t id = rng() % c->n;
+        if (seen.insert(id).second) ids.push_back(id);
+    }
+    cudaMemcpyAsync(init, ids.data(), Lw * 4, cudaMemcpyHostToDevice, c->stream);
+    if ((s = kcna_search_device(c, center, 1, init, Lw, 1, oid, od)) != KCNA_OK) return cleanup(), s;
+    uint32_t ep = 0;
+    cudaMemcpyAsync(&ep, oid, 4, cudaMemcpyDeviceToHost, c->stream);
+    s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "ep sync");
+    cleanup();
+    if (s == KCNA_OK) c->ep = ep < c->n ? ep : 0;
+    return s;
+}
+
+kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
+    const uint32_t N = c->n, words = (N + 31) / 32;
+    uint32_t *vis = nullptr, *qa = nullptr, *qb = nullptr, *cntd = nullptr;
+    kcna_status s = KCNA_OK;
+    auto cleanup = [&]() {
+        cudaFree(vis);
+        cudaFree(qa);
+        cudaFree(qb);
+        cudaFree(cntd);
+    };
+    if ((s = kcna_alloc(c, &vis, words, "visited")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &qa, N, "frontier")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &qb, N, "frontier")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &cntd, 1, "count")) != KCNA_OK) return cleanup(), s;
+    cudaMemsetAsync(vis, 0, (size_t)words * 4, c->stream);
+    uint32_t ep = c->ep, bit = 1u << (ep & 31);
+    cudaMemcpyAsync(vis + (ep >> 5), &bit, 4, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(qa, &ep, 4, cudaMemcpyHostToDevice, c->stream);
+    uint32_t nf = 1;
+    for (uint32_t level = 0; nf > 0 && level < N; ++level) {
+        cudaMemsetAsync(cntd, 0, 4, c->stream);
+        bfs_expand_kernel<<<kcna_div_up((uint64_t)nf * 32, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W, N, qa,
+                                                                                      nf, vis, qb, cntd);
+        KCNA_LAUNCHED(c);
+        cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+        if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs")) != KCNA_OK) return cleanup(), s;
+        std::swap(qa, qb);
+    }
+    cudaMemsetAsync(c->counters + 18, 0, 8, c->stream);
+    attach_kernel<<<1, AT, 0, c->stream>>>(c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist,
+                                           c->g_deg, c->W, p->nsg_R, vis, qa, qb, seed, c->d_err, c->counters + 18);
+    KCNA_LAUNCHED(c);
+    s = kcna_cuda_check(c, cudaGetLastError(), "attach");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach sync");
+    cleanup();
+    return s == KCNA_OK ? kcna_check_device_err(c, "tree_grow") : s;
+}
+
+kcna_status kcna_update_nhoods(kcna_ctx *c, int loopcount) {
+    update_nhoods_kernel<<<kcna_div_up((uint64_t)c->n * 32, 256), 256, 0, c->stream>>>(
+        c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_isnew, c->n, c->W, loopcount == 0 ? 1 : 0);
+    KCNA_LAUNCHED(c);
+    return kcna_cuda_check(c, cudaGetLastError(), "update_nhoods");
+}
+
+// BridgeView (src/kgraph.cpp:2478-2506): rounds of capped pushes and joins;
+// when a round pushes fewer than N*massq_S/2 entries the rest is pushed and
+// the final join runs.
+kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, int loopcount, uint64_t *comps) {
+    const uint32_t N = c->n;
+    const uint32_t S_ = std::max<uint32_t>(p->massq_S, 1);
+    const int cur_loop = loopcount - 1;
+    const uint32_t cur_L = std::min<uint32_t>(p->search_L + (uint32_t)cur_loop * p->step, maxl);
+    const uint32_t pre_L = cur_loop > 0 ? std::min<uint32_t>(p->search_L + (uint32_t)(cur_loop - 1) * p->step, maxl) : 0;
+    const uint32_t Lp = std::min<uint32_t>(p->search_L + (uint32_t)(loopcount - 1) * p->step, maxl);
+    bridge_init_kernel<<<N, 128, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, cur_loop, pre_L, cur_L);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_pools_set_radius(c, maxl));
+    uint32_t *tcount = nullptr, *cursor = nullptr, *rnn = nullptr;
+    uint64_t *off = nullptr, *pushes = nullptr;
+    kcna_status s = KCNA_OK;
+    auto cleanup = [&]() {
+        cudaFree(tcount);
+        cudaFree(cursor);
+        cudaFree(rnn);
+        cudaFree(off);
+        cudaFree(pushes);
+    };
+    if ((s = kcna_alloc(c, &tcount, N, "push counts")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &off, (uint64_t)N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
+    uint64_t total_comps = 0;
+    const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    // the reference loops until a thin round; 100 rounds bound it here
+    for (int round = 0; round < 100; ++round) {
+        // capped round: count, then the uncapped remainder when the round is thin
+        cudaMemsetAsync(tcount, 0, (size_t)N * 4, c->stream);
+        bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 1, 0, tcount,
+                                                             nullptr, nullptr, 0);
+        KCNA_LAUNCHED(c);
+        uint64_t np = 0;
+        if ((s = exclusive_scan(c, tcount, N, off, &np)) != KCNA_OK) return cleanup(), s;
+        const bool last = (float)np / N / S_ < 0.5f;
+        uint64_t np_all = np;
+        if (last) { // also count the remainder (pushed after the capped entries are cleared)
+            uint32_t *tc2 = nullptr;
+            if ((s = kcna_alloc(c, &tc2, N, "push counts")) != KCNA_OK) return cleanup(), s;
+            cudaMemsetAsync(tc2, 0, (size_t)N * 4, c->stream);
+            // remainder = all flagged in the prefix minus the capped ones: count uncapped, subtract
+            bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 0, 0, tc2,
+                                                                 nullptr, nullptr, 0);
+            KCNA_LAUNCHED(c);
+            uint64_t np2 = 0;
+            s = exclusive_scan(c, tc2, N, off, &np2);
+            cudaFree(tc2);
+            if (s != KCNA_OK) return cleanup(), s;
+            np_all = np2; // uncapped count covers the capped pushes too
+        }
+        cudaFree(pushes);
+        pushes = nullptr;
+        cudaFree(rnn);
+        rnn = nullptr;
+        if ((s = kcna_alloc(c, &pushes, std::max<uint64_t>(np_all, 1), "pushes")) != KCNA_OK) return cleanup(), s;
+        if ((s = kcna_alloc(c, &rnn, std::max<uint64_t>(np_all, 1), "rnn")) != KCNA_OK) return cleanup(), s;
+        cudaMemsetAsync(c->counters + 20, 0, 8, c->stream);
+        bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 1, 1, nullptr,
+                                                             pushes, c->counters + 20, np_all);
+        KCNA_LAUNCHED(c);
+        if (last) {
+            bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 0, 1, nullptr,
+                                                                 pushes, c->counters + 20, np_all);
+            KCNA_LAUNCHED(c);
+        }
+        // group pushes by target (offsets already hold the right counts per target)
+        cudaMemsetAsync(cursor, 0, (size_t)N * 4, c->stream);
+        bridge_scatter_kernel<<<kcna_div_up(std::max<uint64_t>(np_all, 1), 256), 256, 0, c->stream>>>(
+            pushes, np_all, off, cursor, rnn, N);
+        KCNA_LAUNCHED(c);
+        cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
+        bridge_join_kernel<<<wblocks, 256, 0, c->stream>>>(c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg,
+                                                           c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt, c->CB,
+                                                           c->counters + 21);
+        KCNA_LAUNCHED(c);
+        unsigned long long h = 0;
+        cudaMemcpyAsync(&h, c->counters + 21, 8, cudaMemcpyDeviceToHost, c->stream);
+        if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bridge join")) != KCNA_OK) return cleanup(), s;
+        total_comps += h;
+        uint64_t ovf = 0, fl = 0;
+        if ((s = kcna_merge(c, maxl, maxl, &ovf, &fl)) != KCNA_OK) return cleanup(), s;
+        if (last || round == 99) break;
+    }
+    cleanup();
+    if (comps) *comps = total_comps;
+    return kcna_check_device_err(c, "bridge_view");
+}

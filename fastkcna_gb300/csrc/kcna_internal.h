@@ -1,0 +1,126 @@
+// kcna_internal.h - host-side context of the GB300 FastKCNA build library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "kcna.h"
+
+#define KCNA_EMPTY_KEY_H 0xFFFFFFFFFFFFFFFFull
+#define KCNA_MAX_ID ((1u << 30) - 1) // ids live in 30 bits of a pool key
+
+struct kcna_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    int *d_err = nullptr; // device error word (kcna_common.cuh KCNA_DERR_*)
+
+    // rows: n_total x ld floats, ld = d rounded up to 4, padding zero
+    float *X = nullptr;
+    uint32_t n_total = 0, n = 0, d = 0, ld = 0;
+
+    // candidate pools: n x cap keys (kcna_common.cuh), counts, filter radius
+    uint32_t cap = 0;
+    uint64_t *pool = nullptr;
+    uint32_t *pool_cnt = nullptr;
+    float *radius = nullptr;
+
+    // NN-descent state
+    uint32_t S = 0, Rr = 0, RB = 0, CB = 0, fwd_new_cap = 0, fwd_old_cap = 0;
+    uint32_t *M = nullptr;
+    float *radiusM = nullptr;
+    uint8_t *found = nullptr;
+    uint32_t *fwd_new = nullptr, *fwd_new_cnt = nullptr;
+    uint32_t *fwd_old = nullptr, *fwd_old_cnt = nullptr;
+    uint32_t *rnew = nullptr, *rnew_cnt = nullptr;
+    uint32_t *rold = nullptr, *rold_cnt = nullptr;
+    uint64_t *cand = nullptr;
+    uint32_t *cand_cnt = nullptr;
+    unsigned long long *counters = nullptr; // device scratch counters (64 slots)
+
+    // graph: n x W ids / dists / isnew flags, degrees; previous-loop ids
+    uint32_t W = 0;
+    uint32_t *g_ids = nullptr, *g_deg = nullptr, *g_old = nullptr, *g_old_deg = nullptr;
+    float *g_dist = nullptr;
+    uint8_t *g_isnew = nullptr;
+    uint32_t ep = 0, width = 0;
+    bool has_graph = false, has_pools = false;
+
+    // controls (exact MAXL-NN of sampled nodes) for the recall estimate
+    std::vector<uint32_t> control_ids;
+    uint32_t *d_controls = nullptr, *d_control_knn = nullptr;
+    uint32_t control_k = 0;
+
+    // generic scratch reused by phases
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void *scratch2 = nullptr;
+    size_t scratch2_bytes = 0;
+
+    kcna_stats *stats = nullptr;
+    double t0 = 0;
+};
+
+// error plumbing
+kcna_status kcna_fail(kcna_ctx *c, kcna_status s, const std::string &msg);
+kcna_status kcna_cuda_check(kcna_ctx *c, cudaError_t e, const char *what);
+kcna_status kcna_check_device_err(kcna_ctx *c, const char *phase);
+kcna_status kcna_scratch(kcna_ctx *c, size_t bytes, void **out);
+kcna_status kcna_scratch2(kcna_ctx *c, size_t bytes, void **out);
+template <typename T>
+kcna_status kcna_alloc(kcna_ctx *c, T **p, size_t count, const char *what) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (count == 0) return KCNA_OK;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        (void)cudaGetLastError();
+        return kcna_fail(c, KCNA_E_OOM, std::string("cudaMalloc failed for ") + what);
+    }
+    return KCNA_OK;
+}
+#define KCNA_TRY(x)                                  \
+    do {                                             \
+        kcna_status _s = (x);                        \
+        if (_s != KCNA_OK) return _s;                \
+    } while (0)
+#define KCNA_LAUNCHED(c) ((c)->launches++)
+double kcna_now();
+void kcna_log(kcna_ctx *c, const kcna_params *p, const char *fmt, ...);
+
+// kcna_knn.cu: exact k-NN of m query rows (device, m x ld) against rows
+// [0, n) of X; q_self (device, may be null) gives a row id to exclude per query.
+kcna_status kcna_knn_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint32_t *q_self, uint32_t k,
+                            uint32_t *d_out_ids, float *d_out_d);
+// gathers rows ids[0..m) of X into dst (m x ld)
+kcna_status kcna_gather_rows(kcna_ctx *c, const uint32_t *d_ids, uint32_t m, float *dst);
+
+// kcna_nnd.cu: NN-descent phases
+kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
+kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
+kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);
+kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk);
+kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);
+kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
+kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall);
+kcna_status kcna_pools_set_radius(kcna_ctx *c, uint32_t limit);
+kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *p, kcna_stats *st);
+
+// kcna_graph.cu: prune / link / entry point / connectivity / P2K / search
+kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W);
+kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
+kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
+kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed);
+kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed);
+kcna_status kcna_update_nhoods(kcna_ctx *c, int loopcount);
+kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, int loopcount, uint64_t *comps);
+kcna_status kcna_search_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint32_t *d_init, uint32_t L,
+                               uint32_t k, uint32_t *d_out_ids, float *d_out_d);

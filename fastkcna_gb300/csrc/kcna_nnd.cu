@@ -1,0 +1,859 @@
+// kcna_nnd.cu - NN-descent on device-resident pools.
+//
+// Replaces the KGraphConstructor constructor loop (src/kgraph.cpp:1281-1459):
+// init (:1001-1044), join (:1097-1117 with Nhood::join :970-987 and
+// parallel_try_insert :948-967), update (:1118-1202) and the per-iteration
+// statistics / stop rule (:1365-1426).
+//
+// GPU form of one iteration:
+//   join    one block per node n: gather the node's new list A and old list B,
+//           compute every pair of A x A (i < j) and A x B with the canonical
+//           FMA-chain distance in register tiles (rows staged through shared
+//           memory in 32-float chunks), and emit each pair to both endpoints'
+//           candidate buffers when it is within that endpoint's radius.
+//           Candidates of one target from one block are written as one
+//           contiguous run after a single atomicAdd.
+//   merge   one block per node: sort the candidate buffer, drop duplicates,
+//           merge with the sorted pool by rank, keep the best `limit`; new
+//           entries carry flag=new (the reference's InsertIntoPool
+//           :261-298 semantics applied to a batch).
+//   sample  the update step: M (prefix holding S new entries), radiusM, the
+//           forward new/old lists and reverse lists (atomics, capped buffers,
+//           random subset of R chosen in the join).
+// The reference inserts into locked pools while joining, so its result depends
+// on thread timing; this batched form inserts all of an iteration's
+// candidates at its end.
+#include <algorithm>
+#include <cmath>
+#include <random>
+
+#include "kcna_internal.h"
+#include "kcna_sort.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// init: S random pool entries + 2S random ids as the first new list.
+// GenRandom (src/kgraph.cpp:82-110): size values < N-size, sorted, made
+// strictly increasing, shifted by a random offset mod N.  Done per warp with a
+// bitonic sort and a prefix maximum (a[i] = i + max_{j<=i}(a[j]-j)).
+// ---------------------------------------------------------------------------
+__device__ void warp_gen_random(uint64_t seed, uint64_t stream, uint32_t size, uint32_t N, uint32_t *s_out,
+                                uint64_t *s_tmp) {
+    const int lane = kcna_lane();
+    if (N == size) {
+        for (uint32_t i = lane; i < size; i += 32) s_out[i] = i;
+        __syncwarp();
+        return;
+    }
+    int p = kcna_pow2_ceil_d((int)size);
+    for (int i = lane; i < p; i += 32)
+        s_tmp[i] = i < (int)size ? (uint64_t)(kcna_rand32(seed, stream, i) % (N - size)) : KCNA_EMPTY_KEY;
+    kcna_warp_bitonic(s_tmp, p);
+    // prefix max of a[j]-j over j, chunk by chunk of 32
+    int64_t carry = INT64_MIN;
+    for (uint32_t base = 0; base < size; base += 32) {
+        uint32_t i = base + lane;
+        int64_t v = i < size ? (int64_t)s_tmp[i] - (int64_t)i : INT64_MIN;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t u = __shfl_up_sync(KCNA_FULL, v, o);
+            if (lane >= o && u > v) v = u;
+        }
+        if (carry > v) v = carry;
+        carry = __shfl_sync(KCNA_FULL, v, 31);
+        if (i < size) s_out[i] = (uint32_t)((int64_t)i + v);
+    }
+    __syncwarp();
+    uint32_t off = kcna_rand32(seed, stream, 0xFFFFFFull) % N;
+    for (uint32_t i = lane; i < size; i += 32) s_out[i] = (uint32_t)(((uint64_t)s_out[i] + off) % N);
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(128) init_kernel(const float *__restrict__ X, int ld, uint32_t N, uint32_t S,
+                                                   uint32_t cap, uint64_t seed, uint64_t *__restrict__ pool,
+                                                   uint32_t *__restrict__ pool_cnt,
+                                                   uint32_t *__restrict__ fwd_new, uint32_t fwd_new_cap,
+                                                   uint32_t *__restrict__ fwd_new_cnt) {
+    __shared__ uint32_t s_ids[4][128];
+    __shared__ uint64_t s_tmp[4][128];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    const uint32_t n = blockIdx.x * 4 + w;
+    if (n >= N) return;
+    // first new list: 2S random ids (may include n itself, as in the reference)
+    warp_gen_random(seed, (uint64_t)n * 4 + 0, 2 * S, N, s_ids[w], s_tmp[w]);
+    for (uint32_t i = lane; i < 2 * S; i += 32) fwd_new[(uint64_t)n * fwd_new_cap + i] = s_ids[w][i];
+    if (lane == 0) fwd_new_cnt[n] = 2 * S;
+    __syncwarp();
+    // pool: S+1 random ids, n dropped, first S kept
+    warp_gen_random(seed, (uint64_t)n * 4 + 1, S + 1, N, s_ids[w], s_tmp[w]);
+    uint64_t key = KCNA_EMPTY_KEY;
+    {
+        uint32_t r = lane <= (int)S ? s_ids[w][lane] : n;
+        bool keep = lane <= (int)S && r != n;
+        unsigned mk = __ballot_sync(KCNA_FULL, keep);
+        int pos = __popc(mk & kcna_lanemask_lt());
+        if (keep && pos < (int)S) {
+            float dd = kcna_l2_ldg(X + (uint64_t)r * ld, X + (uint64_t)n * ld, ld);
+            key = kcna_key(dd, r, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+        }
+    }
+    key = kcna_warp_sort32(key);
+    uint64_t *pr = pool + (uint64_t)n * cap;
+    for (uint32_t i = lane; i < cap; i += 32) pr[i] = (i == (uint32_t)lane && i < S) ? key : KCNA_EMPTY_KEY;
+    if (lane == 0) pool_cnt[n] = S;
+}
+
+// ---------------------------------------------------------------------------
+// join
+// ---------------------------------------------------------------------------
+constexpr int JT = 256;      // threads per join block
+constexpr int JCOLS = 64;    // columns per tile chunk
+constexpr int JKC = 32;      // floats per k chunk
+constexpr int JKP = JKC + 4; // padded row pitch in shared memory
+
+struct JoinArgs {
+    const float *X;
+    int ld;
+    uint32_t N;
+    uint32_t iter;
+    uint64_t seed;
+    uint32_t R, RB;
+    const uint32_t *fwd_new, *fwd_new_cnt;
+    uint32_t fwd_new_cap;
+    const uint32_t *fwd_old, *fwd_old_cnt;
+    uint32_t fwd_old_cap;
+    const uint32_t *rnew, *rnew_cnt, *rold, *rold_cnt;
+    const float *radius;
+    uint64_t *cand;
+    uint32_t *cand_cnt;
+    uint32_t CB;
+    uint8_t *found;
+    unsigned long long *counters; // [0] pairs evaluated
+    uint32_t capA, capB;          // list capacities in shared memory (forward + RB)
+    int *err;
+};
+
+// copies up to R of cnt (capped at RB) reverse entries, a random subset when more
+__device__ void take_reverse(const uint32_t *src, uint32_t cnt, uint32_t RB, uint32_t R, uint64_t seed,
+                             uint64_t stream, uint32_t *dst, uint32_t *s_n) {
+    uint32_t m = min(cnt, RB);
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    if (m > R) {
+        if (threadIdx.x == 0) { // partial Fisher-Yates
+            for (uint32_t i = 0; i < R; ++i) {
+                uint32_t j = i + kcna_rand32(seed, stream, i) % (m - i);
+                uint32_t t = dst[i];
+                dst[i] = dst[j];
+                dst[j] = t;
+            }
+        }
+        m = R;
+    }
+    if (threadIdx.x == 0) *s_n = m;
+    __syncthreads();
+}
+
+template <int RI> // rows per thread = RI, tile rows = 32 * RI
+__device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
+                           float *s_As, float *s_Bs, float *s_D, const float *s_radA, int *s_any) {
+    constexpr int RA = 32 * RI;
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3; // 8 col groups x 32 row groups
+    const int ncol = na + nb;
+    const int ld = a.ld;
+    for (int c0 = 0; c0 < ncol; c0 += JCOLS) {
+        // rows that can pair with this chunk: i < min(na, c0+JCOLS) (i < j inside A)
+        const int rows_needed = min(na, c0 + JCOLS);
+        float acc[RI][8];
+#pragma unroll
+        for (int i = 0; i < RI; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+        for (int k0 = 0; k0 < ld; k0 += JKC) {
+            // stage A rows (RA x 32 floats) and chunk columns (64 x 32 floats)
+            for (int idx = tid; idx < RA * (JKC / 4); idx += JT) {
+                int r = idx >> 3, c = (idx & 7) * 4;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r < rows_needed && k0 + c < ld)
+                    v = __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)s_A[r] * ld + k0 + c));
+                *reinterpret_cast<float4 *>(s_As + r * JKP + c) = v;
+            }
+            for (int idx = tid; idx < JCOLS * (JKC / 4); idx += JT) {
+                int r = idx >> 3, c = (idx & 7) * 4;
+                int col = c0 + r;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (col < ncol && k0 + c < ld) {
+                    uint32_t id = col < na ? s_A[col] : s_B[col - na];
+                    v = __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)id * ld + k0 + c));
+                }
+                *reinterpret_cast<float4 *>(s_Bs + r * JKP + c) = v;
+            }
+            __syncthreads();
+            const int kend = min(JKC, ld - k0);
+            for (int k = 0; k < kend; k += 4) {
+                float4 ra[RI], cb[8];
+#pragma unroll
+                for (int i = 0; i < RI; ++i) ra[i] = *reinterpret_cast<const float4 *>(s_As + (ty + 32 * i) * JKP + k);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) cb[j] = *reinterpret_cast<const float4 *>(s_Bs + (tx + 8 * j) * JKP + k);
+#pragma unroll
+                for (int i = 0; i < RI; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = kcna_acc4(acc[i][j], ra[i], cb[j]);
+            }
+            __syncthreads();
+        }
+        // distances of the chunk to shared memory: s_D[row][col], pitch JCOLS+1
+#pragma unroll
+        for (int i = 0; i < RI; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s_D[(ty + 32 * i) * (JCOLS + 1) + tx + 8 * j] = acc[i][j];
+        __syncthreads();
+        // emission: warp w handles row targets, then column targets
+        const int warp = tid >> 5, lane = tid & 31, nwarp = JT / 32;
+        const int cend = min(JCOLS, ncol - c0);
+        // row targets: A[i] receives column ids
+        for (int i = warp; i < rows_needed; i += nwarp) {
+            uint32_t tgt = s_A[i];
+            float rad = s_radA[i];
+            int cnt = 0;
+            uint64_t keys[2];
+            bool ok[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                int cl = lane + 32 * h, col = c0 + cl;
+                ok[h] = false;
+                if (cl < cend && (col >= na || i < col)) {
+                    uint32_t id = col < na ? s_A[col] : s_B[col - na];
+                    float dd = s_D[i * (JCOLS + 1) + cl];
+                    if (id != tgt && dd <= rad) {
+                        ok[h] = true;
+                        keys[h] = kcna_key(dd, id, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+                    }
+                }
+            }
+            unsigned m0 = __ballot_sync(KCNA_FULL, ok[0]), m1 = __ballot_sync(KCNA_FULL, ok[1]);
+            cnt = __popc(m0) + __popc(m1);
+            if (cnt == 0) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
+            base = __shfl_sync(KCNA_FULL, base, 0);
+            uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
+            if (ok[0]) {
+                uint32_t p = base + __popc(m0 & kcna_lanemask_lt());
+                if (p < a.CB) dst[p] = keys[0];
+            }
+            if (ok[1]) {
+                uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
+                if (p < a.CB) dst[p] = keys[1];
+            }
+            if (lane == 0) *s_any = 1;
+        }
+        // column targets: column id receives row ids
+        for (int cl = warp; cl < cend; cl += nwarp) {
+            int col = c0 + cl;
+            uint32_t tgt = col < na ? s_A[col] : s_B[col - na];
+            float rad = __ldg(a.radius + tgt);
+            unsigned mk[RI];
+            uint64_t keys[RI];
+            int cnt = 0;
+#pragma unroll
+            for (int h = 0; h < RI; ++h) {
+                int i = lane + 32 * h;
+                bool ok = false;
+                if (i < rows_needed && (col >= na || i < col)) {
+                    uint32_t id = s_A[i];
+                    float dd = s_D[i * (JCOLS + 1) + cl];
+                    if (id != tgt && dd <= rad) {
+                        ok = true;
+                        keys[h] = kcna_key(dd, id, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+                    }
+                }
+                mk[h] = __ballot_sync(KCNA_FULL, ok);
+                cnt += __popc(mk[h]);
+            }
+            if (cnt == 0) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
+            base = __shfl_sync(KCNA_FULL, base, 0);
+            uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
+            uint32_t run = base;
+#pragma unroll
+            for (int h = 0; h < RI; ++h) {
+                if (mk[h] & (1u << lane)) {
+                    uint32_t p = run + __popc(mk[h] & kcna_lanemask_lt());
+                    if (p < a.CB) dst[p] = keys[h];
+                }
+                run += __popc(mk[h]);
+            }
+            if (lane == 0) *s_any = 1;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(JT) join_kernel(JoinArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *s_As = reinterpret_cast<float *>(smem);                // 128 x JKP
+    float *s_Bs = s_As + 128 * JKP;                               // JCOLS x JKP
+    float *s_D = s_Bs + JCOLS * JKP;                              // 128 x (JCOLS+1)
+    float *s_radA = s_D + 128 * (JCOLS + 1);                      // capA
+    uint32_t *s_A = reinterpret_cast<uint32_t *>(s_radA + a.capA); // capA
+    uint32_t *s_B = s_A + a.capA;                                 // capB
+    __shared__ uint32_t s_na, s_nb, s_tmp;
+    __shared__ int s_any;
+    const uint32_t node = blockIdx.x;
+    if (threadIdx.x == 0) s_any = 0;
+    // new list: forward new then a random subset (<= R) of reverse new
+    uint32_t fn = min(a.fwd_new_cnt[node], a.fwd_new_cap);
+    for (uint32_t i = threadIdx.x; i < fn; i += blockDim.x) s_A[i] = a.fwd_new[(uint64_t)node * a.fwd_new_cap + i];
+    uint32_t fo = min(a.fwd_old_cnt[node], a.fwd_old_cap);
+    for (uint32_t i = threadIdx.x; i < fo; i += blockDim.x) s_B[i] = a.fwd_old[(uint64_t)node * a.fwd_old_cap + i];
+    __syncthreads();
+    uint32_t rn = 0, ro = 0;
+    if (a.iter > 0) {
+        take_reverse(a.rnew + (uint64_t)node * a.RB, a.rnew_cnt[node], a.RB, a.R, a.seed,
+                     ((uint64_t)a.iter << 40) ^ ((uint64_t)node << 1), s_A + fn, &s_tmp);
+        rn = s_tmp;
+        take_reverse(a.rold + (uint64_t)node * a.RB, a.rold_cnt[node], a.RB, a.R, a.seed,
+                     ((uint64_t)a.iter << 40) ^ ((uint64_t)node << 1) ^ 1ull, s_B + fo, &s_tmp);
+        ro = s_tmp;
+    }
+    // at most 128 rows per tile; the forward list alone is <= S + R < 128 in practice
+    const int na = (int)min(fn + rn, 128u), nb = (int)(fo + ro);
+    for (int i = threadIdx.x; i < na; i += blockDim.x) s_radA[i] = __ldg(a.radius + s_A[i]);
+    __syncthreads();
+    if (na == 0) return;
+    if (threadIdx.x == 0)
+        atomicAdd(a.counters + 0, (unsigned long long)((uint64_t)na * (na - 1) / 2 + (uint64_t)na * nb));
+    if (na <= 32)
+        join_tiles<1>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
+    else if (na <= 64)
+        join_tiles<2>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
+    else
+        join_tiles<4>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
+    if (threadIdx.x == 0) a.found[node] = s_any ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// merge: candidates of one node into its pool (batched InsertIntoPool)
+// ---------------------------------------------------------------------------
+constexpr int MT = 256;
+
+struct MergeArgs {
+    uint64_t *pool;
+    uint32_t *pool_cnt;
+    uint32_t cap, limit, K;
+    float *radius;
+    uint64_t *cand;
+    uint32_t *cand_cnt;
+    uint32_t CB;
+    unsigned long long *counters; // [1] flagged in top-K, [2] overflow, [3] inserted
+};
+
+__global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t node = blockIdx.x;
+    uint64_t *s_pool = reinterpret_cast<uint64_t *>(smem);        // cap
+    uint64_t *s_c = s_pool + a.cap;                               // pow2(CB)
+    uint32_t *s_scan = reinterpret_cast<uint32_t *>(s_c + kcna_pow2_ceil_d((int)a.CB)); // pow2(CB)+1
+    __shared__ uint32_t s_warp[MT / 32];
+    __shared__ unsigned long long s_flagged;
+    const uint32_t raw = a.cand_cnt[node];
+    const uint32_t nc = min(raw, a.CB);
+    const uint32_t np = min(a.pool_cnt[node], a.limit);
+    uint64_t *gp = a.pool + (uint64_t)node * a.cap;
+    if (threadIdx.x == 0) s_flagged = 0;
+    if (nc == 0) {
+        // no candidates: only the statistic (flags among the first K)
+        unsigned long long f = 0;
+        for (uint32_t i = threadIdx.x; i < min(np, a.K); i += MT) f += (gp[i] & KCNA_FLAG_NEW) ? 1 : 0;
+        f = kcna_warp_sum(f);
+        if ((threadIdx.x & 31) == 0 && f) atomicAdd(a.counters + 1, f);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < np; i += MT) s_pool[i] = gp[i];
+    const int cp = kcna_pow2_ceil_d((int)nc);
+    const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+    for (int i = threadIdx.x; i < cp; i += MT) s_c[i] = i < (int)nc ? kcna_key_noflags(gc[i]) : KCNA_EMPTY_KEY;
+    kcna_cta_bitonic(s_c, cp);
+    // keep[j]: first of its (dist,id) run, not empty, not already pooled
+    for (int j = threadIdx.x; j < cp; j += MT) {
+        uint64_t k = s_c[j];
+        bool keep = k != KCNA_EMPTY_KEY && (j == 0 || (s_c[j - 1] >> 2) != (k >> 2));
+        if (keep) {
+            int lb = kcna_lower_bound(s_pool, (int)np, k); // pool keys carry flags: compare without them
+            // s_pool sorted by full key; equal (dist,id) has key in [k, k|3]
+            if (lb < (int)np && (s_pool[lb] >> 2) == (k >> 2)) keep = false;
+        }
+        s_scan[j] = keep ? 1u : 0u;
+    }
+    __syncthreads();
+    // exclusive scan of keep flags over cp entries (block-wide, chunked)
+    {
+        const int per = (cp + MT - 1) / MT;
+        const int b = threadIdx.x * per;
+        uint32_t local = 0;
+        for (int i = 0; i < per && b + i < cp; ++i) local += s_scan[b + i];
+        uint32_t incl = local;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(KCNA_FULL, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) s_warp[w] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int i = 0; i < MT / 32; ++i) {
+                uint32_t t = s_warp[i];
+                s_warp[i] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        uint32_t run = s_warp[w] + incl - local;
+        for (int i = 0; i < per && b + i < cp; ++i) {
+            uint32_t t = s_scan[b + i];
+            s_scan[b + i] = run;
+            run += t;
+        }
+        if (threadIdx.x == MT - 1) s_scan[cp] = run;
+        __syncthreads();
+    }
+    const uint32_t kept = s_scan[cp];
+    const uint32_t newcnt = min(a.limit, np + kept);
+    // ranks: pool element i -> i + #kept candidates below it; kept candidate j -> scan[j] + #pool below it
+    // write straight to the global pool (its entries are staged in s_pool)
+    unsigned long long flagged = 0;
+    for (uint32_t i = threadIdx.x; i < np; i += MT) {
+        uint64_t k = s_pool[i];
+        int lb = kcna_lower_bound(s_c, cp, kcna_key_noflags(k));
+        uint32_t r = i + s_scan[lb];
+        if (r < newcnt) {
+            gp[r] = k;
+            if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
+        }
+    }
+    for (int j = threadIdx.x; j < cp; j += MT) {
+        uint64_t k = s_c[j];
+        bool keep = s_scan[j + 1] != s_scan[j];
+        if (!keep) continue;
+        uint32_t r = s_scan[j] + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
+        if (r < newcnt) {
+            gp[r] = k | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
+            if (r < a.K) ++flagged;
+        }
+    }
+    flagged = kcna_warp_sum(flagged);
+    if ((threadIdx.x & 31) == 0 && flagged) atomicAdd(&s_flagged, flagged);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(a.counters + 1, s_flagged);
+        if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
+        atomicAdd(a.counters + 3, (unsigned long long)(newcnt - min(np, newcnt)));
+        a.pool_cnt[node] = newcnt;
+        a.cand_cnt[node] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        a.radius[node] = newcnt >= a.limit ? kcna_key_dist(gp[a.limit - 1]) : __uint_as_float(0x7F800000u);
+}
+
+// ---------------------------------------------------------------------------
+// sample (update, src/kgraph.cpp:1118-1202)
+// ---------------------------------------------------------------------------
+__global__ void sample_m_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                uint32_t N, uint32_t S, const uint8_t *__restrict__ found, uint32_t *__restrict__ Mv,
+                                float *__restrict__ radiusM) {
+    const uint32_t n = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = kcna_lane();
+    if (n >= N) return;
+    const uint64_t *pr = pool + (uint64_t)n * cap;
+    uint32_t L = pool_cnt[n];
+    uint32_t M = Mv[n];
+    if (found[n]) {
+        uint32_t maxl = min(M + S, L);
+        uint32_t c = 0, l = maxl; // l: smallest prefix holding S flagged entries, else maxl
+        for (uint32_t b = 0; b < maxl; b += 32) {
+            uint32_t i = b + lane;
+            bool f = i < maxl && (pr[i] & KCNA_FLAG_NEW);
+            unsigned mk = __ballot_sync(KCNA_FULL, f);
+            uint32_t tot = __popc(mk);
+            if (c + tot >= S) {
+                // position of the S-th flagged entry in this chunk
+                uint32_t needed = S - c;
+                unsigned mm = mk;
+                for (uint32_t t = 1; t < needed; ++t) mm &= mm - 1;
+                l = b + __ffs(mm);
+                break;
+            }
+            c += tot;
+        }
+        M = l;
+    }
+    if (M == 0) M = min(1u, L); // the reference aborts here (BOOST_VERIFY, :1148)
+    if (lane == 0) {
+        Mv[n] = M;
+        radiusM[n] = M > 0 ? kcna_key_dist(pr[M - 1]) : 0.f;
+    }
+}
+
+__global__ void sample_lists_kernel(uint64_t *__restrict__ pool, uint32_t cap, uint32_t N,
+                                    const uint32_t *__restrict__ Mv, const float *__restrict__ radiusM,
+                                    uint32_t *__restrict__ fwd_new, uint32_t fwd_new_cap,
+                                    uint32_t *__restrict__ fwd_new_cnt, uint32_t *__restrict__ fwd_old,
+                                    uint32_t fwd_old_cap, uint32_t *__restrict__ fwd_old_cnt,
+                                    uint32_t *__restrict__ rnew, uint32_t *__restrict__ rnew_cnt,
+                                    uint32_t *__restrict__ rold, uint32_t *__restrict__ rold_cnt, uint32_t RB,
+                                    unsigned long long *counters) {
+    const uint32_t n = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = kcna_lane();
+    if (n >= N) return;
+    uint64_t *pr = pool + (uint64_t)n * cap;
+    const uint32_t M = Mv[n];
+    uint32_t cn = 0, co = 0;
+    for (uint32_t b = 0; b < M; b += 32) {
+        uint32_t l = b + lane;
+        uint64_t k = l < M ? pr[l] : 0;
+        bool valid = l < M;
+        bool isnew = valid && (k & KCNA_FLAG_NEW);
+        bool isold = valid && !(k & KCNA_FLAG_NEW);
+        uint32_t id = kcna_key_id(k);
+        float dd = kcna_key_dist(k);
+        unsigned mn = __ballot_sync(KCNA_FULL, isnew), mo = __ballot_sync(KCNA_FULL, isold);
+        if (isnew) {
+            uint32_t p = cn + __popc(mn & kcna_lanemask_lt());
+            if (p < fwd_new_cap) {
+                fwd_new[(uint64_t)n * fwd_new_cap + p] = id;
+                pr[l] = k & ~KCNA_FLAG_NEW; // used in a join from now on
+            }
+        }
+        if (isold) {
+            uint32_t p = co + __popc(mo & kcna_lanemask_lt());
+            if (p < fwd_old_cap) fwd_old[(uint64_t)n * fwd_old_cap + p] = id;
+        }
+        // reverse edge n -> id only when n lies outside id's own join prefix
+        if (valid && id < N && dd > radiusM[id]) {
+            if (isnew) {
+                uint32_t p = atomicAdd(rnew_cnt + id, 1u);
+                if (p < RB) rnew[(uint64_t)id * RB + p] = n;
+            } else {
+                uint32_t p = atomicAdd(rold_cnt + id, 1u);
+                if (p < RB) rold[(uint64_t)id * RB + p] = n;
+            }
+        }
+        cn += __popc(mn);
+        co += __popc(mo);
+    }
+    if (lane == 0) {
+        if (cn > fwd_new_cap) atomicAdd(counters + 4, (unsigned long long)(cn - fwd_new_cap));
+        fwd_new_cnt[n] = min(cn, fwd_new_cap);
+        fwd_old_cnt[n] = min(co, fwd_old_cap);
+    }
+}
+
+// control recall: |pool[0..min(cnt,K)) ∩ exact[0..K)| per control
+__global__ void control_recall_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
+                                      uint32_t cap, const uint32_t *__restrict__ controls,
+                                      const uint32_t *__restrict__ knn, uint32_t knn_k, uint32_t K,
+                                      unsigned long long *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *s = reinterpret_cast<uint64_t *>(smem);
+    const uint32_t c = blockIdx.x, id = controls[c];
+    const int p = kcna_pow2_ceil_d((int)K);
+    for (int i = threadIdx.x; i < p; i += blockDim.x) s[i] = i < (int)K ? knn[(uint64_t)c * knn_k + i] : KCNA_EMPTY_KEY;
+    kcna_cta_bitonic(s, p);
+    uint32_t lim = min(pool_cnt[id], K);
+    unsigned long long f = 0;
+    for (uint32_t i = threadIdx.x; i < lim; i += blockDim.x) {
+        uint64_t q = kcna_key_id(pool[(uint64_t)id * cap + i]);
+        int lb = kcna_lower_bound(s, (int)K, q);
+        if (lb < (int)K && s[lb] == q) ++f;
+    }
+    f = kcna_warp_sum(f);
+    if ((threadIdx.x & 31) == 0 && f) atomicAdd(out, f);
+}
+
+__global__ void set_radius_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
+                                  uint32_t cap, uint32_t N, uint32_t limit, float *__restrict__ radius) {
+    uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    radius[n] = pool_cnt[n] >= limit ? kcna_key_dist(pool[(uint64_t)n * cap + limit - 1]) : __uint_as_float(0x7F800000u);
+}
+
+size_t join_smem_bytes(uint32_t capA, uint32_t capB) {
+    return (size_t)(128 * JKP + JCOLS * JKP + 128 * (JCOLS + 1)) * sizeof(float) + (size_t)capA * 4 * 2 +
+           (size_t)capB * 4;
+}
+size_t merge_smem_bytes(uint32_t cap, uint32_t CB) {
+    size_t cp = (size_t)kcna_pow2_ceil((int)CB);
+    return cap * 8 + cp * 8 + (cp + 1) * 4;
+}
+
+} // namespace
+
+kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
+    const uint64_t N = c->n;
+    c->cap = maxl;
+    c->S = p->S;
+    c->Rr = p->R;
+    c->RB = std::max<uint32_t>(2 * p->R, 32);
+    const char *cb = getenv("KCNA_CAND_CAP");
+    uint32_t CB = cb ? (uint32_t)atoi(cb) : 4 * std::max<uint32_t>(p->L, 64);
+    CB = std::min<uint32_t>(std::max<uint32_t>(CB, 64), 8192);
+    c->CB = (uint32_t)kcna_pow2_ceil((int)CB);
+    c->fwd_new_cap = std::max<uint32_t>(2 * p->S, 64);
+    c->fwd_old_cap = std::max<uint32_t>(p->L, 1);
+    KCNA_TRY(kcna_alloc(c, &c->pool, N * c->cap, "pool"));
+    KCNA_TRY(kcna_alloc(c, &c->pool_cnt, N, "pool_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->radius, N, "radius"));
+    KCNA_TRY(kcna_alloc(c, &c->M, N, "M"));
+    KCNA_TRY(kcna_alloc(c, &c->radiusM, N, "radiusM"));
+    KCNA_TRY(kcna_alloc(c, &c->found, N, "found"));
+    KCNA_TRY(kcna_alloc(c, &c->fwd_new, N * c->fwd_new_cap, "fwd_new"));
+    KCNA_TRY(kcna_alloc(c, &c->fwd_new_cnt, N, "fwd_new_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->fwd_old, N * c->fwd_old_cap, "fwd_old"));
+    KCNA_TRY(kcna_alloc(c, &c->fwd_old_cnt, N, "fwd_old_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->rnew, N * c->RB, "rnew"));
+    KCNA_TRY(kcna_alloc(c, &c->rnew_cnt, N, "rnew_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->rold, N * c->RB, "rold"));
+    KCNA_TRY(kcna_alloc(c, &c->rold_cnt, N, "rold_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
+    KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
+    if (!c->counters) KCNA_TRY(kcna_alloc(c, &c->counters, 64, "counters"));
+    cudaStream_t s = c->stream;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->cand_cnt, 0, N * 4, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rnew_cnt, 0, N * 4, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rold_cnt, 0, N * 4, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->fwd_old_cnt, 0, N * 4, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->found, 0, N, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 64 * 8, s), "memset"));
+    return KCNA_OK;
+}
+
+kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p) {
+    if (p->S == 0 || p->S > 31) return kcna_fail(c, KCNA_E_ARG, "S must be in [1, 31]");
+    init_kernel<<<kcna_div_up(c->n, 4), 128, 0, c->stream>>>(c->X, (int)c->ld, c->n, p->S, c->cap, p->seed, c->pool,
+                                                           c->pool_cnt, c->fwd_new, c->fwd_new_cap, c->fwd_new_cnt);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "init_kernel"));
+    KCNA_TRY(kcna_pools_set_radius(c, p->L));
+    // M = S (src/kgraph.cpp:1030)
+    std::vector<uint32_t> Ms(c->n, p->S);
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->M, Ms.data(), (size_t)c->n * 4, cudaMemcpyHostToDevice, c->stream),
+                             "M init"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "init sync"));
+    c->has_pools = true;
+    return KCNA_OK;
+}
+
+kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps) {
+    JoinArgs a;
+    a.X = c->X;
+    a.ld = (int)c->ld;
+    a.N = c->n;
+    a.iter = (uint32_t)iter;
+    a.seed = p->seed;
+    a.R = p->R;
+    a.RB = c->RB;
+    a.fwd_new = c->fwd_new;
+    a.fwd_new_cnt = c->fwd_new_cnt;
+    a.fwd_new_cap = c->fwd_new_cap;
+    a.fwd_old = c->fwd_old;
+    a.fwd_old_cnt = c->fwd_old_cnt;
+    a.fwd_old_cap = c->fwd_old_cap;
+    a.rnew = c->rnew;
+    a.rnew_cnt = c->rnew_cnt;
+    a.rold = c->rold;
+    a.rold_cnt = c->rold_cnt;
+    a.radius = c->radius;
+    a.cand = c->cand;
+    a.cand_cnt = c->cand_cnt;
+    a.CB = c->CB;
+    a.found = c->found;
+    a.counters = c->counters;
+    a.capA = c->fwd_new_cap + c->RB;
+    a.capB = c->fwd_old_cap + c->RB;
+    a.err = c->d_err;
+    size_t sm = join_smem_bytes(a.capA, a.capB);
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(sm, 48 * 1024)),
+                             "join smem attr"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8, c->stream), "memset"));
+    join_kernel<<<c->n, JT, sm, c->stream>>>(a);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "join_kernel"));
+    unsigned long long h = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "join sync"));
+    if (n_comps) *n_comps = h;
+    return KCNA_OK;
+}
+
+kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk) {
+    MergeArgs a;
+    a.pool = c->pool;
+    a.pool_cnt = c->pool_cnt;
+    a.cap = c->cap;
+    a.limit = std::min(limit, c->cap);
+    a.K = K;
+    a.radius = c->radius;
+    a.cand = c->cand;
+    a.cand_cnt = c->cand_cnt;
+    a.CB = c->CB;
+    a.counters = c->counters;
+    size_t sm = merge_smem_bytes(c->cap, c->CB);
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(sm, 48 * 1024)),
+                             "merge smem attr"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 1, 0, 3 * 8, c->stream), "memset"));
+    merge_kernel<<<c->n, MT, sm, c->stream>>>(a);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
+    unsigned long long h[4] = {0, 0, 0, 0};
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 32, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "merge sync"));
+    if (overflow) *overflow = h[2];
+    if (flagged_topk) *flagged_topk = h[1];
+    return KCNA_OK;
+}
+
+kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter) {
+    (void)iter;
+    cudaStream_t s = c->stream;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rnew_cnt, 0, (size_t)c->n * 4, s), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rold_cnt, 0, (size_t)c->n * 4, s), "memset"));
+    sample_m_kernel<<<kcna_div_up(c->n, 8), 256, 0, s>>>(c->pool, c->pool_cnt, c->cap, c->n, p->S, c->found, c->M,
+                                                          c->radiusM);
+    KCNA_LAUNCHED(c);
+    sample_lists_kernel<<<kcna_div_up(c->n, 8), 256, 0, s>>>(c->pool, c->cap, c->n, c->M, c->radiusM, c->fwd_new,
+                                                              c->fwd_new_cap, c->fwd_new_cnt, c->fwd_old,
+                                                              c->fwd_old_cap, c->fwd_old_cnt, c->rnew, c->rnew_cnt,
+                                                              c->rold, c->rold_cnt, c->RB, c->counters);
+    KCNA_LAUNCHED(c);
+    return kcna_cuda_check(c, cudaGetLastError(), "sample kernels");
+}
+
+kcna_status kcna_pools_set_radius(kcna_ctx *c, uint32_t limit) {
+    set_radius_kernel<<<kcna_div_up(c->n, 256), 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, c->n,
+                                                                      std::min(limit, c->cap), c->radius);
+    KCNA_LAUNCHED(c);
+    return kcna_cuda_check(c, cudaGetLastError(), "set_radius");
+}
+
+// Controls: C random nodes and their exact MAXL-NN (GenerateControl,
+// src/kgraph.cpp:363-387); nodes drawn with mt19937(seed).
+kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
+    uint32_t C = std::min<uint32_t>(p->controls, c->n - 1);
+    c->control_ids.clear();
+    if (C == 0) return KCNA_OK;
+    std::vector<uint32_t> idx(c->n);
+    for (uint32_t i = 0; i < c->n; ++i) idx[i] = i;
+    std::mt19937 rng(p->seed);
+    for (uint32_t i = 0; i < C; ++i) {
+        uint32_t j = i + rng() % (c->n - i);
+        std::swap(idx[i], idx[j]);
+    }
+    c->control_ids.assign(idx.begin(), idx.begin() + C);
+    c->control_k = maxl;
+    KCNA_TRY(kcna_alloc(c, &c->d_controls, C, "controls"));
+    KCNA_TRY(kcna_alloc(c, &c->d_control_knn, (size_t)C * maxl, "control knn"));
+    float *dd = nullptr, *rows = nullptr;
+    KCNA_TRY(kcna_alloc(c, &dd, (size_t)C * maxl, "control dists"));
+    KCNA_TRY(kcna_alloc(c, &rows, (size_t)C * c->ld, "control rows"));
+    kcna_status st = kcna_cuda_check(c, cudaMemcpyAsync(c->d_controls, c->control_ids.data(), C * 4,
+                                                        cudaMemcpyHostToDevice, c->stream), "h2d");
+    if (st == KCNA_OK) st = kcna_gather_rows(c, c->d_controls, C, rows);
+    if (st == KCNA_OK) st = kcna_knn_device(c, rows, C, c->d_controls, maxl, c->d_control_knn, dd);
+    if (st == KCNA_OK) st = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "controls sync");
+    cudaFree(dd);
+    cudaFree(rows);
+    return st;
+}
+
+kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall) {
+    uint32_t C = (uint32_t)c->control_ids.size();
+    if (C == 0) {
+        *recall = 0.f;
+        return KCNA_OK;
+    }
+    K = std::min(K, c->control_k);
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 8, 0, 8, c->stream), "memset"));
+    size_t sm = (size_t)kcna_pow2_ceil((int)K) * 8;
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(control_recall_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(sm, 48 * 1024)),
+                             "attr"));
+    control_recall_kernel<<<C, 256, sm, c->stream>>>(c->pool, c->pool_cnt, c->cap, c->d_controls, c->d_control_knn,
+                                                     c->control_k, K, c->counters + 8);
+    KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "control_recall"));
+    unsigned long long h = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 8, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "recall sync"));
+    *recall = (float)((double)h / ((double)C * K));
+    return KCNA_OK;
+}
+
+// The constructor loop of src/kgraph.cpp:1281-1459 with its stop rule
+// (delta <= params.delta, recall >= params.recall, or I iterations).
+kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *st) {
+    kcna_params P = *pin;
+    const uint32_t N = c->n;
+    if (N < 3) return kcna_fail(c, KCNA_E_ARG, "need at least 3 rows");
+    // parameter clamping, src/kgraph.cpp:1289-1327
+    if (N <= P.controls) P.controls = N - 1;
+    if (N <= P.L) P.L = N - 1;
+    if (N <= P.S) P.S = N - 1;
+    if (N <= P.search_L) P.search_L = N - 1;
+    if (N <= P.search_K) P.search_K = N - 1;
+    if (N <= P.K) {
+        P.K = N - 1;
+        P.loop_i = 0;
+        P.S = N - 1;
+        P.iterations = 0;
+    }
+    const uint32_t maxl = std::max(std::max(P.L, P.K), std::max(P.search_L, P.search_K));
+    if (maxl > 1024) return kcna_fail(c, KCNA_E_ARG, "max(L, K, search_L, search_K) must be <= 1024");
+    st->maxl = maxl;
+    KCNA_TRY(kcna_nnd_alloc(c, &P, maxl));
+    KCNA_TRY(kcna_controls_setup(c, &P, maxl));
+    KCNA_TRY(kcna_nnd_init(c, &P));
+    uint64_t comps_total = 0;
+    st->stop_condition = 0;
+    st->iterations = 0;
+    for (uint32_t it = 0; it < P.iterations; ++it) {
+        uint64_t comps = 0, overflow = 0, flagged = 0;
+        KCNA_TRY(kcna_nnd_join(c, &P, (int)it, &comps));
+        KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged));
+        comps_total += comps;
+        float delta = (float)((double)flagged / ((double)N * P.K));
+        float recall = 0.f;
+        KCNA_TRY(kcna_control_recall(c, P.K, &recall));
+        if (it < KCNA_MAX_ITERS) {
+            st->iter_recall[it] = recall;
+            st->iter_delta[it] = delta;
+            st->iter_time[it] = kcna_now() - c->t0;
+            st->iter_cand_overflow[it] = overflow;
+        }
+        st->iterations = it + 1;
+        kcna_log(c, &P, "iteration %u recall %.4f delta %.4f comps %llu overflow %llu t %.3f", it + 1, recall, delta,
+                 (unsigned long long)comps, (unsigned long long)overflow, kcna_now() - c->t0);
+        KCNA_TRY(kcna_check_device_err(c, "nndescent"));
+        if (delta <= P.delta) {
+            st->stop_condition = 1;
+            break;
+        }
+        if (recall >= P.recall) {
+            st->stop_condition = 2;
+            break;
+        }
+        if (it + 1 >= P.iterations) break;
+        KCNA_TRY(kcna_nnd_sample(c, &P, (int)it));
+    }
+    st->n_comps = comps_total;
+    return KCNA_OK;
+}

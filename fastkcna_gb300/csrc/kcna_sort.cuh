@@ -1,0 +1,96 @@
+// kcna_sort.cuh - shared-memory and warp sorting/merging primitives.
+#pragma once
+#include "kcna_common.cuh"
+
+// Ascending bitonic sort of n (a power of two) 64-bit keys in shared memory by
+// the whole thread block.  Ends with a __syncthreads.
+__device__ __forceinline__ void kcna_cta_bitonic(uint64_t *s, int n) {
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+                int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                int j = i + stride;
+                bool asc = (i & size) == 0;
+                uint64_t a = s[i], b = s[j];
+                if ((a > b) == asc) {
+                    s[i] = b;
+                    s[j] = a;
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Ascending bitonic sort of n (power of two, <= 32*E) keys in shared memory by
+// one warp (no block barrier).
+__device__ __forceinline__ void kcna_warp_bitonic(uint64_t *s, int n) {
+    const int lane = kcna_lane();
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncwarp();
+            for (int t = lane; t < (n >> 1); t += 32) {
+                int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                int j = i + stride;
+                bool asc = (i & size) == 0;
+                uint64_t a = s[i], b = s[j];
+                if ((a > b) == asc) {
+                    s[i] = b;
+                    s[j] = a;
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// Register bitonic sort of 32 keys, one per lane, ascending by lane.
+__device__ __forceinline__ uint64_t kcna_warp_sort32(uint64_t v) {
+    const int lane = kcna_lane();
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            uint64_t o = __shfl_xor_sync(KCNA_FULL, v, stride);
+            bool up = (lane & size) == 0;
+            bool lower = (lane & stride) == 0;
+            uint64_t mn = v < o ? v : o, mx = v < o ? o : v;
+            v = (up == lower) ? mn : mx;
+        }
+    }
+    return v;
+}
+
+static inline int kcna_pow2_ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+__device__ __forceinline__ int kcna_pow2_ceil_d(int x) {
+    return x <= 1 ? 1 : 1 << (32 - __clz(x - 1));
+}
+
+// Number of elements of sorted a[0..na) strictly less than key (lower bound).
+__device__ __forceinline__ int kcna_lower_bound(const uint64_t *a, int na, uint64_t key) {
+    int lo = 0, hi = na;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ int kcna_upper_bound(const uint64_t *a, int na, uint64_t key) {
+    int lo = 0, hi = na;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] <= key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}

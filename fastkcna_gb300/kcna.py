@@ -1,0 +1,284 @@
+"""ctypes binding of the C ABI in include/kcna.h (libkcna.so, built in-tree).
+
+This is the Python face of the drop-in boundary: numpy arrays in, numpy arrays
+out, status codes turned into the exception types of the reference
+(kgraph::invalid_argument -> ValueError, kgraph::io_error -> IOError,
+kgraph::runtime_error -> RuntimeError; src/kgraph.h:363-376).  There is no
+fallback: when the CUDA library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkcna.so")
+
+NSG, HNSW_LAYER, TAUMNG, ALPHAPG = 1, 2, 3, 4
+KINDS = {"nsg": NSG, "hnsw": HNSW_LAYER, "taumng": TAUMNG, "alphapg": ALPHAPG}
+SCREEN_FP32, SCREEN_BF16 = 0, 1
+MAX_ITERS, MAX_LOOPS = 64, 16
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "cuda error", 4: "timeout", 5: "io error",
+          6: "bad call order"}
+
+
+class KcnaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"kcna {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class KcnaArgError(KcnaError, ValueError):
+    pass
+
+
+class KcnaIOError(KcnaError, IOError):
+    pass
+
+
+class Params(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("K", "L", "S", "R", "iterations", "controls", "seed", "nthreads")] + [
+        ("delta", C.c_float), ("recall", C.c_float)] + [
+        (n, C.c_uint32) for n in ("nsg_R", "search_L", "search_K", "step", "massq_S", "loop_i")] + [
+        ("tau", C.c_float), ("angle", C.c_float), ("screen", C.c_uint32), ("learned_seed", C.c_uint32),
+        ("verbosity", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_uint32), ("stop_condition", C.c_uint32), ("maxl", C.c_uint32), ("loops", C.c_uint32),
+        ("iter_recall", C.c_float * MAX_ITERS), ("iter_delta", C.c_float * MAX_ITERS),
+        ("iter_time", C.c_double * MAX_ITERS), ("iter_cand_overflow", C.c_uint64 * MAX_ITERS),
+        ("loop_recall", C.c_float * (MAX_LOOPS + 1)),
+        ("prune_time", C.c_double * MAX_LOOPS), ("inter_time", C.c_double * MAX_LOOPS),
+        ("tree_grow_time", C.c_double * MAX_LOOPS), ("buildnsg_time", C.c_double * MAX_LOOPS),
+        ("search_time", C.c_double * MAX_LOOPS), ("con_time", C.c_double * MAX_LOOPS),
+        ("nndescent_time", C.c_double), ("total_time", C.c_double),
+        ("n_comps", C.c_uint64), ("prune_comps", C.c_uint64), ("bridge_comps", C.c_uint64),
+        ("screened_pairs", C.c_uint64), ("rescored_pairs", C.c_uint64),
+        ("ep", C.c_uint32), ("width", C.c_uint32), ("aod", C.c_uint32),
+        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+    def as_dict(self):
+        it = self.iterations
+        lp = self.loops
+        return dict(iterations=it, stop_condition=self.stop_condition, maxl=self.maxl, loops=lp,
+                    iter_recall=list(self.iter_recall[:it]), iter_delta=list(self.iter_delta[:it]),
+                    iter_time=list(self.iter_time[:it]), iter_cand_overflow=list(self.iter_cand_overflow[:it]),
+                    loop_recall=list(self.loop_recall[:lp]), prune_time=list(self.prune_time[:lp]),
+                    tree_grow_time=list(self.tree_grow_time[:lp]), search_time=list(self.search_time[:max(lp - 1, 0)]),
+                    con_time=list(self.con_time[:lp]), nndescent_time=self.nndescent_time,
+                    total_time=self.total_time, n_comps=self.n_comps, prune_comps=self.prune_comps,
+                    bridge_comps=self.bridge_comps, screened_pairs=self.screened_pairs,
+                    rescored_pairs=self.rescored_pairs, ep=self.ep, width=self.width, aod=self.aod,
+                    min_degree=self.min_degree, max_degree=self.max_degree)
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                          "(the CUDA library is required; there is no CPU fallback)")
+    lib = C.CDLL(path)
+    P, U32, U64, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float
+    sig = {
+        "kcna_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+        "kcna_destroy": ([P], None),
+        "kcna_last_error": ([P], C.c_char_p),
+        "kcna_version": ([], C.c_char_p),
+        "kcna_params_default": ([C.POINTER(Params)], None),
+        "kcna_upload": ([P, P, U32, U32, U64], C.c_int),
+        "kcna_upload_device": ([P, P, U32, U32, U64], C.c_int),
+        "kcna_set_size": ([P, U32], C.c_int),
+        "kcna_knn_exact": ([P, P, U32, U32, P, P], C.c_int),
+        "kcna_knn_queries": ([P, P, U32, U64, U32, P, P], C.c_int),
+        "kcna_build": ([P, C.POINTER(Params), C.c_int, C.POINTER(Stats)], C.c_int),
+        "kcna_nndescent": ([P, C.POINTER(Params), C.POINTER(Stats)], C.c_int),
+        "kcna_get_graph": ([P, P, P, P, P], C.c_int),
+        "kcna_pool_capacity": ([P, C.POINTER(U32)], C.c_int),
+        "kcna_get_pools": ([P, P, P, P, U32], C.c_int),
+        "kcna_set_pools": ([P, C.POINTER(Params), P, P, P, U32], C.c_int),
+        "kcna_prune": ([P, C.POINTER(Params), C.c_int], C.c_int),
+        "kcna_link": ([P, C.POINTER(Params), C.c_int], C.c_int),
+        "kcna_set_graph": ([P, P, P, U32, U32], C.c_int),
+        "kcna_search": ([P, P, U32, U64, P, U32, U32, P, P], C.c_int),
+        "kcna_kernel_launches": ([P], U64),
+        "kcna_write_nsg": ([P, C.c_char_p], C.c_int),
+    }
+    for name, (argt, rest) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = argt
+        f.restype = rest
+    _lib = lib
+    return lib
+
+
+def params(**kw) -> Params:
+    """IndexParams defaults (src/kgraph.h:12-40) overridden by keywords."""
+    lib = load_library()
+    p = Params()
+    lib.kcna_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KcnaArgError(1, f"unknown parameter {k}")
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+def _u32(x):
+    return np.ascontiguousarray(x, dtype=np.uint32)
+
+
+class Index:
+    """One build context on one CUDA device (the KGraph object of the reference)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.kcna_create(C.byref(h), device)
+        if rc != 0:
+            raise KcnaError(rc, f"kcna_create(device={device}) failed")
+        self.h = h
+        self.n = 0
+        self.d = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kcna_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc == 0:
+            return
+        msg = (self.lib.kcna_last_error(self.h) or b"").decode()
+        if rc == 1:
+            raise KcnaArgError(rc, msg)
+        if rc == 5:
+            raise KcnaIOError(rc, msg)
+        raise KcnaError(rc, msg)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.kcna_kernel_launches(self.h))
+
+    def upload(self, X) -> None:
+        """Host rows (n, d) float32 -> device."""
+        X = _f32(X)
+        self._check(self.lib.kcna_upload(self.h, _ptr(X), X.shape[0], X.shape[1], X.strides[0]))
+        self.n, self.d = X.shape
+
+    def upload_device(self, ptr: int, n: int, d: int, stride_bytes: int) -> None:
+        """Rows already in device memory of this context's device."""
+        self._check(self.lib.kcna_upload_device(self.h, C.c_void_p(ptr), n, d, stride_bytes))
+        self.n, self.d = n, d
+
+    def set_size(self, n_prefix: int) -> None:
+        self._check(self.lib.kcna_set_size(self.h, n_prefix))
+        self.n = min(n_prefix, self.n)
+
+    def knn_exact(self, ids, k: int):
+        ids = _u32(ids)
+        oi = np.empty((ids.size, k), np.uint32)
+        od = np.empty((ids.size, k), np.float32)
+        self._check(self.lib.kcna_knn_exact(self.h, _ptr(ids), ids.size, k, _ptr(oi), _ptr(od)))
+        return oi, od
+
+    def knn_queries(self, Q, k: int):
+        Q = _f32(Q)
+        oi = np.empty((Q.shape[0], k), np.uint32)
+        od = np.empty((Q.shape[0], k), np.float32)
+        self._check(self.lib.kcna_knn_queries(self.h, _ptr(Q), Q.shape[0], Q.strides[0], k, _ptr(oi), _ptr(od)))
+        return oi, od
+
+    def build(self, kind="nsg", p: Params | None = None, **kw) -> dict:
+        p = p or params(**kw)
+        st = Stats()
+        self._check(self.lib.kcna_build(self.h, C.byref(p), KINDS.get(kind, kind), C.byref(st)))
+        return st.as_dict()
+
+    def nndescent(self, p: Params | None = None, **kw) -> dict:
+        p = p or params(**kw)
+        st = Stats()
+        self._check(self.lib.kcna_nndescent(self.h, C.byref(p), C.byref(st)))
+        return st.as_dict()
+
+    def graph(self):
+        """(ids (n, width) padded with 0xFFFFFFFF, degrees (n,), ep)."""
+        w = C.c_uint32()
+        ep = C.c_uint32()
+        self._check(self.lib.kcna_get_graph(self.h, None, None, C.byref(ep), C.byref(w)))
+        ids = np.empty((self.n, w.value), np.uint32)
+        deg = np.empty(self.n, np.uint32)
+        self._check(self.lib.kcna_get_graph(self.h, _ptr(ids), _ptr(deg), C.byref(ep), C.byref(w)))
+        return ids, deg, int(ep.value)
+
+    def pools(self):
+        cap = C.c_uint32()
+        self._check(self.lib.kcna_pool_capacity(self.h, C.byref(cap)))
+        c = cap.value
+        ids = np.empty((self.n, c), np.uint32)
+        d = np.empty((self.n, c), np.float32)
+        cnt = np.empty(self.n, np.uint32)
+        self._check(self.lib.kcna_get_pools(self.h, _ptr(ids), _ptr(d), _ptr(cnt), c))
+        return ids, d, cnt
+
+    def set_pools(self, ids, dists, counts, p: Params | None = None, **kw):
+        p = p or params(**kw)
+        ids, dists, counts = _u32(ids), _f32(dists), _u32(counts)
+        self._check(self.lib.kcna_set_pools(self.h, C.byref(p), _ptr(ids), _ptr(dists), _ptr(counts),
+                                            ids.shape[1]))
+
+    def prune(self, kind="nsg", p: Params | None = None, **kw):
+        p = p or params(**kw)
+        self._check(self.lib.kcna_prune(self.h, C.byref(p), KINDS.get(kind, kind)))
+
+    def link(self, kind="nsg", p: Params | None = None, **kw):
+        p = p or params(**kw)
+        self._check(self.lib.kcna_link(self.h, C.byref(p), KINDS.get(kind, kind)))
+
+    def set_graph(self, ids, degrees, ep: int):
+        ids, degrees = _u32(ids), _u32(degrees)
+        self._check(self.lib.kcna_set_graph(self.h, _ptr(ids), _ptr(degrees), ids.shape[1], ep))
+
+    def search(self, Q, L: int, k: int, init_ids=None):
+        Q = _f32(Q)
+        m = Q.shape[0]
+        init = None if init_ids is None else _u32(init_ids)
+        oi = np.empty((m, k), np.uint32)
+        od = np.empty((m, k), np.float32)
+        self._check(self.lib.kcna_search(self.h, _ptr(Q), m, Q.strides[0], _ptr(init), L, k, _ptr(oi), _ptr(od)))
+        return oi, od
+
+    def write_nsg(self, path: str):
+        self._check(self.lib.kcna_write_nsg(self.h, path.encode()))
+
+
+def version() -> str:
+    return load_library().kcna_version().decode()

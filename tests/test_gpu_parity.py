@@ -1,0 +1,181 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle.
+
+Bit-exact where the path is deterministic (exact k-NN, prune, link, beam
+search); recall-based where the reference itself is stochastic (NN-descent,
+P2K refinement, full builds).
+"""
+import numpy as np
+import pytest
+
+import oracle_py
+from conftest import recall_at, rows_equal_as_sets
+from fastkcna_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+KINDS = {1: "nsg", 3: "taumng", 4: "alphapg"}
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return synth.base("c1", 6000)
+
+
+@pytest.fixture(scope="module")
+def c2():
+    return synth.base("c2", 6000)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_knn_exact_bit_identical(index, oracle, name, c1, c2):
+    X = c1 if name == "c1" else c2
+    index.upload(X)
+    ids = np.arange(0, X.shape[0], 37, dtype=np.uint32)
+    gi, gd = index.knn_exact(ids, 100)
+    oi, od = oracle.knn(X, ids, 100)
+    assert np.array_equal(gd, od)
+    assert np.array_equal(gi, oi)
+
+
+def test_knn_edge_sizes(index, oracle):
+    X = synth.base("c1", 257)  # ragged n, d=32
+    index.upload(X)
+    ids = np.array([0, 1, 255, 256], np.uint32)
+    gi, gd = index.knn_exact(ids, 256)  # k = n - 1: every other row
+    oi, od = oracle.knn(X, ids, 256)
+    assert np.array_equal(gi, oi) and np.array_equal(gd, od)
+
+
+def test_knn_queries(index, oracle, c2):
+    index.upload(c2)
+    Q = synth.queries("c2", 50)
+    gi, gd = index.knn_queries(Q, 10)
+    oi, od = oracle.knn_queries(c2, Q, 10)
+    assert np.array_equal(gi, oi) and np.array_equal(gd, od)
+
+
+def test_knn_duplicate_rows_tie_break(index, oracle):
+    X = synth.base("c2", 500)
+    X[100:200] = X[0]  # many exact ties
+    index.upload(X)
+    ids = np.array([0, 5, 150], np.uint32)
+    gi, gd = index.knn_exact(ids, 120)
+    oi, od = oracle.knn(X, ids, 120)
+    assert np.array_equal(gi, oi) and np.array_equal(gd, od)
+
+
+def _pools(oracle, X, **kw):
+    p = oracle_py.params(**kw)
+    pid, pd, pc, st = oracle.nndescent(X, p, nthreads=1)
+    return p, pid, pd, pc
+
+
+@pytest.mark.parametrize("kind", [1, 3, 4])
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_prune_bit_identical(index, oracle, kind, name, c1, c2):
+    from fastkcna_gb300 import kcna
+
+    X = c1 if name == "c1" else c2
+    tau = 0.05 if name == "c1" else 10.0
+    kw = dict(K=100, L=100, S=10, R=100, iterations=4, search_L=40, nsg_R=32, search_K=100, tau=tau, angle=60.0)
+    p, pid, pd, pc = _pools(oracle, X, **kw)
+    index.upload(X)
+    kp = kcna.params(**kw)
+    index.set_pools(pid, pd, pc, kp)
+    index.prune(KINDS[kind], kp)
+    g, deg, _ = index.graph()
+    oi, od, odeg = oracle.prune(kind, X, p, pid, pd, pc, g.shape[1])
+    assert np.array_equal(deg, odeg)
+    assert np.array_equal(g, oi)
+
+
+@pytest.mark.parametrize("kind", [1, 3, 4])
+def test_link_bit_identical(index, oracle, kind, c1):
+    from fastkcna_gb300 import kcna
+
+    kw = dict(K=100, L=100, S=10, R=100, iterations=4, search_L=40, nsg_R=16, search_K=100, tau=0.05, angle=60.0)
+    p, pid, pd, pc = _pools(oracle, c1, **kw)
+    index.upload(c1)
+    kp = kcna.params(**kw)
+    index.set_pools(pid, pd, pc, kp)
+    index.link(KINDS[kind], kp)
+    g, deg, _ = index.graph()
+    oi, od, odeg = oracle.link(kind, c1, p, pid, pd, pc, g.shape[1])
+    assert np.array_equal(deg, odeg)
+    assert rows_equal_as_sets(g, deg, oi, odeg) == 0
+    assert np.array_equal(g, oi)
+
+
+def test_beam_search_bit_identical(index, oracle, c1):
+    kw = dict(K=100, L=100, S=10, R=100, iterations=4, search_L=40, nsg_R=24, search_K=100)
+    p, pid, pd, pc = _pools(oracle, c1, **kw)
+    W = 64
+    gi, gd, gdeg = oracle.link(1, c1, p, pid, pd, pc, W)
+    index.upload(c1)
+    index.set_graph(gi, gdeg, 0)
+    Q = synth.queries("c1", 200)
+    rng = np.random.default_rng(7)
+    L = 40
+    init = np.stack([rng.choice(c1.shape[0], L, replace=False) for _ in range(Q.shape[0])]).astype(np.uint32)
+    ki, kd = index.search(Q, L, 10, init)
+    oi, od = oracle.beam_search(c1, gi, gdeg, Q, init, L, 10)
+    assert np.array_equal(ki, oi) and np.array_equal(kd, od)
+
+
+def test_nndescent_recall_matches_oracle(index, oracle):
+    X = synth.base("c1", 20000)
+    kw = dict(K=100, L=100, S=10, R=100, iterations=6, search_L=40, nsg_R=32, search_K=100, controls=100)
+    index.upload(X)
+    st = index.nndescent(**kw)
+    _, _, _, ost = oracle.nndescent(X, oracle_py.params(**kw), nthreads=8)
+    g = st["loop_recall"][0]
+    o = ost.loop_recall[0]
+    # stochastic path: the GPU's batched joins must not lose recall against the reference loop
+    assert g >= o - 0.01, (g, o, st)
+    # exact recall on a subset, independent of the control estimator
+    pid, pd, pc = index.pools()
+    ids = np.arange(0, X.shape[0], 200, dtype=np.uint32)
+    ti, _ = oracle.knn(X, ids, 100)
+    r = recall_at(pid[ids], ti, 100)
+    assert r >= o - 0.02, (r, o)
+    # pools sorted, no duplicate ids, no self
+    for i in ids:
+        row = pid[i, : pc[i]]
+        assert len(set(row.tolist())) == len(row) and i not in row
+        assert np.all(np.diff(pd[i, : pc[i]]) >= 0)
+
+
+@pytest.mark.parametrize("kind", ["nsg", "taumng", "alphapg"])
+def test_build_search_recall(index, oracle, kind):
+    X = synth.base("c1", 20000)
+    Q = synth.queries("c1", 500)
+    kw = dict(K=100, L=100, S=10, R=100, iterations=6, search_L=40, nsg_R=32, search_K=100, massq_S=10,
+              angle=60.0, tau=0.05, loop_i=2)
+    index.upload(X)
+    st = index.build(kind, **kw)
+    g, deg, ep = index.graph()
+    n = X.shape[0]
+    assert deg.max() <= 32 + 1 and np.all(g[np.arange(g.shape[1])[None, :] < deg[:, None]] < n)
+    # connectivity from the entry point (tree_grow)
+    seen = np.zeros(n, bool)
+    seen[ep] = True
+    front = [ep]
+    while front:
+        nxt = []
+        for u in front:
+            for v in g[u, : deg[u]]:
+                if not seen[v]:
+                    seen[v] = True
+                    nxt.append(v)
+        front = nxt
+    assert seen.all()
+    truth, _ = oracle.knn_queries(X, Q, 10)
+    gi, _ = index.search(Q, 64, 10)
+    r_gpu = recall_at(gi, truth, 10)
+    # the oracle build of the same kind, searched by the same GPU searcher
+    kid = {"nsg": 1, "taumng": 3, "alphapg": 4}[kind]
+    og, odeg, ost = oracle.build(kid, X, oracle_py.params(**kw), width=g.shape[1], nthreads=8)
+    index.set_graph(og, odeg, ost.ep)
+    oi, _ = index.search(Q, 64, 10)
+    r_orc = recall_at(oi, truth, 10)
+    assert r_gpu >= r_orc - 0.01, (r_gpu, r_orc, st)
