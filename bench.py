@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Headline benchmark: FastNSG graph build of a 1M x 128 dataset on one GB300.
+
+Metric: seconds per build of the FastNSG graph of the 1,000,000 x 128
+integer-valued mixture (a seeded stand-in for Sift1M) with the reference's
+C2 flags (-K 500 -L 500 -S 12 -R 100 --search_L 80 --nsg_R 50 --search_K 500
+--massq_S 10 --loop_i 2 --step 10) and --recall 0.99 as the NN-descent stop
+rule; the final KNN-graph recall@K (control recall@MAXL, the reference's
+evaluate()) is reported with every line.  One step = one full build (NN-descent,
+prune + link, entry point, tree_grow, P2K refinement).
+
+  value  device-resident: rows uploaded once before the timed region; each step
+         is kcna_build on the resident rows, timed with CUDA events on the
+         library's stream.
+  e2e    the same build through the C ABI with host buffers: every step copies
+         the rows from pinned host memory, builds, and reads the graph back.
+
+--impl reference times the reference's CPU build of the same workload on the
+host cores (the reference compiled from its sources when that library loads
+on this machine, else the oracle port), on a bounded sample of N rows,
+reported in the same unit (seconds scaled linearly to 1M rows).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1M×128 graph build s @0.99 KNN recall: learned+BF16 vs plain FP32 (1 GB300)"
+UNIT = "s"
+FLAGS = dict(K=500, L=500, S=12, R=100, iterations=12, search_L=80, nsg_R=50, search_K=500, massq_S=10,
+             loop_i=2, step=10, angle=60.0, recall=0.99, controls=100, seed=2024)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), float(j["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_build_seconds(n_sample: int, threads: int, prefer_reference: bool):
+    """One CPU build of an n_sample-row sample; returns (seconds, kind, recall)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from fastkcna_gb300 import synth
+
+    X = synth.base("c2", n_sample)
+    p = oracle_py.params(**{**FLAGS, "nthreads": threads})
+    if prefer_reference and oracle_py.Reference.available():
+        try:
+            ref = oracle_py.Reference()
+        except OSError:
+            ref = None  # the library was built for another architecture
+        if ref is not None:
+            sys.stdout.flush()
+            saved = os.dup(1)  # the reference prints progress with printf
+            devnull = os.open(os.devnull, os.O_WRONLY)
+            os.dup2(devnull, 1)
+            try:
+                t = time.perf_counter()
+                ref.build(oracle_py.KCNA_NSG, X, p, nthreads=threads)
+                dt = time.perf_counter() - t
+            finally:
+                import ctypes
+
+                ctypes.CDLL(None).fflush(None)  # drain C stdio into /dev/null before restoring
+                os.dup2(saved, 1)
+                os.close(saved)
+                os.close(devnull)
+            return dt, "reference", None
+    O = oracle_py.Oracle()
+    t = time.perf_counter()
+    _, _, st = O.build(oracle_py.KCNA_NSG, X, p, width=64, nthreads=threads)
+    return time.perf_counter() - t, "port", float(st.loop_recall[max(st.loops - 1, 0)])
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.cpu_n
+    scale = 1_000_000 / n
+    for _ in range(args.warmup):
+        cpu_build_seconds(n, threads, True)
+    times, kind = [], None
+    for _ in range(args.steps):
+        t, kind, rec = cpu_build_seconds(n, threads, True)
+        times.append(t * scale)
+    v = statistics.median(times)
+    sample = (f"FastNSG build of a {n:,}-row sample of the 1M x 128 workload (same flags), "
+              f"{threads} host threads, seconds x {scale:g} (linear in N)")
+    print(json.dumps({
+        "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(v * 1000, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c2 FastNSG 1M x 128 (CPU sample)", "n_sample": n, **FLAGS},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def roofline(st, hbm_gbs, ld):
+    """Dominant device phase with its algorithmic bytes per launch."""
+    ph, launches = st["phase_ms"], st["phase_launches"]
+    models = {
+        # join: every gathered row once + every candidate written once
+        "join": st["join_rows"] * ld * 4 + st["cand_emitted"] * 8,
+        # merge: candidates read once, pool entries read and written once
+        "merge": st["cand_merged"] * 8 + st["pool_entries_merged"] * 16,
+    }
+    name = max(models, key=lambda k: ph.get(k, 0.0))
+    ms, nl = ph[name], max(launches[name], 1)
+    per_launch_bytes = models[name] / nl
+    per_launch_s = ms / 1000.0 / nl
+    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    return name, {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
+                  "frac": round(achieved / hbm_gbs, 4), "traffic": traffic_from_profile(name),
+                  "kernel": f"{name}_kernel", "launches_per_step": int(nl)}
+
+
+def traffic_from_profile(name):
+    """DRAM bytes per launch from the committed ncu summary, when present."""
+    path = os.path.join(ROOT, "profiles", f"{name}_kernel_c2.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_gpu(args, ws, rank, local):
+    import torch
+
+    from fastkcna_gb300 import kcna, synth
+
+    torch.cuda.set_device(local)
+    n = args.n
+    X = synth.base("c2", n)
+    p = kcna.params(**FLAGS)
+    ix = kcna.Index(local)
+    stream = torch.cuda.ExternalStream(ix.stream, device=torch.device("cuda", local))
+    ix.upload(X)
+    for _ in range(args.warmup):
+        ix.build("nsg", p)
+    # timed region: device-resident rows, one build per step
+    clock = ClockSampler(local)
+    clock.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    launches0 = ix.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stats = []
+    for _ in range(args.steps):
+        stats.append(ix.build("nsg", p))
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = clock.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = (ix.launches - launches0) // args.steps
+    ms = max_over_ranks(ws, ms)
+    # end-to-end through the C ABI with host buffers (pinned)
+    Xh = torch.empty((n, X.shape[1]), dtype=torch.float32, pin_memory=True)
+    Xh.numpy()[:] = X
+    W = None
+    e2e = []
+    for i in range(args.steps + 1):
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc = ix.lib.kcna_upload(ix.h, Xh.data_ptr(), n, X.shape[1], X.shape[1] * 4)
+        if rc != 0:
+            raise RuntimeError(f"kcna_upload failed: {rc}")
+        ix.build("nsg", p)
+        g, deg, ep = ix.graph()
+        e1.record(stream)
+        e1.synchronize()
+        if i > 0:  # first e2e step re-warms the allocator
+            e2e.append(e0.elapsed_time(e1) / 1000.0)
+        W = g.shape[1]
+    e2e_s = max_over_ranks(ws, statistics.median(e2e))
+    st = stats[-1]
+    hbm, bf16, src = peaks()
+    kname, roof = roofline(st, hbm, (X.shape[1] + 3) // 4 * 4)
+    roof["peak_source"] = f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
+    final_recall = st["loop_recall"][-1]
+    line = {
+        "metric": METRIC, "value": round(ms / 1000.0, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c2 FastNSG 1M x 128 (integer-valued 256-cluster mixture)", "n": n,
+                   "mode": "plain FP32", "l2_policy": "inputs larger than L2 (rows 512 MB, pools 4 GB)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU", **FLAGS,
+                   "knn_recall_at_K": round(final_recall, 4),
+                   "nndescent_iterations": st["iterations"],
+                   "nndescent_recall": [round(x, 4) for x in st["iter_recall"]],
+                   "phase_ms": {k: round(v, 2) for k, v in st["phase_ms"].items() if v},
+                   "dist_evals_per_s": round((st["n_comps"] + st["prune_comps"] + st["bridge_comps"]) / (ms / 1000.0)),
+                   "cand_overflow": sum(st["iter_cand_overflow"])},
+        "gpu_launches": int(launches),
+        "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
+                "d2h_bytes_per_step": int(n * W * 4 + n * 4 + 8)},
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        t, kind, rec = cpu_build_seconds(args.cpu_n, threads, True)
+        scale = 1_000_000 / args.cpu_n
+        line["cpu_baseline"] = {"value": round(t * scale, 3), "unit": UNIT, "cores": threads, "kind": kind,
+                                "sample": f"one FastNSG build of a {args.cpu_n:,}-row sample of the workload, "
+                                          f"same flags, {t:.2f} s x {scale:g} (linear in N)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ix.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--cpu-n", type=int, default=50_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

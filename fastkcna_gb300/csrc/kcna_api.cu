@@ -54,6 +54,42 @@ kcna_status kcna_check_device_err(kcna_ctx *c, const char *phase) {
     return kcna_fail(c, h == 2 ? KCNA_E_TIMEOUT : KCNA_E_CUDA, std::string(phase) + ": device error: " + what);
 }
 
+kcna_status kcna_phase_begin(kcna_ctx *c) {
+    c->launches_at_begin = c->launches;
+    return kcna_cuda_check(c, cudaEventRecord(c->ev0, c->stream), "event record");
+}
+
+kcna_status kcna_phase_end(kcna_ctx *c, int phase) {
+    KCNA_TRY(kcna_cuda_check(c, cudaEventRecord(c->ev1, c->stream), "event record"));
+    KCNA_TRY(kcna_cuda_check(c, cudaEventSynchronize(c->ev1), "event sync"));
+    float ms = 0.f;
+    KCNA_TRY(kcna_cuda_check(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event elapsed"));
+    if (phase >= 0 && phase < KCNA_NUM_PHASES) {
+        c->phase_ms[phase] += ms;
+        c->phase_launches[phase] += c->launches - c->launches_at_begin;
+    }
+    return KCNA_OK;
+}
+
+static void reset_phase_stats(kcna_ctx *c) {
+    for (int i = 0; i < KCNA_NUM_PHASES; ++i) {
+        c->phase_ms[i] = 0;
+        c->phase_launches[i] = 0;
+    }
+    c->join_rows = c->cand_emitted = c->cand_merged = c->pool_entries_merged = 0;
+}
+
+static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
+    for (int i = 0; i < KCNA_NUM_PHASES; ++i) {
+        st->phase_ms[i] = c->phase_ms[i];
+        st->phase_launches[i] = c->phase_launches[i];
+    }
+    st->join_rows = c->join_rows;
+    st->cand_emitted = c->cand_emitted;
+    st->cand_merged = c->cand_merged;
+    st->pool_entries_merged = c->pool_entries_merged;
+}
+
 static kcna_status grow(kcna_ctx *c, void **p, size_t *cur, size_t bytes) {
     if (*cur >= bytes && *p) return KCNA_OK;
     if (*p) cudaFree(*p);
@@ -161,6 +197,8 @@ kcna_status kcna_create(kcna_ctx **out, int device) {
     if (s == KCNA_OK) s = kcna_alloc(c, &c->d_err, 1, "error word");
     if (s == KCNA_OK) s = kcna_alloc(c, &c->counters, 64, "counters");
     if (s == KCNA_OK) s = kcna_cuda_check(c, cudaMemset(c->d_err, 0, 4), "memset");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaEventCreate(&c->ev0), "event");
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaEventCreate(&c->ev1), "event");
     if (s != KCNA_OK) {
         kcna_destroy(c);
         return s;
@@ -179,6 +217,8 @@ void kcna_destroy(kcna_ctx *c) {
     if (c->scratch2) cudaFree(c->scratch2);
     if (c->d_err) cudaFree(c->d_err);
     if (c->counters) cudaFree(c->counters);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -186,6 +226,8 @@ void kcna_destroy(kcna_ctx *c) {
 const char *kcna_last_error(const kcna_ctx *c) { return c ? c->err.c_str() : "no context"; }
 
 uint64_t kcna_kernel_launches(const kcna_ctx *c) { return c ? c->launches : 0; }
+
+void *kcna_stream(const kcna_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 static kcna_status upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d, uint64_t stride, cudaMemcpyKind kind) {
     if (!c) return KCNA_E_ARG;
@@ -297,6 +339,7 @@ kcna_status kcna_nndescent(kcna_ctx *c, const kcna_params *p, kcna_stats *st) {
     if (!st) st = &local;
     memset(st, 0, sizeof *st);
     free_state(c);
+    reset_phase_stats(c);
     c->t0 = kcna_now();
     KCNA_TRY(kcna_nndescent_run(c, p, st));
     float r = 0;
@@ -304,6 +347,7 @@ kcna_status kcna_nndescent(kcna_ctx *c, const kcna_params *p, kcna_stats *st) {
     st->loop_recall[0] = r;
     st->nndescent_time = kcna_now() - c->t0;
     st->total_time = st->nndescent_time;
+    copy_phase_stats(c, st);
     return kcna_check_device_err(c, "nndescent");
 }
 
@@ -337,6 +381,7 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
     if (!st) st = &local;
     memset(st, 0, sizeof *st);
     free_state(c);
+    reset_phase_stats(c);
     c->t0 = kcna_now();
     kcna_params P = *p;
     KCNA_TRY(kcna_nndescent_run(c, &P, st));
@@ -388,6 +433,7 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
     st->bridge_comps = bridge_comps;
     KCNA_TRY(degree_stats(c, st));
     st->total_time = kcna_now() - c->t0;
+    copy_phase_stats(c, st);
     return kcna_check_device_err(c, "build");
 }
 

@@ -882,11 +882,13 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     PruneRule rule = make_rule(p, kind);
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 16, 0, 8, c->stream), "memset"));
     size_t sm = (size_t)PW * 2 * range * 4;
+    KCNA_TRY(kcna_phase_begin(c));
     prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
         c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, (int)std::min(p->search_K, c->cap),
         c->g_ids, c->g_dist, c->g_deg, c->W, c->counters + 16);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
+    KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_PRUNE));
     unsigned long long h = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 16, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "prune sync"));
@@ -913,6 +915,7 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     if ((s = kcna_alloc(c, &indeg, N, "indeg")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &off, N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
     cudaMemsetAsync(indeg, 0, N * 4, c->stream);
     cudaMemsetAsync(cursor, 0, N * 4, c->stream);
     rev_count_kernel<<<kcna_div_up(N * W, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, (uint32_t)N, W, indeg);
@@ -933,7 +936,7 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     unsigned long long h = 0;
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 17, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
-    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync");
+    if (s == KCNA_OK) s = kcna_phase_end(c, KCNA_PHASE_LINK);
     cleanup();
     if (comps) *comps = pc + h;
     return s == KCNA_OK ? kcna_check_device_err(c, "link") : s;
@@ -983,6 +986,7 @@ kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     if ((s = kcna_alloc(c, &init, Lw, "init ids")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &oid, Lw, "ep ids")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &od, Lw, "ep dists")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
     centroid_partial_kernel<<<nb, 128, 0, c->stream>>>(c->X, (int)ld, nrows, (int)d, part);
     centroid_final_kernel<<<1, 128, 0, c->stream>>>(part, nb, (int)d, (int)ld, nrows, center);
     c->launches += 2;
@@ -1009,7 +1013,7 @@ kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     if ((s = kcna_search_device(c, center, 1, init, Lw, 1, oid, od)) != KCNA_OK) return cleanup(), s;
     uint32_t ep = 0;
     cudaMemcpyAsync(&ep, oid, 4, cudaMemcpyDeviceToHost, c->stream);
-    s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "ep sync");
+    s = kcna_phase_end(c, KCNA_PHASE_EP);
     cleanup();
     if (s == KCNA_OK) c->ep = ep < c->n ? ep : 0;
     return s;
@@ -1029,6 +1033,7 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     if ((s = kcna_alloc(c, &qa, N, "frontier")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &qb, N, "frontier")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cntd, 1, "count")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
     cudaMemsetAsync(vis, 0, (size_t)words * 4, c->stream);
     uint32_t ep = c->ep, bit = 1u << (ep & 31);
     cudaMemcpyAsync(vis + (ep >> 5), &bit, 4, cudaMemcpyHostToDevice, c->stream);
@@ -1048,7 +1053,7 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
                                            c->g_deg, c->W, p->nsg_R, vis, qa, qb, seed, c->d_err, c->counters + 18);
     KCNA_LAUNCHED(c);
     s = kcna_cuda_check(c, cudaGetLastError(), "attach");
-    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach sync");
+    if (s == KCNA_OK) s = kcna_phase_end(c, KCNA_PHASE_TREE);
     cleanup();
     return s == KCNA_OK ? kcna_check_device_err(c, "tree_grow") : s;
 }
@@ -1091,6 +1096,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     // the reference loops until a thin round; 100 rounds bound it here
     for (int round = 0; round < 100; ++round) {
         // capped round: count, then the uncapped remainder when the round is thin
+        if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
         cudaMemsetAsync(tcount, 0, (size_t)N * 4, c->stream);
         bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 1, 0, tcount,
                                                              nullptr, nullptr, 0);
@@ -1140,7 +1146,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         KCNA_LAUNCHED(c);
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, c->counters + 21, 8, cudaMemcpyDeviceToHost, c->stream);
-        if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bridge join")) != KCNA_OK) return cleanup(), s;
+        if ((s = kcna_phase_end(c, KCNA_PHASE_P2K)) != KCNA_OK) return cleanup(), s;
         total_comps += h;
         uint64_t ovf = 0, fl = 0;
         if ((s = kcna_merge(c, maxl, maxl, &ovf, &fl)) != KCNA_OK) return cleanup(), s;

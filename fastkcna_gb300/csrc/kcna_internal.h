@@ -64,7 +64,19 @@ struct kcna_ctx {
 
     kcna_stats *stats = nullptr;
     double t0 = 0;
+
+    // phase timing with CUDA events on `stream`
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double phase_ms[KCNA_NUM_PHASES] = {};
+    uint64_t phase_launches[KCNA_NUM_PHASES] = {};
+    uint64_t launches_at_begin = 0;
+    uint64_t join_rows = 0, cand_emitted = 0, cand_merged = 0, pool_entries_merged = 0;
 };
+
+// Brackets one phase with events on the context stream; end() waits for the
+// phase and adds its device time and launch count.
+kcna_status kcna_phase_begin(kcna_ctx *c);
+kcna_status kcna_phase_end(kcna_ctx *c, int phase);
 
 // error plumbing
 kcna_status kcna_fail(kcna_ctx *c, kcna_status s, const std::string &msg);

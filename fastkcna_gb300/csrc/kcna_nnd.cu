@@ -157,7 +157,8 @@ __device__ void take_reverse(const uint32_t *src, uint32_t cnt, uint32_t RB, uin
 
 template <int RI> // rows per thread = RI, tile rows = 32 * RI
 __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
-                           float *s_As, float *s_Bs, float *s_D, const float *s_radA, int *s_any) {
+                           float *s_As, float *s_Bs, float *s_D, const float *s_radA, int *s_any,
+                           unsigned *s_emit) {
     constexpr int RA = 32 * RI;
     const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3; // 8 col groups x 32 row groups
     const int ncol = na + nb;
@@ -248,7 +249,10 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
                 uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
                 if (p < a.CB) dst[p] = keys[1];
             }
-            if (lane == 0) *s_any = 1;
+            if (lane == 0) {
+                *s_any = 1;
+                atomicAdd(s_emit, (unsigned)cnt);
+            }
         }
         // column targets: column id receives row ids
         for (int cl = warp; cl < cend; cl += nwarp) {
@@ -287,7 +291,10 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
                 }
                 run += __popc(mk[h]);
             }
-            if (lane == 0) *s_any = 1;
+            if (lane == 0) {
+                *s_any = 1;
+                atomicAdd(s_emit, (unsigned)cnt);
+            }
         }
         __syncthreads();
     }
@@ -303,6 +310,7 @@ __global__ void __launch_bounds__(JT) join_kernel(JoinArgs a) {
     uint32_t *s_B = s_A + a.capA;                                 // capB
     __shared__ uint32_t s_na, s_nb, s_tmp;
     __shared__ int s_any;
+    __shared__ unsigned s_emit;
     const uint32_t node = blockIdx.x;
     if (threadIdx.x == 0) s_any = 0;
     // new list: forward new then a random subset (<= R) of reverse new
@@ -325,15 +333,21 @@ __global__ void __launch_bounds__(JT) join_kernel(JoinArgs a) {
     for (int i = threadIdx.x; i < na; i += blockDim.x) s_radA[i] = __ldg(a.radius + s_A[i]);
     __syncthreads();
     if (na == 0) return;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         atomicAdd(a.counters + 0, (unsigned long long)((uint64_t)na * (na - 1) / 2 + (uint64_t)na * nb));
+        atomicAdd(a.counters + 5, (unsigned long long)(na + nb));
+        s_emit = 0;
+    }
     if (na <= 32)
-        join_tiles<1>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
+        join_tiles<1>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
     else if (na <= 64)
-        join_tiles<2>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
+        join_tiles<2>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
     else
-        join_tiles<4>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any);
-    if (threadIdx.x == 0) a.found[node] = s_any ? 1 : 0;
+        join_tiles<4>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+    if (threadIdx.x == 0) {
+        a.found[node] = s_any ? 1 : 0;
+        if (s_emit) atomicAdd(a.counters + 6, (unsigned long long)s_emit);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -454,6 +468,8 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a) {
         atomicAdd(a.counters + 1, s_flagged);
         if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
         atomicAdd(a.counters + 3, (unsigned long long)(newcnt - min(np, newcnt)));
+        atomicAdd(a.counters + 7, (unsigned long long)nc);
+        atomicAdd(a.counters + 9, (unsigned long long)newcnt);
         a.pool_cnt[node] = newcnt;
         a.cand_cnt[node] = 0;
     }
@@ -636,6 +652,7 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
 
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p) {
     if (p->S == 0 || p->S > 31) return kcna_fail(c, KCNA_E_ARG, "S must be in [1, 31]");
+    KCNA_TRY(kcna_phase_begin(c));
     init_kernel<<<kcna_div_up(c->n, 4), 128, 0, c->stream>>>(c->X, (int)c->ld, c->n, p->S, c->cap, p->seed, c->pool,
                                                            c->pool_cnt, c->fwd_new, c->fwd_new_cap, c->fwd_new_cnt);
     KCNA_LAUNCHED(c);
@@ -645,7 +662,7 @@ kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p) {
     std::vector<uint32_t> Ms(c->n, p->S);
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->M, Ms.data(), (size_t)c->n * 4, cudaMemcpyHostToDevice, c->stream),
                              "M init"));
-    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "init sync"));
+    KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_INIT));
     c->has_pools = true;
     return KCNA_OK;
 }
@@ -682,14 +699,18 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "join smem attr"));
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
+    KCNA_TRY(kcna_phase_begin(c));
     join_kernel<<<c->n, JT, sm, c->stream>>>(a);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "join_kernel"));
-    unsigned long long h = 0;
-    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_JOIN));
+    unsigned long long h[8] = {};
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 8 * 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "join sync"));
-    if (n_comps) *n_comps = h;
+    if (n_comps) *n_comps = h[0];
+    c->join_rows += h[5];
+    c->cand_emitted += h[6];
     return KCNA_OK;
 }
 
@@ -709,13 +730,17 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "merge smem attr"));
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 1, 0, 3 * 8, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
+    KCNA_TRY(kcna_phase_begin(c));
     merge_kernel<<<c->n, MT, sm, c->stream>>>(a);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
-    unsigned long long h[4] = {0, 0, 0, 0};
-    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 32, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_MERGE));
+    unsigned long long h[10] = {};
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 10 * 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "merge sync"));
+    c->cand_merged += h[7];
+    c->pool_entries_merged += h[9];
     if (overflow) *overflow = h[2];
     if (flagged_topk) *flagged_topk = h[1];
     return KCNA_OK;
@@ -724,6 +749,7 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter) {
     (void)iter;
     cudaStream_t s = c->stream;
+    KCNA_TRY(kcna_phase_begin(c));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rnew_cnt, 0, (size_t)c->n * 4, s), "memset"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rold_cnt, 0, (size_t)c->n * 4, s), "memset"));
     sample_m_kernel<<<kcna_div_up(c->n, 8), 256, 0, s>>>(c->pool, c->pool_cnt, c->cap, c->n, p->S, c->found, c->M,
@@ -734,7 +760,8 @@ kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter) {
                                                               c->fwd_old_cap, c->fwd_old_cnt, c->rnew, c->rnew_cnt,
                                                               c->rold, c->rold_cnt, c->RB, c->counters);
     KCNA_LAUNCHED(c);
-    return kcna_cuda_check(c, cudaGetLastError(), "sample kernels");
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "sample kernels"));
+    return kcna_phase_end(c, KCNA_PHASE_SAMPLE);
 }
 
 kcna_status kcna_pools_set_radius(kcna_ctx *c, uint32_t limit) {
@@ -764,11 +791,13 @@ kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl
     float *dd = nullptr, *rows = nullptr;
     KCNA_TRY(kcna_alloc(c, &dd, (size_t)C * maxl, "control dists"));
     KCNA_TRY(kcna_alloc(c, &rows, (size_t)C * c->ld, "control rows"));
-    kcna_status st = kcna_cuda_check(c, cudaMemcpyAsync(c->d_controls, c->control_ids.data(), C * 4,
-                                                        cudaMemcpyHostToDevice, c->stream), "h2d");
+    kcna_status st = kcna_phase_begin(c);
+    if (st == KCNA_OK)
+        st = kcna_cuda_check(c, cudaMemcpyAsync(c->d_controls, c->control_ids.data(), C * 4, cudaMemcpyHostToDevice,
+                                                c->stream), "h2d");
     if (st == KCNA_OK) st = kcna_gather_rows(c, c->d_controls, C, rows);
     if (st == KCNA_OK) st = kcna_knn_device(c, rows, C, c->d_controls, maxl, c->d_control_knn, dd);
-    if (st == KCNA_OK) st = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "controls sync");
+    if (st == KCNA_OK) st = kcna_phase_end(c, KCNA_PHASE_CONTROLS);
     cudaFree(dd);
     cudaFree(rows);
     return st;
@@ -781,6 +810,7 @@ kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall) {
         return KCNA_OK;
     }
     K = std::min(K, c->control_k);
+    KCNA_TRY(kcna_phase_begin(c));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 8, 0, 8, c->stream), "memset"));
     size_t sm = (size_t)kcna_pow2_ceil((int)K) * 8;
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(control_recall_kernel,
@@ -791,6 +821,7 @@ kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall) {
                                                      c->control_k, K, c->counters + 8);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "control_recall"));
+    KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_CONTROLS));
     unsigned long long h = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 8, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "recall sync"));

@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(HERE, "libkcna.so")
 NSG, HNSW_LAYER, TAUMNG, ALPHAPG = 1, 2, 3, 4
 KINDS = {"nsg": NSG, "hnsw": HNSW_LAYER, "taumng": TAUMNG, "alphapg": ALPHAPG}
 SCREEN_FP32, SCREEN_BF16 = 0, 1
-MAX_ITERS, MAX_LOOPS = 64, 16
+MAX_ITERS, MAX_LOOPS, NUM_PHASES = 64, 16, 12
+PHASES = ["join", "merge", "sample", "prune", "link", "p2k", "ep", "tree", "controls", "init", "other", "spare"]
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "cuda error", 4: "timeout", 5: "io error",
           6: "bad call order"}
 
@@ -59,7 +60,10 @@ class Stats(C.Structure):
         ("n_comps", C.c_uint64), ("prune_comps", C.c_uint64), ("bridge_comps", C.c_uint64),
         ("screened_pairs", C.c_uint64), ("rescored_pairs", C.c_uint64),
         ("ep", C.c_uint32), ("width", C.c_uint32), ("aod", C.c_uint32),
-        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
+        ("phase_ms", C.c_double * NUM_PHASES), ("phase_launches", C.c_uint64 * NUM_PHASES),
+        ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
+        ("pool_entries_merged", C.c_uint64)]
 
     def as_dict(self):
         it = self.iterations
@@ -67,13 +71,17 @@ class Stats(C.Structure):
         return dict(iterations=it, stop_condition=self.stop_condition, maxl=self.maxl, loops=lp,
                     iter_recall=list(self.iter_recall[:it]), iter_delta=list(self.iter_delta[:it]),
                     iter_time=list(self.iter_time[:it]), iter_cand_overflow=list(self.iter_cand_overflow[:it]),
-                    loop_recall=list(self.loop_recall[:lp]), prune_time=list(self.prune_time[:lp]),
+                    loop_recall=list(self.loop_recall[:max(lp, 1)]), prune_time=list(self.prune_time[:lp]),
                     tree_grow_time=list(self.tree_grow_time[:lp]), search_time=list(self.search_time[:max(lp - 1, 0)]),
                     con_time=list(self.con_time[:lp]), nndescent_time=self.nndescent_time,
                     total_time=self.total_time, n_comps=self.n_comps, prune_comps=self.prune_comps,
                     bridge_comps=self.bridge_comps, screened_pairs=self.screened_pairs,
                     rescored_pairs=self.rescored_pairs, ep=self.ep, width=self.width, aod=self.aod,
-                    min_degree=self.min_degree, max_degree=self.max_degree)
+                    min_degree=self.min_degree, max_degree=self.max_degree,
+                    phase_ms={PHASES[i]: self.phase_ms[i] for i in range(NUM_PHASES)},
+                    phase_launches={PHASES[i]: int(self.phase_launches[i]) for i in range(NUM_PHASES)},
+                    join_rows=self.join_rows, cand_emitted=self.cand_emitted, cand_merged=self.cand_merged,
+                    pool_entries_merged=self.pool_entries_merged)
 
 
 _lib = None
@@ -110,6 +118,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "kcna_set_graph": ([P, P, P, U32, U32], C.c_int),
         "kcna_search": ([P, P, U32, U64, P, U32, U32, P, P], C.c_int),
         "kcna_kernel_launches": ([P], U64),
+        "kcna_stream": ([P], C.c_void_p),
         "kcna_write_nsg": ([P, C.c_char_p], C.c_int),
     }
     for name, (argt, rest) in sig.items():
@@ -183,6 +192,11 @@ class Index:
         if rc == 5:
             raise KcnaIOError(rc, msg)
         raise KcnaError(rc, msg)
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.lib.kcna_stream(self.h) or 0)
 
     @property
     def launches(self) -> int:

@@ -83,6 +83,20 @@ void kcna_params_default(kcna_params *p);
  * (SaveResult, src/kgraph.cpp:1725-1807) and IndexInfo (src/kgraph.h:186-198). */
 #define KCNA_MAX_ITERS 64
 #define KCNA_MAX_LOOPS 16
+#define KCNA_NUM_PHASES 12
+enum {
+    KCNA_PHASE_JOIN = 0,     /* NN-descent local join */
+    KCNA_PHASE_MERGE = 1,    /* candidate merge into pools (NN-descent and P2K) */
+    KCNA_PHASE_SAMPLE = 2,   /* new/old sampling and reverse lists */
+    KCNA_PHASE_PRUNE = 3,    /* occlusion prune of the pools */
+    KCNA_PHASE_LINK = 4,     /* reverse edges + re-prune */
+    KCNA_PHASE_P2K = 5,      /* P2K pushes and join */
+    KCNA_PHASE_EP = 6,       /* centroid + entry-point beam search */
+    KCNA_PHASE_TREE = 7,     /* reachability + attach */
+    KCNA_PHASE_CONTROLS = 8, /* exact k-NN of the controls + recall */
+    KCNA_PHASE_INIT = 9,     /* pool initialisation */
+    KCNA_PHASE_OTHER = 10
+};
 typedef struct {
     uint32_t iterations;       /* NN-descent iterations run */
     uint32_t stop_condition;   /* 0 ITERATION, 1 DELTA, 2 RECALL (IndexInfo::StopCondition) */
@@ -111,6 +125,15 @@ typedef struct {
     uint32_t aod;              /* average out-degree (CalculateNSG, :2273-2293) */
     uint32_t min_degree, max_degree;
     uint32_t reserved[3];
+    /* Device time per phase, measured with CUDA events on the context stream
+     * (milliseconds, summed over the build), and kernel launches per phase.
+     * Phases: see KCNA_PHASE_* below. */
+    double phase_ms[KCNA_NUM_PHASES];
+    uint64_t phase_launches[KCNA_NUM_PHASES];
+    uint64_t join_rows;        /* rows gathered by the NN-descent joins (new + old lists) */
+    uint64_t cand_emitted;     /* candidates written to buffers (join + P2K) */
+    uint64_t cand_merged;      /* candidates read by the merges */
+    uint64_t pool_entries_merged; /* pool entries rewritten by the merges */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;
@@ -185,6 +208,9 @@ kcna_status kcna_search(kcna_ctx *ctx, const float *queries, uint32_t m, uint64_
 
 /* Number of kernels this context has launched so far. */
 uint64_t kcna_kernel_launches(const kcna_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), so that a caller can order its
+ * own work or timing events against the library's kernels. */
+void *kcna_stream(const kcna_ctx *ctx);
 
 /* Writes the graph in the NSG/efanna format written by SaveNsg
  * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */

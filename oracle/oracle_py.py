@@ -47,6 +47,9 @@ class Stats(C.Structure):
         ("screened_pairs", C.c_uint64), ("rescored_pairs", C.c_uint64),
         ("ep", C.c_uint32), ("width", C.c_uint32), ("aod", C.c_uint32),
         ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
+        ("phase_ms", C.c_double * 12), ("phase_launches", C.c_uint64 * 12),
+        ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
+        ("pool_entries_merged", C.c_uint64),
     ]
 
 
