@@ -212,6 +212,32 @@ uint64_t kcna_kernel_launches(const kcna_ctx *ctx);
  * own work or timing events against the library's kernels. */
 void *kcna_stream(const kcna_ctx *ctx);
 
+/* Exact k-NN that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc where they need neighbours: code that
+ * runs under a fixed memory budget and hands out device memory only through its
+ * own arena, or a plugin called from inside a host framework that owns the
+ * device allocator.  Base rows, queries and outputs are caller-owned DEVICE
+ * buffers (base n x d, pitch base_stride_bytes; queries m x d, pitch
+ * q_stride_bytes; outputs m x k ids and squared L2 distances, ties broken by
+ * the lower id, identical to kcna_knn_queries).  The only working memory is one
+ * static device array of KCNA_NOALLOC_SCRATCH_BYTES (16 MiB) inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits; queries are processed in batches of (16 MiB - 256 B) / (4 n) rows.
+ * Limits (KCNA_E_ARG otherwise): n * 4 <= 16 MiB - 256 B (n <= 4,194,240),
+ * 1 <= k <= min(n, 1024), d a multiple of 4, strides multiples of 16 bytes,
+ * 16-byte aligned pointers.  Runs on `stream` (a cudaStream_t, NULL = the
+ * legacy default stream) of the current device and synchronises it before
+ * returning.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  All calls share the one array: calls whose kernels
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Each call clears the array's error word itself. */
+#define KCNA_NOALLOC_SCRATCH_BYTES (16u << 20)
+kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n, uint32_t d, uint64_t base_stride_bytes,
+                                     const float *d_queries, uint32_t m, uint64_t q_stride_bytes, uint32_t k,
+                                     uint32_t *d_out_ids, float *d_out_dists, void *stream);
+
 /* Writes the graph in the NSG/efanna format written by SaveNsg
  * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */
 kcna_status kcna_write_nsg(kcna_ctx *ctx, const char *path);
