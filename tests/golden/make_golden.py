@@ -1,0 +1,65 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+Runs the reference's own code (oracle/_ref/libkcna_ref.so, compiled from the
+reference sources by oracle/build_ref.sh) on two small seeded datasets and
+stores its outputs:
+  * exact k-NN (LinearSearch, src/kgraph.cpp:309-330) of 40 rows, k = 48;
+  * NN-descent pools (KGraphConstructor, src/kgraph.cpp:1281-1459, one thread);
+  * sync_prune edge lists of the three kinds on those pools
+    (src/kgraph.cpp:1809-1851, 2833-2876, 3157-3203);
+  * Link (prune + InterInsert + reversed prune) of the three kinds, one thread
+    (src/kgraph.cpp:2087-2143, 3085-3141, 3424-3480);
+  * beam search (get_neighbors, src/kgraph.cpp:1560-1623) of 20 queries over
+    the NSG link graph from fixed seed ids.
+The datasets are stored with the outputs (C2-like rows as uint8).
+
+Usage: python tests/golden/make_golden.py   (needs oracle/_ref built here)
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle_py  # noqa: E402
+from fastkcna_gb300 import synth  # noqa: E402
+
+N, K, W = 1000, 48, 40
+PARAMS = dict(K=K, L=K, S=8, R=48, iterations=5, search_L=24, nsg_R=16, search_K=K, controls=20, massq_S=8,
+              angle=60.0)
+
+
+def make(name, X, tau):
+    ref = oracle_py.Reference()
+    p = oracle_py.params(**PARAMS, tau=tau)
+    out = {"X": X.astype(np.uint8) if name == "c2" else X, "tau": np.float32(tau)}
+    ids = np.arange(0, N, 25, dtype=np.uint32)
+    out["knn_ids"], out["knn_d"] = ref.linear_search(X, ids, K)
+    out["knn_q"] = ids
+    pid, pd, pc, rec, fin = ref.nndescent(X, p, nthreads=1)
+    out["pool_ids"], out["pool_d"], out["pool_cnt"] = pid, pd, pc
+    for kind, tag in ((1, "nsg"), (3, "tau"), (4, "alpha")):
+        gi, gd, deg = ref.prune(kind, X, p, pid, pd, pc, W)
+        out[f"prune_{tag}_ids"], out[f"prune_{tag}_deg"] = gi, deg
+        gi, gd, deg = ref.link(kind, X, p, pid, pd, pc, W)
+        out[f"link_{tag}_ids"], out[f"link_{tag}_deg"] = gi, deg
+    rng = np.random.default_rng(11)
+    Q = synth.queries(name, 20)
+    if name == "c2":
+        Q = np.rint(Q)
+    init = np.stack([rng.choice(N, 24, replace=False) for _ in range(20)]).astype(np.uint32)
+    bi, bd = ref.beam_search(X, out["link_nsg_ids"], out["link_nsg_deg"], Q, init, 24, 10)
+    out.update(bs_q=Q.astype(np.float32), bs_init=init, bs_ids=bi, bs_d=bd)
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+
+
+if __name__ == "__main__":
+    if not oracle_py.Reference.available():
+        sys.exit("oracle/_ref/libkcna_ref.so is missing: run oracle/build_ref.sh")
+    make("c1", synth.base("c1", N), 0.05)
+    make("c2", synth.base("c2", N), 10.0)
+    print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

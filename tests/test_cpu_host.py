@@ -1,0 +1,155 @@
+"""CPU-only tests: the C ABI exports, pool-insert semantics, the dataset
+generator, the live reference pins (where the reference compiled here) and the
+bench's host logic (reference arm, two-rank gloo)."""
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import oracle_py
+from conftest import ROOT
+from fastkcna_gb300 import synth
+
+
+def test_abi_exports_every_declared_function():
+    import ctypes
+
+    lib_path = os.path.join(ROOT, "fastkcna_gb300", "libkcna.so")
+    if not os.path.exists(lib_path):
+        from fastkcna_gb300 import build
+
+        build.build()
+    lib = ctypes.CDLL(lib_path)  # loads without a GPU; nothing is called
+    header = open(os.path.join(ROOT, "include", "kcna.h")).read()
+    header = re.sub(r"/\*.*?\*/", "", header, flags=re.S)
+    names = sorted(set(re.findall(r"\b(kcna_\w+)\s*\(", header)))
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def _model_pool(L, cap, entries):
+    """Top-`cap` by (distance, insertion order) of unique ids: what the
+    sequential try-insert keeps when no distance ties at the boundary."""
+    best = {}
+    for i, (idx, d) in enumerate(entries):
+        if idx not in best:
+            best[idx] = (d, i)
+    order = sorted(best.items(), key=lambda kv: kv[1])
+    return [k for k, _ in order[:cap]]
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_pool_insert_matches_top_l_model(oracle, seed):
+    rng = np.random.default_rng(seed)
+    cap = 32
+    ids0 = rng.choice(10_000, 10, replace=False).astype(np.uint32)
+    d0 = np.sort(rng.random(10).astype(np.float32))
+    cid = rng.integers(0, 10_000, 400).astype(np.uint32)
+    cd = rng.random(400).astype(np.float32)
+    # same id always has the same distance (the distance of a pair is a function of the pair)
+    dist_of = {int(i): float(d) for i, d in zip(ids0, d0)}
+    for j in range(cid.size):
+        cd[j] = dist_of.setdefault(int(cid[j]), float(cd[j]))
+    ids, dists, flags, L, rad, ret = oracle.pool_insert_seq(ids0, d0, np.zeros(10, np.uint8), 10, cap, np.inf,
+                                                            cid, cd)
+    assert L == cap and np.all(np.diff(dists) >= 0) and len(set(ids.tolist())) == L
+    model = _model_pool(L, cap, list(zip(ids0.tolist(), d0.tolist())) + list(zip(cid.tolist(), cd.tolist())))
+    assert ids.tolist() == model
+    assert rad == dists[-1]
+
+
+def test_synth_shapes_and_ranges():
+    x = synth.base("c2", 4096)
+    assert x.shape == (4096, 128) and x.dtype == np.float32
+    assert x.min() >= 0 and x.max() <= 255 and np.all(x == np.rint(x))
+    y = synth.base("c3", 1000)
+    np.testing.assert_allclose(np.linalg.norm(y, axis=1), 1.0, rtol=1e-5)
+    z = synth.base("c4", 100)
+    assert z.shape == (100, 960) and z.min() >= 0
+    assert np.array_equal(synth.base("c1", 500), synth.base("c1", 500))
+
+
+def test_lshkit_round_trip(tmp_path):
+    x = synth.base("c1", 300)
+    p = str(tmp_path / "x.lshkit")
+    synth.write_lshkit(p, x)
+    assert np.array_equal(synth.read_lshkit(p), x)
+    raw = np.fromfile(p, dtype=np.uint32, count=3)
+    assert raw.tolist() == [4, 300, 32]
+
+
+needs_ref = pytest.mark.skipif(not oracle_py.Reference.available(), reason="reference not compiled here")
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_oracle_matches_live_reference(oracle, name):
+    ref = oracle_py.Reference()
+    X = synth.base(name, 3000)
+    p = oracle_py.params(K=64, L=64, S=10, R=64, iterations=4, search_L=32, nsg_R=24, search_K=64,
+                         tau=0.05 if name == "c1" else 10.0, controls=20)
+    ids = np.arange(0, 3000, 101, dtype=np.uint32)
+    oi, od = oracle.knn(X, ids, 64)
+    ri, rd = ref.linear_search(X, ids, 64)
+    assert np.array_equal(oi, ri)
+    pid, pd, pc, rec, fin = ref.nndescent(X, p, nthreads=2)
+    for kind in (1, 3, 4):
+        a = oracle.prune(kind, X, p, pid, pd, pc, 40)
+        b = ref.prune(kind, X, p, pid, pd, pc, 40)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+@needs_ref
+def test_oracle_nndescent_recall_tracks_reference(oracle):
+    ref = oracle_py.Reference()
+    X = synth.base("c1", 8000)
+    p = oracle_py.params(K=64, L=64, S=10, R=64, iterations=6, search_L=32, nsg_R=24, search_K=64, controls=100)
+    _, _, _, rec, fin = ref.nndescent(X, p, nthreads=4)
+    _, _, _, st = oracle.nndescent(X, p, nthreads=4)
+    assert abs(st.loop_recall[0] - fin) < 0.02, (st.loop_recall[0], fin)
+
+
+def test_bench_reference_arm_prints_one_json_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--cpu-n", "3000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["unit"] == "s" and j["higher_is_better"] is False
+    assert j["cpu_baseline"]["kind"] in ("reference", "port") and j["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def _rank_main(rank, world, port, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    import bench
+
+    ws, r, _ = bench.dist_setup()
+    bench.barrier(ws)
+    q.put((r, bench.max_over_ranks(ws, float(10 + r))))
+
+
+def test_bench_two_rank_gloo_max_over_ranks():
+    import multiprocessing as mp
+    import socket
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(120)
+    got = sorted(q.get(timeout=5) for _ in ps)
+    assert got == [(0, 11.0), (1, 11.0)]
