@@ -301,7 +301,13 @@ def run_gpu(args, ws, rank, local):
                    "nndescent_recall": [round(x, 4) for x in st["iter_recall"]],
                    "phase_ms": {k: round(v, 2) for k, v in st["phase_ms"].items() if v},
                    "dist_evals_per_s": round((st["n_comps"] + st["prune_comps"] + st["bridge_comps"]) / (ms / 1000.0)),
-                   "cand_overflow": sum(st["iter_cand_overflow"])},
+                   "cand_overflow": sum(st["iter_cand_overflow"]), "cand_emitted": st["cand_emitted"],
+                   "cand_merged": st["cand_merged"], "tree_attached": st["tree_attached"],
+                   "avg_degree": st["aod"],
+                   "iter_join_ms": [round(x, 1) for x in st["iter_join_ms"]],
+                   "iter_merge_ms": [round(x, 1) for x in st["iter_merge_ms"]],
+                   "iter_cand_M": [round(x / 1e6, 1) for x in st["iter_cand"]],
+                   "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]]},
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
                 "d2h_bytes_per_step": int(n * W * 4 + n * 4 + 8)},

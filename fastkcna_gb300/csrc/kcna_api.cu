@@ -76,7 +76,7 @@ static void reset_phase_stats(kcna_ctx *c) {
         c->phase_ms[i] = 0;
         c->phase_launches[i] = 0;
     }
-    c->join_rows = c->cand_emitted = c->cand_merged = c->pool_entries_merged = 0;
+    c->join_rows = c->cand_emitted = c->cand_merged = c->pool_entries_merged = c->tree_attached = 0;
 }
 
 static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
@@ -88,6 +88,7 @@ static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
     st->cand_emitted = c->cand_emitted;
     st->cand_merged = c->cand_merged;
     st->pool_entries_merged = c->pool_entries_merged;
+    st->tree_attached = c->tree_attached;
 }
 
 static kcna_status grow(kcna_ctx *c, void **p, size_t *cur, size_t bytes) {
@@ -130,7 +131,7 @@ static void free_state(kcna_ctx *c) {
     void *bufs[] = {c->pool, c->pool_cnt, c->radius, c->M, c->radiusM, c->found, c->fwd_new, c->fwd_new_cnt,
                     c->fwd_old, c->fwd_old_cnt, c->rnew, c->rnew_cnt, c->rold, c->rold_cnt, c->cand, c->cand_cnt,
                     c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
-                    c->d_control_knn};
+                    c->d_control_knn, c->big_list, c->big_cnt};
     for (void *b : bufs)
         if (b) cudaFree(b);
     c->pool = nullptr;
@@ -143,6 +144,7 @@ static void free_state(kcna_ctx *c) {
     c->rnew = c->rnew_cnt = c->rold = c->rold_cnt = nullptr;
     c->cand = nullptr;
     c->cand_cnt = nullptr;
+    c->big_list = c->big_cnt = nullptr;
     c->g_ids = c->g_deg = c->g_old = c->g_old_deg = nullptr;
     c->g_dist = nullptr;
     c->g_isnew = nullptr;

@@ -10,6 +10,7 @@
 #define KCNA_FULL 0xFFFFFFFFu
 #define KCNA_NONE 0xFFFFFFFFu
 #define KCNA_EMPTY_KEY 0xFFFFFFFFFFFFFFFFull
+#define KCNA_EMPTY_KEY_NOFLAGS 0xFFFFFFFFFFFFFFFCull
 
 // ---------------------------------------------------------------------------
 // Pool entries are 64-bit keys ordered by (distance, id):

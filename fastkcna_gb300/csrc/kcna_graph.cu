@@ -41,17 +41,28 @@ __device__ __forceinline__ bool occludes(const PruneRule &r, float td, float djk
     return djk < pd;
 }
 
-// Prune of one candidate list by one warp.  cand ids/dists are read through
-// get(i); the kept list (ids, dists) lives in shared memory.  Candidates are
-// taken 32 at a time: each lane tests its candidate against the kept list, then
-// the batch is resolved in order (the first unoccluded lane is kept and tests
-// the later lanes), which gives exactly the sequential result.
-template <typename GetFn>
-__device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle, const PruneRule &rule,
-                          uint32_t self, int first, int lim, int range, GetFn get, uint32_t *kid, float *kd,
-                          unsigned long long *comps) {
+// Two-phase form of warp_prune with the same result.  Almost every candidate is
+// occluded by one of the first kept neighbours, so each batch of 32 candidates
+// is first tested against kept[0..3] with four independent FMA chains per lane
+// (the candidate row is read once); the few survivors are then tested one at
+// a time against kept[4..nk) with one lane per kept row.  With STAGED the kept
+// rows are copied into shared memory (pitch ld+4 floats, conflict-free float4
+// reads) as they are kept.  The in-batch resolution is the same as warp_prune.
+template <bool STAGED, typename GetFn>
+__device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracle, const PruneRule &rule, int first,
+                           int lim, int range, GetFn get, uint32_t *kid, float *kd, float *kr,
+                           unsigned long long *comps) {
     const int lane = kcna_lane();
+    const int krp = ld + 4;
     if (first >= lim || range <= 0) return 0;
+    auto krow = [&](int t) -> const float * { return STAGED ? kr + (size_t)t * krp : X + (uint64_t)kid[t] * ld; };
+    auto stage = [&](int t, uint32_t id) {
+        if (STAGED) {
+            const float4 *src = reinterpret_cast<const float4 *>(X + (uint64_t)id * ld);
+            float4 *dst = reinterpret_cast<float4 *>(kr + (size_t)t * krp);
+            for (int k = lane; k < (ld >> 2); k += 32) dst[k] = __ldg(src + k);
+        }
+    };
     int nk = 0;
     {
         uint32_t id0;
@@ -61,6 +72,8 @@ __device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle
             kid[0] = id0;
             kd[0] = d0;
         }
+        __syncwarp();
+        stage(0, id0);
         nk = 1;
     }
     __syncwarp();
@@ -76,22 +89,85 @@ __device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle
         }
         const float *prow = X + (uint64_t)(live ? id : 0) * ld;
         bool occ = false;
+        // phase 1: kept[0..min(nk,4)), four independent chains, candidate row read once
+        const int t1 = min(nk, 4);
         if (live) {
-            for (int t = 0; t < nk; ++t) {
-                uint32_t tid = kid[t];
-                if (tid == id) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            const float4 *p4 = reinterpret_cast<const float4 *>(prow);
+            const float4 *k0 = reinterpret_cast<const float4 *>(krow(0));
+            const float4 *k1 = reinterpret_cast<const float4 *>(krow(t1 > 1 ? 1 : 0));
+            const float4 *k2 = reinterpret_cast<const float4 *>(krow(t1 > 2 ? 2 : 0));
+            const float4 *k3 = reinterpret_cast<const float4 *>(krow(t1 > 3 ? 3 : 0));
+            const int nv = ld >> 2;
+            for (int k0i = 0; k0i < nv; k0i += 8) { // eight independent row loads in flight
+                float4 pv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    pv[u] = k0i + u < nv ? __ldg(p4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (k0i + u >= nv) break;
+                    const int k = k0i + u;
+                    a0 = kcna_acc4(a0, k0[k], pv[u]);
+                    if (t1 > 1) a1 = kcna_acc4(a1, k1[k], pv[u]);
+                    if (t1 > 2) a2 = kcna_acc4(a2, k2[k], pv[u]);
+                    if (t1 > 3) a3 = kcna_acc4(a3, k3[k], pv[u]);
+                }
+            }
+            const float ds[4] = {a0, a1, a2, a3};
+            for (int t = 0; t < t1; ++t) {
+                if (kid[t] == id) {
                     occ = true;
                     break;
                 }
                 ++cc;
-                float djk = kcna_l2_ldg(X + (uint64_t)tid * ld, prow, ld);
-                if (occludes(rule, kd[t], djk, pd)) {
+                if (occludes(rule, kd[t], ds[t], pd)) {
                     occ = true;
                     break;
                 }
             }
         }
         unsigned rem = __ballot_sync(KCNA_FULL, live && !occ);
+        // phase 2: survivors against kept[4..nk), one lane per kept row
+        if (nk > 4) {
+            unsigned todo = rem;
+            while (todo) {
+                const int b = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const uint32_t bid = __shfl_sync(KCNA_FULL, id, b);
+                const float bd = __shfl_sync(KCNA_FULL, pd, b);
+                const float *brow = X + (uint64_t)bid * ld;
+                bool hit = false;
+                for (int t0 = 4; t0 < nk && !hit; t0 += 32) {
+                    const int t = t0 + lane;
+                    bool h = false;
+                    if (t < nk) {
+                        if (kid[t] == bid) {
+                            h = true;
+                        } else {
+                            ++cc;
+                            const float4 *kt = reinterpret_cast<const float4 *>(krow(t)); // shared or global
+                            const float4 *b4 = reinterpret_cast<const float4 *>(brow);
+                            const int nv = ld >> 2;
+                            float acc = 0.f;
+                            for (int k0i = 0; k0i < nv; k0i += 8) {
+                                float4 bv[8];
+#pragma unroll
+                                for (int u = 0; u < 8; ++u)
+                                    bv[u] = k0i + u < nv ? __ldg(b4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                                for (int u = 0; u < 8; ++u)
+                                    if (k0i + u < nv) acc = kcna_acc4(acc, kt[k0i + u], bv[u]);
+                            }
+                            h = occludes(rule, kd[t], acc, bd);
+                        }
+                    }
+                    hit = __ballot_sync(KCNA_FULL, h) != 0;
+                }
+                if (hit) rem &= ~(1u << b);
+            }
+        }
+        // in-batch resolution, in candidate order
         while (rem && nk < range) {
             const int a = __ffs(rem) - 1;
             const uint32_t aid = __shfl_sync(KCNA_FULL, id, a);
@@ -100,6 +176,8 @@ __device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle
                 kid[nk] = aid;
                 kd[nk] = ad;
             }
+            __syncwarp();
+            stage(nk, aid);
             ++nk;
             __syncwarp();
             rem &= ~((2u << a) - 1u); // lanes after a
@@ -110,7 +188,21 @@ __device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle
                     o2 = true;
                 } else {
                     ++cc;
-                    float djk = kcna_l2_ldg(X + (uint64_t)aid * ld, prow, ld);
+                    // kept row a (staged copy when STAGED) against this lane's row, loads batched
+                    const float4 *ka = reinterpret_cast<const float4 *>(STAGED ? kr + (size_t)(nk - 1) * krp
+                                                                               : X + (uint64_t)aid * ld);
+                    const float4 *p4 = reinterpret_cast<const float4 *>(prow);
+                    const int nv = ld >> 2;
+                    float djk = 0.f;
+                    for (int k0i = 0; k0i < nv; k0i += 8) {
+                        float4 pv[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            pv[u] = k0i + u < nv ? __ldg(p4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            if (k0i + u < nv) djk = kcna_acc4(djk, ka[k0i + u], pv[u]);
+                    }
                     o2 = occludes(rule, ad, djk, pd);
                 }
             }
@@ -123,19 +215,20 @@ __device__ int warp_prune(const float *__restrict__ X, int ld, uint32_t n_oracle
     return nk;
 }
 
-constexpr int PW = 4; // warps per prune block
-
-__global__ void __launch_bounds__(PW * 32) prune_kernel(const float *__restrict__ X, int ld, uint32_t N,
-                                                        const uint64_t *__restrict__ pool,
-                                                        const uint32_t *__restrict__ pool_cnt, uint32_t cap,
-                                                        PruneRule rule, int range, int maxc, uint32_t *__restrict__ g_ids,
-                                                        float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
-                                                        uint32_t W, unsigned long long *comps) {
+// Staged prune: one warp per node, kept rows in shared memory.
+template <bool STAGED>
+__global__ void prune2_kernel(const float *__restrict__ X, int ld, uint32_t N, const uint64_t *__restrict__ pool,
+                              const uint32_t *__restrict__ pool_cnt, uint32_t cap, PruneRule rule, int range, int maxc,
+                              uint32_t *__restrict__ g_ids, float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
+                              uint32_t W, unsigned long long *comps) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
-    uint32_t *kid = reinterpret_cast<uint32_t *>(smem) + w * 2 * range;
+    const size_t per_warp = (size_t)range * 2 * 4 + (STAGED ? (size_t)range * (ld + 4) * 4 : 0);
+    unsigned char *mine = smem + w * ((per_warp + 15) & ~(size_t)15);
+    float *kr = reinterpret_cast<float *>(mine);
+    uint32_t *kid = reinterpret_cast<uint32_t *>(mine + (STAGED ? (size_t)range * (ld + 4) * 4 : 0));
     float *kd = reinterpret_cast<float *>(kid + range);
-    const uint32_t q = blockIdx.x * PW + w;
+    const uint32_t q = blockIdx.x * (blockDim.x >> 5) + w;
     if (q >= N) return;
     const uint64_t *pr = pool + (uint64_t)q * cap;
     const int cnt = (int)pool_cnt[q];
@@ -147,7 +240,9 @@ __global__ void __launch_bounds__(PW * 32) prune_kernel(const float *__restrict_
         id = kcna_key_id(k);
         dd = kcna_key_dist(k);
     };
-    int nk = (first < cnt) ? warp_prune(X, ld, N, rule, q, first, max(lim, first + 1), range, get, kid, kd, comps) : 0;
+    int nk = (first < cnt) ? warp_prune2<STAGED>(X, ld, N, rule, first, max(lim, first + 1), range, get, kid, kd, kr,
+                                                 comps)
+                           : 0;
     for (int j = lane; j < (int)W; j += 32) {
         g_ids[(uint64_t)q * W + j] = j < nk ? kid[j] : KCNA_NONE;
         g_dist[(uint64_t)q * W + j] = j < nk ? kd[j] : 0.f;
@@ -337,7 +432,7 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(const float *__restrict_
             get(0, id0, d0);
             if (id0 == q) first = 1;
         }
-        int nk = warp_prune(X, ld, 0xFFFFFFFFu, rule, q, first, total, range, get, s_kid, s_kd, comps);
+        int nk = warp_prune2<false>(X, ld, 0xFFFFFFFFu, rule, first, total, range, get, s_kid, s_kd, nullptr, comps);
         for (int j = lane; j < (int)W; j += 32) {
             g_ids[(uint64_t)q * W + j] = j < nk ? s_kid[j] : KCNA_NONE;
             g_dist[(uint64_t)q * W + j] = j < nk ? s_kd[j] : 0.f;
@@ -520,124 +615,109 @@ __global__ void bfs_expand_kernel(const uint32_t *__restrict__ g_ids, const uint
     }
 }
 
-// Attach loop in one block: smallest unreached id u; first reached node r in
-// u's pool with degree < nsg_R (else a random reached node with degree <
-// nsg_R * factor); edge r -> u; block-level BFS from u.  Every round visits
-// at least u, so the loop ends after at most N rounds.
-constexpr int AT = 1024;
-__global__ void __launch_bounds__(AT) attach_kernel(const float *__restrict__ X, int ld, uint32_t N,
-                                                    const uint64_t *__restrict__ pool,
-                                                    const uint32_t *__restrict__ pool_cnt, uint32_t cap,
-                                                    uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
-                                                    uint32_t *__restrict__ g_deg, uint32_t W, uint32_t nsg_R,
-                                                    uint32_t *__restrict__ visited, uint32_t *__restrict__ qa,
-                                                    uint32_t *__restrict__ qb, uint64_t seed, int *err,
-                                                    unsigned long long *attached) {
-    __shared__ uint32_t s_u, s_root, s_na, s_nb;
-    __shared__ int s_found;
-    const uint32_t words = (N + 31) / 32;
-    uint32_t start_word = 0;
-    for (uint32_t round = 0; round < N; ++round) {
-        // smallest unreached id
-        if (threadIdx.x == 0) s_u = KCNA_NONE;
-        __syncthreads();
-        for (uint32_t wbase = start_word; wbase < words; wbase += AT) {
-            uint32_t wd = wbase + threadIdx.x;
-            if (wd < words) {
-                uint32_t v = visited[wd];
-                uint32_t valid = (wd == words - 1 && (N & 31)) ? ((1u << (N & 31)) - 1u) : 0xFFFFFFFFu;
-                uint32_t miss = ~v & valid;
-                if (miss) atomicMin(&s_u, wd * 32 + (__ffs(miss) - 1));
-            }
-            __syncthreads();
-            if (s_u != KCNA_NONE) break;
-            __syncthreads();
-        }
-        const uint32_t u = s_u;
-        if (u == KCNA_NONE) return;
-        start_word = u >> 5;
-        // attach point: first reached pool entry of u with degree < nsg_R
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
-            const uint32_t cnt = pool_cnt[u];
-            uint32_t root = KCNA_NONE;
-            for (uint32_t b0 = 0; b0 < cnt && root == KCNA_NONE; b0 += 32) {
-                uint32_t i = b0 + lane;
-                bool ok = false;
-                uint32_t cid = 0;
-                if (i < cnt) {
-                    cid = kcna_key_id(pool[(uint64_t)u * cap + i]);
-                    ok = cid < N && ((visited[cid >> 5] >> (cid & 31)) & 1u) && g_deg[cid] < nsg_R;
-                }
-                unsigned mk = __ballot_sync(KCNA_FULL, ok);
-                if (mk) root = __shfl_sync(KCNA_FULL, cid, __ffs(mk) - 1);
-            }
-            if (lane == 0) {
-                if (root == KCNA_NONE) { // random reached node, src/kgraph.cpp:2216-2230
-                    for (uint64_t t = 1; t <= 64ull * N + 64; ++t) {
-                        uint32_t factor = (uint32_t)(t / N) + 1;
-                        uint32_t rid = kcna_rand32(seed, u, t) % N;
-                        if (((visited[rid >> 5] >> (rid & 31)) & 1u) && g_deg[rid] < nsg_R * factor) {
-                            root = rid;
-                            break;
-                        }
-                    }
-                }
-                s_found = root != KCNA_NONE;
-                s_root = root;
-                if (root != KCNA_NONE) {
-                    uint32_t dg = g_deg[root];
-                    if (dg < W) {
-                        g_ids[(uint64_t)root * W + dg] = u;
-                        g_dist[(uint64_t)root * W + dg] = kcna_l2(X + (uint64_t)root * ld, X + (uint64_t)u * ld, ld);
-                        g_deg[root] = dg + 1;
-                    } else {
-                        kcna_set_err(err, KCNA_DERR_DEGREE);
-                    }
-                    atomicAdd(attached, 1ull);
-                } else {
-                    kcna_set_err(err, KCNA_DERR_SPIN);
-                }
-                visited[u >> 5] |= 1u << (u & 31);
-                qa[0] = u;
-                s_na = 1;
-            }
-        }
-        __syncthreads();
-        if (!s_found) return;
-        // block BFS from u
-        uint32_t *cur = qa, *nxt = qb;
-        while (s_na > 0) {
-            if (threadIdx.x == 0) s_nb = 0;
-            __syncthreads();
-            const uint32_t na = s_na;
-            for (uint32_t t = threadIdx.x; t < na * 64u; t += AT) {
-                uint32_t f = t / 64u, j = t % 64u;
-                uint32_t x = cur[f];
-                if (j >= min(g_deg[x], W)) continue;
-                uint32_t v = g_ids[(uint64_t)x * W + j];
-                if (v >= N) continue;
-                uint32_t old = atomicOr(visited + (v >> 5), 1u << (v & 31));
-                if (!(old & (1u << (v & 31)))) nxt[atomicAdd(&s_nb, 1u)] = v;
-            }
-            // degrees above 64: second pass
-            for (uint32_t t = threadIdx.x; t < na; t += AT) {
-                uint32_t x = cur[t];
-                for (uint32_t j = 64; j < min(g_deg[x], W); ++j) {
-                    uint32_t v = g_ids[(uint64_t)x * W + j];
-                    if (v >= N) continue;
-                    uint32_t old = atomicOr(visited + (v >> 5), 1u << (v & 31));
-                    if (!(old & (1u << (v & 31)))) nxt[atomicAdd(&s_nb, 1u)] = v;
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) s_na = s_nb;
-            uint32_t *tmp = cur;
-            cur = nxt;
-            nxt = tmp;
-            __syncthreads();
+// Parallel attach rounds for tree_grow (src/kgraph.cpp:2145-2236).  The
+// reference walks unreached ids in order, attaching each not-yet-reached one
+// to a reached node and running a DFS from it, so it adds one edge per
+// unreached component source.  Here every round attaches all sources at once:
+// an unreached node is a source when no unreached node has an edge to it
+// (mark_targets_kernel); when every unreached node has such an edge (the rest
+// are cycles) the nodes whose id is below all their unreached out-neighbours
+// are used.  The attach point is the reference's rule: the first pool entry
+// of u that is reached and has degree < nsg_R, else a random reached node with
+// degree < nsg_R * factor; slots are reserved with atomicAdd on the degree.
+__global__ void mark_targets_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg,
+                                    uint32_t W, uint32_t N, const uint32_t *__restrict__ visited,
+                                    uint32_t *__restrict__ targeted, uint32_t *__restrict__ localmin,
+                                    unsigned long long *n_unreached) {
+    const uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (u >= N || ((visited[u >> 5] >> (u & 31)) & 1u)) return;
+    const int deg = (int)min(g_deg[u], W);
+    bool below_all = true;
+    for (int j = lane; j < deg; j += 32) {
+        const uint32_t v = g_ids[(uint64_t)u * W + j];
+        if (v < N && !((visited[v >> 5] >> (v & 31)) & 1u)) {
+            atomicOr(targeted + (v >> 5), 1u << (v & 31));
+            if (v < u) below_all = false;
         }
     }
+    below_all = __all_sync(KCNA_FULL, below_all);
+    if (lane == 0) {
+        if (below_all) atomicOr(localmin + (u >> 5), 1u << (u & 31));
+        atomicAdd(n_unreached, 1ull);
+    }
+}
+
+__device__ __forceinline__ bool reserve_slot(uint32_t *g_deg, uint32_t r, uint32_t limit, uint32_t W, uint32_t *slot) {
+    const uint32_t old = atomicAdd(g_deg + r, 1u);
+    if (old < limit && old < W) {
+        *slot = old;
+        return true;
+    }
+    atomicSub(g_deg + r, 1u);
+    return false;
+}
+
+__global__ void attach_sources_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                      const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
+                                      uint32_t cap, uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
+                                      uint32_t *__restrict__ g_deg, uint32_t W, uint32_t nsg_R,
+                                      const uint32_t *__restrict__ visited, const uint32_t *__restrict__ pick,
+                                      uint32_t *__restrict__ frontier, uint32_t *__restrict__ nfront, uint64_t seed,
+                                      int *err, unsigned long long *attached) {
+    const uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = kcna_lane();
+    if (u >= N || ((visited[u >> 5] >> (u & 31)) & 1u) || !((pick[u >> 5] >> (u & 31)) & 1u)) return;
+    uint32_t root = KCNA_NONE, slot = 0;
+    const uint32_t cnt = min(pool_cnt[u], cap);
+    for (uint32_t b0 = 0; b0 < cnt && root == KCNA_NONE; b0 += 32) {
+        const uint32_t i = b0 + lane;
+        uint32_t cid = KCNA_NONE;
+        if (i < cnt) {
+            cid = kcna_key_id(pool[(uint64_t)u * cap + i]);
+            if (!(cid < N && ((visited[cid >> 5] >> (cid & 31)) & 1u) && g_deg[cid] < nsg_R)) cid = KCNA_NONE;
+        }
+        unsigned mk = __ballot_sync(KCNA_FULL, cid != KCNA_NONE);
+        while (mk && root == KCNA_NONE) { // candidates in pool order; a full slot moves on to the next one
+            const int src = __ffs(mk) - 1;
+            mk &= mk - 1;
+            const uint32_t r = __shfl_sync(KCNA_FULL, cid, src);
+            uint32_t got = 0, sl = 0;
+            if (lane == 0) got = reserve_slot(g_deg, r, nsg_R, W, &sl) ? 1u : 0u;
+            got = __shfl_sync(KCNA_FULL, got, 0);
+            if (got) {
+                root = r;
+                slot = __shfl_sync(KCNA_FULL, sl, 0);
+            }
+        }
+    }
+    if (root == KCNA_NONE && lane == 0) { // random reached node, src/kgraph.cpp:2216-2230
+        for (uint64_t t = 1; t <= 64ull * N + 64; ++t) {
+            const uint32_t factor = (uint32_t)(t / N) + 1;
+            const uint32_t rid = kcna_rand32(seed, u, t) % N;
+            if (((visited[rid >> 5] >> (rid & 31)) & 1u) && g_deg[rid] < nsg_R * factor &&
+                reserve_slot(g_deg, rid, nsg_R * factor, W, &slot)) {
+                root = rid;
+                break;
+            }
+        }
+        if (root == KCNA_NONE) kcna_set_err(err, KCNA_DERR_SPIN);
+    }
+    if (lane == 0 && root != KCNA_NONE) {
+        g_ids[(uint64_t)root * W + slot] = u;
+        g_dist[(uint64_t)root * W + slot] = kcna_l2(X + (uint64_t)root * ld, X + (uint64_t)u * ld, ld);
+        frontier[atomicAdd(nfront, 1u)] = u;
+        atomicAdd(attached, 1ull);
+    }
+}
+
+__global__ void invert_kernel(uint32_t *__restrict__ w, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = ~w[i];
+}
+__global__ void mark_frontier_kernel(const uint32_t *__restrict__ f, uint32_t nf, uint32_t *__restrict__ visited) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nf) atomicOr(visited + (f[i] >> 5), 1u << (f[i] & 31));
 }
 
 __global__ void degree_stats_kernel(const uint32_t *__restrict__ g_deg, uint32_t N, unsigned long long *out) {
@@ -757,57 +837,77 @@ __global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint6
     if (off[tgt] + p < off[tgt + 1]) rnn[off[tgt] + p] = (uint32_t)v;
 }
 
-// P2K join: for q, each pusher u (with its isnew bit) against q's PG
-// neighbours w: d(u, w) -> candidate (w) for pool u.  Warp per (q, u).
-__global__ void bridge_join_kernel(const float *__restrict__ X, int ld, uint32_t N, const uint64_t *__restrict__ off,
-                                   const uint32_t *__restrict__ rnn, const uint32_t *__restrict__ g_ids,
-                                   const uint32_t *__restrict__ g_deg, const uint8_t *__restrict__ g_isnew,
-                                   uint32_t W, const float *__restrict__ radius, uint64_t *__restrict__ cand,
-                                   uint32_t *__restrict__ cand_cnt, uint32_t CB, unsigned long long *comps) {
-    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = kcna_lane();
-    if (q >= N) return;
-    const uint64_t r0 = off[q], r1 = off[q + 1];
-    if (r0 == r1) return;
-    const int deg = (int)min(g_deg[q], W);
-    uint32_t wid[2] = {KCNA_NONE, KCNA_NONE};
-    bool wnew[2] = {false, false};
-    for (int h = 0; h < 2; ++h) {
-        int j = lane + 32 * h;
-        if (j < deg) {
-            wid[h] = g_ids[(uint64_t)q * W + j];
-            wnew[h] = g_isnew[(uint64_t)q * W + j] != 0;
+// P2K join, tiled: one block per node q.  Rows = pushers u of q (rnn(q), up to
+// 128 per tile), columns = q's graph neighbours w (up to 64), staged through
+// shared memory in 32-float chunks; each thread keeps RI x 8 canonical FMA
+// accumulators.  Pair (u, w) is skipped when u == w or both are old
+// (src/kgraph.cpp:2639-2641); survivors within u's radius become candidates of
+// u, written as one run per (q, u) after one atomicAdd.
+constexpr int PJT = 256, PJC = 64, PJK = 32, PJP = PJK + 4, PJR = 128;
+
+template <int RI>
+__device__ void p2k_tile(const float *__restrict__ X, int ld, uint32_t N, const uint32_t *s_u, const uint8_t *s_unew,
+                         int nu, const uint32_t *s_w, const uint8_t *s_wnew, int nw, const float *__restrict__ radius,
+                         uint64_t *__restrict__ cand, uint32_t *__restrict__ cand_cnt, uint32_t CB, float *s_As,
+                         float *s_Bs, float *s_D, unsigned long long *s_cc) {
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
+    float acc[RI][8];
+#pragma unroll
+    for (int i = 0; i < RI; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int k0 = 0; k0 < ld; k0 += PJK) {
+        for (int idx = tid; idx < 32 * RI * (PJK / 4); idx += PJT) {
+            int r = idx >> 3, c = (idx & 7) * 4;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < nu && k0 + c < ld) v = __ldg(reinterpret_cast<const float4 *>(X + (uint64_t)s_u[r] * ld + k0 + c));
+            *reinterpret_cast<float4 *>(s_As + r * PJP + c) = v;
         }
+        for (int idx = tid; idx < PJC * (PJK / 4); idx += PJT) {
+            int r = idx >> 3, c = (idx & 7) * 4;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < nw && k0 + c < ld) v = __ldg(reinterpret_cast<const float4 *>(X + (uint64_t)s_w[r] * ld + k0 + c));
+            *reinterpret_cast<float4 *>(s_Bs + r * PJP + c) = v;
+        }
+        __syncthreads();
+        const int kend = min(PJK, ld - k0);
+        for (int k = 0; k < kend; k += 4) {
+            float4 ra[RI], cb[8];
+#pragma unroll
+            for (int i = 0; i < RI; ++i) ra[i] = *reinterpret_cast<const float4 *>(s_As + (ty + 32 * i) * PJP + k);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) cb[j] = *reinterpret_cast<const float4 *>(s_Bs + (tx + 8 * j) * PJP + k);
+#pragma unroll
+            for (int i = 0; i < RI; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = kcna_acc4(acc[i][j], ra[i], cb[j]);
+        }
+        __syncthreads();
     }
+#pragma unroll
+    for (int i = 0; i < RI; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s_D[(ty + 32 * i) * (PJC + 1) + tx + 8 * j] = acc[i][j];
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
     unsigned long long cc = 0;
-    for (uint64_t r = r0; r < r1; ++r) {
-        uint32_t v = rnn[r];
-        uint32_t u = v & 0x7FFFFFFFu;
-        bool ifnew = (v & 0x80000000u) != 0;
-        if (u >= N) continue;
-        const float rad = radius[u];
-        const float *urow = X + (uint64_t)u * ld;
+    for (int i = warp; i < nu; i += PJT / 32) {
+        const uint32_t u = s_u[i];
+        const bool unew = s_unew[i] != 0;
+        const float rad = __ldg(radius + u);
+        bool ok[2];
         uint64_t keys[2];
-        bool ok[2] = {false, false};
+#pragma unroll
         for (int h = 0; h < 2; ++h) {
-            uint32_t w = wid[h];
-            if (w >= N || w == u || (!ifnew && !wnew[h])) continue;
-            ++cc;
-            float dd = kcna_l2_ldg(urow, X + (uint64_t)w * ld, ld);
-            if (dd <= rad) {
-                ok[h] = true;
-                keys[h] = kcna_key(dd, w, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
-            }
-        }
-        for (int j = 64 + lane; j < deg; j += 32) { // rows wider than 64: direct emission
-            uint32_t w = g_ids[(uint64_t)q * W + j];
-            bool wn = g_isnew[(uint64_t)q * W + j] != 0;
-            if (w >= N || w == u || (!ifnew && !wn)) continue;
-            ++cc;
-            float dd = kcna_l2_ldg(urow, X + (uint64_t)w * ld, ld);
-            if (dd <= rad) {
-                uint32_t p = atomicAdd(cand_cnt + u, 1u);
-                if (p < CB) cand[(uint64_t)u * CB + p] = kcna_key(dd, w, 3u);
+            const int j = lane + 32 * h;
+            ok[h] = false;
+            if (j < nw && s_w[j] != u && (unew || s_wnew[j])) {
+                ++cc;
+                float dd = s_D[i * (PJC + 1) + j];
+                if (dd <= rad) {
+                    ok[h] = true;
+                    keys[h] = kcna_key(dd, s_w[j], (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+                }
             }
         }
         unsigned m0 = __ballot_sync(KCNA_FULL, ok[0]), m1 = __ballot_sync(KCNA_FULL, ok[1]);
@@ -827,7 +927,69 @@ __global__ void bridge_join_kernel(const float *__restrict__ X, int ld, uint32_t
         }
     }
     cc = kcna_warp_sum(cc);
-    if (lane == 0 && cc) atomicAdd(comps, cc);
+    if (lane == 0 && cc) atomicAdd(s_cc, cc);
+    __syncthreads();
+}
+
+template <int RMAX>
+constexpr size_t p2k_smem_bytes() {
+    return (size_t)(RMAX * PJP + PJC * PJP + RMAX * (PJC + 1)) * sizeof(float);
+}
+
+// RMAX = 32: nodes with at most 32 pushers (almost all), 22 KB of shared memory
+// so eight blocks fit per SM; RMAX = 128: the other nodes, in row tiles of 128.
+template <int RMAX>
+__global__ void __launch_bounds__(PJT) p2k_join_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                       const uint64_t *__restrict__ off,
+                                                       const uint32_t *__restrict__ rnn,
+                                                       const uint32_t *__restrict__ g_ids,
+                                                       const uint32_t *__restrict__ g_deg,
+                                                       const uint8_t *__restrict__ g_isnew, uint32_t W,
+                                                       const float *__restrict__ radius, uint64_t *__restrict__ cand,
+                                                       uint32_t *__restrict__ cand_cnt, uint32_t CB,
+                                                       unsigned long long *comps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *s_As = reinterpret_cast<float *>(smem); // RMAX x PJP
+    float *s_Bs = s_As + RMAX * PJP;               // PJC x PJP
+    float *s_D = s_Bs + PJC * PJP;                 // RMAX x (PJC+1)
+    __shared__ uint32_t s_u[RMAX], s_w[PJC];
+    __shared__ uint8_t s_unew[RMAX], s_wnew[PJC];
+    __shared__ unsigned long long s_cc;
+    const uint32_t q = blockIdx.x;
+    const uint64_t r0 = off[q], r1 = off[q + 1];
+    const int deg = (int)min(g_deg[q], W);
+    if (r0 == r1 || deg == 0) return;
+    if ((RMAX == 32) != (r1 - r0 <= 32)) return; // each node is handled by one of the two instances
+    if (threadIdx.x == 0) s_cc = 0;
+    for (int c0 = 0; c0 < deg; c0 += PJC) { // graph rows wider than 64: column chunks
+        const int nw = min(PJC, deg - c0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < nw; j += PJT) {
+            s_w[j] = g_ids[(uint64_t)q * W + c0 + j];
+            s_wnew[j] = g_isnew[(uint64_t)q * W + c0 + j];
+        }
+        for (uint64_t t0 = r0; t0 < r1; t0 += RMAX) {
+            const int nu = (int)min((uint64_t)RMAX, r1 - t0);
+            __syncthreads();
+            for (int i = threadIdx.x; i < nu; i += PJT) {
+                uint32_t v = rnn[t0 + i];
+                uint32_t u = v & 0x7FFFFFFFu;
+                s_u[i] = u < N ? u : 0;
+                s_unew[i] = (v & 0x80000000u) ? 1 : 0;
+            }
+            __syncthreads();
+            if (RMAX == 32 || nu <= 32)
+                p2k_tile<1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB, s_As, s_Bs, s_D,
+                            &s_cc);
+            else if (nu <= 64)
+                p2k_tile<RMAX >= 64 ? 2 : 1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
+                                             s_As, s_Bs, s_D, &s_cc);
+            else
+                p2k_tile<RMAX >= 128 ? 4 : 1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
+                                              s_As, s_Bs, s_D, &s_cc);
+        }
+    }
+    if (threadIdx.x == 0 && s_cc) atomicAdd(comps, s_cc);
 }
 
 PruneRule make_rule(const kcna_params *p, int kind) {
@@ -881,11 +1043,28 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     KCNA_TRY(kcna_graph_alloc(c, std::max<uint32_t>(c->W, range + 8)));
     PruneRule rule = make_rule(p, kind);
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 16, 0, 8, c->stream), "memset"));
-    size_t sm = (size_t)PW * 2 * range * 4;
+    // kept rows in shared memory when a warp's share fits (ld <= ~256 at nsg_R 50)
+    const size_t ids_bytes = (size_t)range * 2 * 4;
+    const size_t rows_bytes = (size_t)range * (c->ld + 4) * 4;
+    const bool staged = false; // two-phase prune with kept rows read from L2: occupancy wins over staging
+    const size_t per_warp = ((staged ? ids_bytes + rows_bytes : ids_bytes) + 15) & ~(size_t)15;
+    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
+    const size_t sm = per_warp * wpb;
+    const int maxc = (int)std::min(p->search_K, c->cap);
     KCNA_TRY(kcna_phase_begin(c));
-    prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
-        c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, (int)std::min(p->search_K, c->cap),
-        c->g_ids, c->g_dist, c->g_deg, c->W, c->counters + 16);
+    if (staged) {
+        KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune2_kernel<true>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)std::max<size_t>(sm, 48 * 1024)),
+                                 "prune smem attr"));
+        prune2_kernel<true><<<kcna_div_up(c->n, wpb), wpb * 32, sm, c->stream>>>(
+            c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids, c->g_dist,
+            c->g_deg, c->W, c->counters + 16);
+    } else {
+        prune2_kernel<false><<<kcna_div_up(c->n, wpb), wpb * 32, sm, c->stream>>>(
+            c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids, c->g_dist,
+            c->g_deg, c->W, c->counters + 16);
+    }
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_PRUNE));
@@ -1048,12 +1227,65 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
         if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs")) != KCNA_OK) return cleanup(), s;
         std::swap(qa, qb);
     }
-    cudaMemsetAsync(c->counters + 18, 0, 8, c->stream);
-    attach_kernel<<<1, AT, 0, c->stream>>>(c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist,
-                                           c->g_deg, c->W, p->nsg_R, vis, qa, qb, seed, c->d_err, c->counters + 18);
-    KCNA_LAUNCHED(c);
+    cudaMemsetAsync(c->counters + 18, 0, 16, c->stream);
+    uint32_t *targeted = nullptr, *localmin = nullptr;
+    auto cleanup2 = [&]() {
+        cudaFree(targeted);
+        cudaFree(localmin);
+    };
+    if ((s = kcna_alloc(c, &targeted, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
+    if ((s = kcna_alloc(c, &localmin, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
+    const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    for (uint32_t round = 0; round < N; ++round) {
+        cudaMemsetAsync(targeted, 0, (size_t)words * 4, c->stream);
+        cudaMemsetAsync(localmin, 0, (size_t)words * 4, c->stream);
+        cudaMemsetAsync(c->counters + 19, 0, 8, c->stream);
+        mark_targets_kernel<<<wblocks, 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W, N, vis, targeted, localmin,
+                                                             c->counters + 19);
+        KCNA_LAUNCHED(c);
+        unsigned long long unreached = 0;
+        cudaMemcpyAsync(&unreached, c->counters + 19, 8, cudaMemcpyDeviceToHost, c->stream);
+        if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "tree marks")) != KCNA_OK)
+            return cleanup2(), cleanup(), s;
+        if (unreached == 0) break;
+        // sources: unreached and not targeted (pick = ~targeted); none left -> local minima
+        invert_kernel<<<kcna_div_up(words, 256), 256, 0, c->stream>>>(targeted, words);
+        KCNA_LAUNCHED(c);
+        for (int pass = 0; pass < 2; ++pass) {
+            cudaMemsetAsync(cntd, 0, 4, c->stream);
+            attach_sources_kernel<<<wblocks, 256, 0, c->stream>>>(
+                c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist, c->g_deg, c->W, p->nsg_R, vis,
+                pass == 0 ? targeted : localmin, qa, cntd, seed + round * 2 + pass, c->d_err, c->counters + 18);
+            KCNA_LAUNCHED(c);
+            cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach")) != KCNA_OK)
+                return cleanup2(), cleanup(), s;
+            if (nf > 0) break;
+        }
+        if (nf == 0) {
+            s = kcna_fail(c, KCNA_E_CUDA, "tree_grow: no attach point for an unreached node");
+            return cleanup2(), cleanup(), s;
+        }
+        // mark the attached sources and BFS from them
+        mark_frontier_kernel<<<kcna_div_up(nf, 256), 256, 0, c->stream>>>(qa, nf, vis);
+        KCNA_LAUNCHED(c);
+        for (uint32_t level = 0; nf > 0 && level < N; ++level) {
+            cudaMemsetAsync(cntd, 0, 4, c->stream);
+            bfs_expand_kernel<<<kcna_div_up((uint64_t)nf * 32, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W,
+                                                                                          N, qa, nf, vis, qb, cntd);
+            KCNA_LAUNCHED(c);
+            cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs")) != KCNA_OK)
+                return cleanup2(), cleanup(), s;
+            std::swap(qa, qb);
+        }
+    }
+    cleanup2();
     s = kcna_cuda_check(c, cudaGetLastError(), "attach");
     if (s == KCNA_OK) s = kcna_phase_end(c, KCNA_PHASE_TREE);
+    unsigned long long att = 0;
+    if (s == KCNA_OK) s = kcna_cuda_check(c, cudaMemcpy(&att, c->counters + 18, 8, cudaMemcpyDeviceToHost), "d2h");
+    c->tree_attached += att;
     cleanup();
     return s == KCNA_OK ? kcna_check_device_err(c, "tree_grow") : s;
 }
@@ -1093,6 +1325,10 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     if ((s = kcna_alloc(c, &off, (uint64_t)N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
     uint64_t total_comps = 0;
     const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    if ((s = kcna_cuda_check(c, cudaFuncSetAttribute(p2k_join_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)p2k_smem_bytes<128>()),
+                             "p2k smem attr")) != KCNA_OK)
+        return cleanup(), s;
     // the reference loops until a thin round; 100 rounds bound it here
     for (int round = 0; round < 100; ++round) {
         // capped round: count, then the uncapped remainder when the round is thin
@@ -1140,9 +1376,13 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             pushes, np_all, off, cursor, rnn, N);
         KCNA_LAUNCHED(c);
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
-        bridge_join_kernel<<<wblocks, 256, 0, c->stream>>>(c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg,
-                                                           c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt, c->CB,
-                                                           c->counters + 21);
+        p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
+            c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+            c->CB, c->counters + 21);
+        p2k_join_kernel<128><<<N, PJT, p2k_smem_bytes<128>(), c->stream>>>(
+            c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+            c->CB, c->counters + 21);
+        c->launches++;
         KCNA_LAUNCHED(c);
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, c->counters + 21, 8, cudaMemcpyDeviceToHost, c->stream);

@@ -41,6 +41,7 @@ struct kcna_ctx {
     uint32_t *rold = nullptr, *rold_cnt = nullptr;
     uint64_t *cand = nullptr;
     uint32_t *cand_cnt = nullptr;
+    uint32_t *big_list = nullptr, *big_cnt = nullptr; // merge queue of nodes with many candidates
     unsigned long long *counters = nullptr; // device scratch counters (64 slots)
 
     // graph: n x W ids / dists / isnew flags, degrees; previous-loop ids
@@ -70,7 +71,7 @@ struct kcna_ctx {
     double phase_ms[KCNA_NUM_PHASES] = {};
     uint64_t phase_launches[KCNA_NUM_PHASES] = {};
     uint64_t launches_at_begin = 0;
-    uint64_t join_rows = 0, cand_emitted = 0, cand_merged = 0, pool_entries_merged = 0;
+    uint64_t join_rows = 0, cand_emitted = 0, cand_merged = 0, pool_entries_merged = 0, tree_attached = 0;
 };
 
 // Brackets one phase with events on the context stream; end() waits for the
@@ -119,7 +120,8 @@ kcna_status kcna_gather_rows(kcna_ctx *c, const uint32_t *d_ids, uint32_t m, flo
 kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);
-kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk);
+kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
+                       uint64_t *merged = nullptr, uint64_t *inserted = nullptr);
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);
 kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall);

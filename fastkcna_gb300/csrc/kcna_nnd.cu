@@ -300,7 +300,7 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
     }
 }
 
-__global__ void __launch_bounds__(JT) join_kernel(JoinArgs a) {
+__global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float *s_As = reinterpret_cast<float *>(smem);                // 128 x JKP
     float *s_Bs = s_As + 128 * JKP;                               // JCOLS x JKP
@@ -366,116 +366,281 @@ struct MergeArgs {
     unsigned long long *counters; // [1] flagged in top-K, [2] overflow, [3] inserted
 };
 
-__global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a) {
+// Warp-per-node merge for nodes with at most MW_SMALL candidates (most nodes
+// in late NN-descent iterations and in every P2K round).  Nodes with more
+// candidates are queued for merge_big_kernel.  Same result as the block merge.
+constexpr int MW_WARPS = 8, MW_SMALL = 256;
+
+__global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, uint32_t N, uint32_t *big_list,
+                                                                  uint32_t *big_cnt) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t node = blockIdx.x;
-    uint64_t *s_pool = reinterpret_cast<uint64_t *>(smem);        // cap
-    uint64_t *s_c = s_pool + a.cap;                               // pow2(CB)
-    uint32_t *s_scan = reinterpret_cast<uint32_t *>(s_c + kcna_pow2_ceil_d((int)a.CB)); // pow2(CB)+1
-    __shared__ uint32_t s_warp[MT / 32];
-    __shared__ unsigned long long s_flagged;
-    const uint32_t raw = a.cand_cnt[node];
-    const uint32_t nc = min(raw, a.CB);
-    const uint32_t np = min(a.pool_cnt[node], a.limit);
-    uint64_t *gp = a.pool + (uint64_t)node * a.cap;
-    if (threadIdx.x == 0) s_flagged = 0;
-    if (nc == 0) {
-        // no candidates: only the statistic (flags among the first K)
-        unsigned long long f = 0;
-        for (uint32_t i = threadIdx.x; i < min(np, a.K); i += MT) f += (gp[i] & KCNA_FLAG_NEW) ? 1 : 0;
-        f = kcna_warp_sum(f);
-        if ((threadIdx.x & 31) == 0 && f) atomicAdd(a.counters + 1, f);
-        return;
-    }
-    for (uint32_t i = threadIdx.x; i < np; i += MT) s_pool[i] = gp[i];
-    const int cp = kcna_pow2_ceil_d((int)nc);
-    const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
-    for (int i = threadIdx.x; i < cp; i += MT) s_c[i] = i < (int)nc ? kcna_key_noflags(gc[i]) : KCNA_EMPTY_KEY;
-    kcna_cta_bitonic(s_c, cp);
-    // keep[j]: first of its (dist,id) run, not empty, not already pooled
-    for (int j = threadIdx.x; j < cp; j += MT) {
-        uint64_t k = s_c[j];
-        bool keep = k != KCNA_EMPTY_KEY && (j == 0 || (s_c[j - 1] >> 2) != (k >> 2));
-        if (keep) {
-            int lb = kcna_lower_bound(s_pool, (int)np, k); // pool keys carry flags: compare without them
-            // s_pool sorted by full key; equal (dist,id) has key in [k, k|3]
-            if (lb < (int)np && (s_pool[lb] >> 2) == (k >> 2)) keep = false;
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    const size_t per_warp = (size_t)MW_SMALL * 8 + (size_t)a.cap * 8 + (MW_SMALL + 1) * 4;
+    unsigned char *base = smem + w * ((per_warp + 15) & ~(size_t)15);
+    uint64_t *s_c = reinterpret_cast<uint64_t *>(base);
+    uint64_t *s_pool = s_c + MW_SMALL;
+    uint32_t *s_keep = reinterpret_cast<uint32_t *>(s_pool + a.cap);
+    __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
+    if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t node = blockIdx.x * MW_WARPS + w;
+    if (node < N) {
+        const uint32_t raw = a.cand_cnt[node];
+        const uint32_t nc = min(raw, a.CB);
+        const uint32_t np = min(a.pool_cnt[node], a.limit);
+        uint64_t *gp = a.pool + (uint64_t)node * a.cap;
+        if (nc > (uint32_t)MW_SMALL) {
+            if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = node;
+        } else if (nc == 0) {
+            unsigned long long f = 0;
+            for (uint32_t i = lane; i < min(np, a.K); i += 32) f += (gp[i] & KCNA_FLAG_NEW) ? 1 : 0;
+            f = kcna_warp_sum(f);
+            if (lane == 0 && f) atomicAdd(&s_stat[0], f);
+        } else {
+            for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
+            const int cp = kcna_pow2_ceil_d((int)nc);
+            const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+            for (int i = lane; i < cp; i += 32) s_c[i] = i < (int)nc ? kcna_key_noflags(gc[i]) : KCNA_EMPTY_KEY;
+            kcna_warp_bitonic(s_c, cp);
+            // keep flags + exclusive scan, 32 at a time
+            uint32_t run = 0;
+            for (int b0 = 0; b0 < cp; b0 += 32) {
+                const int j = b0 + lane;
+                bool keep = false;
+                if (j < cp) {
+                    uint64_t k = s_c[j];
+                    keep = k != KCNA_EMPTY_KEY && (j == 0 || (s_c[j - 1] >> 2) != (k >> 2));
+                    if (keep) {
+                        int lb = kcna_lower_bound(s_pool, (int)np, k);
+                        if (lb < (int)np && (s_pool[lb] >> 2) == (k >> 2)) keep = false;
+                    }
+                }
+                unsigned mk = __ballot_sync(KCNA_FULL, keep);
+                if (j < cp) s_keep[j] = run + __popc(mk & kcna_lanemask_lt());
+                run += __popc(mk);
+            }
+            if (lane == 0) s_keep[cp] = run;
+            __syncwarp();
+            const uint32_t kept = run;
+            const uint32_t newcnt = min(a.limit, np + kept);
+            unsigned long long flagged = 0;
+            for (uint32_t i = lane; i < np; i += 32) {
+                uint64_t k = s_pool[i];
+                int lb = kcna_lower_bound(s_c, cp, kcna_key_noflags(k));
+                uint32_t r = i + s_keep[lb];
+                if (r < newcnt) {
+                    gp[r] = k;
+                    if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
+                }
+            }
+            for (int j = lane; j < cp; j += 32) {
+                if (s_keep[j + 1] == s_keep[j]) continue;
+                uint64_t k = s_c[j];
+                uint32_t r = s_keep[j] + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
+                if (r < newcnt) {
+                    gp[r] = k | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
+                    if (r < a.K) ++flagged;
+                }
+            }
+            flagged = kcna_warp_sum(flagged);
+            __syncwarp();
+            if (lane == 0) {
+                if (flagged) atomicAdd(&s_stat[0], flagged);
+                atomicAdd(&s_stat[1], (unsigned long long)(newcnt - min(np, newcnt)));
+                atomicAdd(&s_stat[2], (unsigned long long)nc);
+                atomicAdd(&s_stat[3], (unsigned long long)newcnt);
+                if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
+                a.pool_cnt[node] = newcnt;
+                a.cand_cnt[node] = 0;
+                a.radius[node] =
+                    newcnt >= a.limit ? kcna_key_dist(gp[a.limit - 1]) : __uint_as_float(0x7F800000u);
+            }
         }
-        s_scan[j] = keep ? 1u : 0u;
     }
     __syncthreads();
-    // exclusive scan of keep flags over cp entries (block-wide, chunked)
-    {
-        const int per = (cp + MT - 1) / MT;
-        const int b = threadIdx.x * per;
-        uint32_t local = 0;
-        for (int i = 0; i < per && b + i < cp; ++i) local += s_scan[b + i];
-        uint32_t incl = local;
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        if (s_stat[0]) atomicAdd(a.counters + 1, s_stat[0]);
+        if (s_stat[1]) atomicAdd(a.counters + 3, s_stat[1]);
+        if (s_stat[2]) atomicAdd(a.counters + 7, s_stat[2]);
+        if (s_stat[3]) atomicAdd(a.counters + 9, s_stat[3]);
+    }
+}
+
+// In-place exclusive scan of data[0..n) by the whole block; data[n] receives
+// the total.  s_warp holds blockDim.x/32 words.
+__device__ uint32_t block_exclusive_scan(uint32_t *data, int n, uint32_t *s_warp) {
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per;
+    uint32_t local = 0;
+    for (int i = 0; i < per && b + i < n; ++i) local += data[b + i];
+    uint32_t incl = local;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t u = __shfl_up_sync(KCNA_FULL, incl, o);
-            if (lane >= o) incl += u;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(KCNA_FULL, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            uint32_t t = s_warp[i];
+            s_warp[i] = run;
+            run += t;
         }
-        if (lane == 31) s_warp[w] = incl;
+    }
+    __syncthreads();
+    uint32_t run = s_warp[w] + incl - local;
+    for (int i = 0; i < per && b + i < n; ++i) {
+        uint32_t t = data[b + i];
+        data[b + i] = run;
+        run += t;
+    }
+    if (threadIdx.x == blockDim.x - 1) data[n] = run;
+    __syncthreads();
+    return data[n];
+}
+
+// Block merge of nodes with many candidates (queued by merge_warp_kernel).
+// Each candidate is placed by binary search into the gap of the sorted pool
+// it falls in (its bucket: the number of pool entries below it); candidates
+// equal to a pool entry or with bucket >= limit are dropped.  A counting sort
+// by bucket then an insertion sort inside each bucket (block bitonic for the
+// rare bucket above 32 entries) leave all candidates sorted, since buckets
+// are ordered; duplicates are then adjacent.  Final position of pool entry i
+// = i + kept candidates in buckets 0..i; of a kept candidate in bucket b =
+// b + kept candidates before it.  Work is O(c log L + L) instead of a full
+// sort of the candidates.
+__global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *big_list, const uint32_t *big_cnt) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int cbp = kcna_pow2_ceil_d((int)a.CB);
+    uint64_t *s_pool = reinterpret_cast<uint64_t *>(smem); // cap
+    uint64_t *s_c = s_pool + a.cap;                        // cbp (candidate keys, then bitonic scratch)
+    uint64_t *s_sorted = s_c + cbp;                        // cbp
+    uint32_t *s_b = reinterpret_cast<uint32_t *>(s_sorted + cbp); // cbp  bucket per candidate
+    uint32_t *s_kept = s_b + cbp;                          // cbp + 1
+    uint32_t *s_hist = s_kept + cbp + 1;                   // cap + 2
+    uint32_t *s_off = s_hist + a.cap + 2;                  // cap + 2
+    uint32_t *s_giant = s_off + a.cap + 2;                 // cap + 2
+    __shared__ uint32_t s_warp[MT / 32];
+    __shared__ uint32_t s_ngiant;
+    __shared__ unsigned long long s_flagged;
+    for (uint32_t bi = blockIdx.x; bi < *big_cnt; bi += gridDim.x) {
         __syncthreads();
+        const uint32_t node = big_list[bi];
+        const uint32_t raw = a.cand_cnt[node];
+        const uint32_t nc = min(raw, a.CB);
+        const uint32_t np = min(a.pool_cnt[node], a.limit);
+        uint64_t *gp = a.pool + (uint64_t)node * a.cap;
+        const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
         if (threadIdx.x == 0) {
-            uint32_t run = 0;
-            for (int i = 0; i < MT / 32; ++i) {
-                uint32_t t = s_warp[i];
-                s_warp[i] = run;
-                run += t;
+            s_flagged = 0;
+            s_ngiant = 0;
+        }
+        for (uint32_t i = threadIdx.x; i < np; i += MT) s_pool[i] = gp[i];
+        for (uint32_t i = threadIdx.x; i <= np + 1; i += MT) s_hist[i] = 0;
+        __syncthreads();
+        // bucket of every candidate
+        for (uint32_t j = threadIdx.x; j < nc; j += MT) {
+            const uint64_t k = kcna_key_noflags(gc[j]);
+            s_c[j] = k;
+            const int b = kcna_lower_bound(s_pool, (int)np, k);
+            const bool dup = b < (int)np && (s_pool[b] >> 2) == (k >> 2);
+            if (dup || b >= (int)a.limit || k == KCNA_EMPTY_KEY_NOFLAGS) {
+                s_b[j] = KCNA_NONE;
+            } else {
+                s_b[j] = (uint32_t)b;
+                atomicAdd(&s_hist[b], 1u);
             }
         }
         __syncthreads();
-        uint32_t run = s_warp[w] + incl - local;
-        for (int i = 0; i < per && b + i < cp; ++i) {
-            uint32_t t = s_scan[b + i];
-            s_scan[b + i] = run;
-            run += t;
-        }
-        if (threadIdx.x == MT - 1) s_scan[cp] = run;
+        for (uint32_t i = threadIdx.x; i <= np; i += MT) s_off[i] = s_hist[i];
         __syncthreads();
-    }
-    const uint32_t kept = s_scan[cp];
-    const uint32_t newcnt = min(a.limit, np + kept);
-    // ranks: pool element i -> i + #kept candidates below it; kept candidate j -> scan[j] + #pool below it
-    // write straight to the global pool (its entries are staged in s_pool)
-    unsigned long long flagged = 0;
-    for (uint32_t i = threadIdx.x; i < np; i += MT) {
-        uint64_t k = s_pool[i];
-        int lb = kcna_lower_bound(s_c, cp, kcna_key_noflags(k));
-        uint32_t r = i + s_scan[lb];
-        if (r < newcnt) {
-            gp[r] = k;
-            if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
+        const uint32_t total = block_exclusive_scan(s_off, (int)np + 1, s_warp); // s_off[np+1] = total
+        for (uint32_t i = threadIdx.x; i <= np; i += MT) s_hist[i] = 0;
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < nc; j += MT) {
+            const uint32_t b = s_b[j];
+            if (b != KCNA_NONE) s_sorted[s_off[b] + atomicAdd(&s_hist[b], 1u)] = s_c[j];
         }
-    }
-    for (int j = threadIdx.x; j < cp; j += MT) {
-        uint64_t k = s_c[j];
-        bool keep = s_scan[j + 1] != s_scan[j];
-        if (!keep) continue;
-        uint32_t r = s_scan[j] + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
-        if (r < newcnt) {
-            gp[r] = k | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
-            if (r < a.K) ++flagged;
+        __syncthreads();
+        // sort inside buckets
+        for (uint32_t b = threadIdx.x; b <= np; b += MT) {
+            const uint32_t lo = s_off[b], hi = s_off[b + 1];
+            if (hi - lo > 32) {
+                s_giant[atomicAdd(&s_ngiant, 1u)] = b;
+            } else {
+                for (uint32_t x = lo + 1; x < hi; ++x) {
+                    const uint64_t v = s_sorted[x];
+                    uint32_t y = x;
+                    while (y > lo && s_sorted[y - 1] > v) {
+                        s_sorted[y] = s_sorted[y - 1];
+                        --y;
+                    }
+                    s_sorted[y] = v;
+                }
+            }
         }
+        __syncthreads();
+        const uint32_t ng = s_ngiant;
+        for (uint32_t g = 0; g < ng; ++g) {
+            const uint32_t b = s_giant[g];
+            const uint32_t lo = s_off[b], len = s_off[b + 1] - lo;
+            const int p2 = kcna_pow2_ceil_d((int)len);
+            for (int i = threadIdx.x; i < p2; i += MT) s_c[i] = i < (int)len ? s_sorted[lo + i] : KCNA_EMPTY_KEY;
+            kcna_cta_bitonic(s_c, p2);
+            for (uint32_t i = threadIdx.x; i < len; i += MT) s_sorted[lo + i] = s_c[i];
+            __syncthreads();
+        }
+        // duplicates among candidates are now adjacent
+        for (uint32_t j = threadIdx.x; j < total; j += MT)
+            s_kept[j] = (j == 0 || (s_sorted[j - 1] >> 2) != (s_sorted[j] >> 2)) ? 1u : 0u;
+        __syncthreads();
+        const uint32_t kept = block_exclusive_scan(s_kept, (int)total, s_warp);
+        const uint32_t newcnt = min(a.limit, np + kept);
+        unsigned long long flagged = 0;
+        for (uint32_t i = threadIdx.x; i < np; i += MT) {
+            const uint64_t k = s_pool[i];
+            const uint32_t r = i + s_kept[s_off[i + 1]];
+            if (r < newcnt) {
+                gp[r] = k;
+                if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
+            }
+        }
+        for (uint32_t j = threadIdx.x; j < total; j += MT) {
+            if (s_kept[j + 1] == s_kept[j]) continue; // duplicate
+            // bucket of sorted position j: last b with s_off[b] <= j
+            int lo = 0, hi = (int)np + 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= j)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const uint32_t r = (uint32_t)lo + s_kept[j];
+            if (r < newcnt) {
+                gp[r] = s_sorted[j] | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
+                if (r < a.K) ++flagged;
+            }
+        }
+        flagged = kcna_warp_sum(flagged);
+        if ((threadIdx.x & 31) == 0 && flagged) atomicAdd(&s_flagged, flagged);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicAdd(a.counters + 1, s_flagged);
+            if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
+            atomicAdd(a.counters + 3, (unsigned long long)(newcnt - min(np, newcnt)));
+            atomicAdd(a.counters + 7, (unsigned long long)nc);
+            atomicAdd(a.counters + 9, (unsigned long long)newcnt);
+            a.pool_cnt[node] = newcnt;
+            a.cand_cnt[node] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            a.radius[node] = newcnt >= a.limit ? kcna_key_dist(gp[a.limit - 1]) : __uint_as_float(0x7F800000u);
     }
-    flagged = kcna_warp_sum(flagged);
-    if ((threadIdx.x & 31) == 0 && flagged) atomicAdd(&s_flagged, flagged);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        atomicAdd(a.counters + 1, s_flagged);
-        if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
-        atomicAdd(a.counters + 3, (unsigned long long)(newcnt - min(np, newcnt)));
-        atomicAdd(a.counters + 7, (unsigned long long)nc);
-        atomicAdd(a.counters + 9, (unsigned long long)newcnt);
-        a.pool_cnt[node] = newcnt;
-        a.cand_cnt[node] = 0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-        a.radius[node] = newcnt >= a.limit ? kcna_key_dist(gp[a.limit - 1]) : __uint_as_float(0x7F800000u);
 }
 
 // ---------------------------------------------------------------------------
@@ -606,7 +771,7 @@ size_t join_smem_bytes(uint32_t capA, uint32_t capB) {
 }
 size_t merge_smem_bytes(uint32_t cap, uint32_t CB) {
     size_t cp = (size_t)kcna_pow2_ceil((int)CB);
-    return cap * 8 + cp * 8 + (cp + 1) * 4;
+    return cap * 8 + cp * 8 * 2 + cp * 4 + (cp + 1) * 4 + (size_t)(cap + 2) * 4 * 3;
 }
 
 } // namespace
@@ -639,6 +804,8 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     KCNA_TRY(kcna_alloc(c, &c->rold_cnt, N, "rold_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
     KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->big_list, N, "merge queue"));
+    KCNA_TRY(kcna_alloc(c, &c->big_cnt, 1, "merge queue count"));
     if (!c->counters) KCNA_TRY(kcna_alloc(c, &c->counters, 64, "counters"));
     cudaStream_t s = c->stream;
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->cand_cnt, 0, N * 4, s), "memset"));
@@ -714,7 +881,8 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     return KCNA_OK;
 }
 
-kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk) {
+kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
+                       uint64_t *merged, uint64_t *inserted) {
     MergeArgs a;
     a.pool = c->pool;
     a.pool_cnt = c->pool_cnt;
@@ -730,10 +898,17 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "merge smem attr"));
+    const size_t smw = (((size_t)MW_SMALL * 8 + (size_t)c->cap * 8 + (MW_SMALL + 1) * 4 + 15) & ~(size_t)15) * MW_WARPS;
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(smw, 48 * 1024)),
+                             "merge smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->big_cnt, 0, 4, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    merge_kernel<<<c->n, MT, sm, c->stream>>>(a);
-    KCNA_LAUNCHED(c);
+    merge_warp_kernel<<<kcna_div_up(c->n, MW_WARPS), MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list,
+                                                                                      c->big_cnt);
+    merge_kernel<<<std::max(1, c->num_sms) * 4, MT, sm, c->stream>>>(a, c->big_list, c->big_cnt);
+    c->launches += 2;
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_MERGE));
     unsigned long long h[10] = {};
@@ -741,6 +916,8 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "merge sync"));
     c->cand_merged += h[7];
     c->pool_entries_merged += h[9];
+    if (merged) *merged = h[7];
+    if (inserted) *inserted = h[3];
     if (overflow) *overflow = h[2];
     if (flagged_topk) *flagged_topk = h[1];
     return KCNA_OK;
@@ -857,9 +1034,16 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
     st->stop_condition = 0;
     st->iterations = 0;
     for (uint32_t it = 0; it < P.iterations; ++it) {
-        uint64_t comps = 0, overflow = 0, flagged = 0;
+        uint64_t comps = 0, overflow = 0, flagged = 0, merged = 0, inserted = 0;
+        const double j0 = c->phase_ms[KCNA_PHASE_JOIN], m0 = c->phase_ms[KCNA_PHASE_MERGE];
         KCNA_TRY(kcna_nnd_join(c, &P, (int)it, &comps));
-        KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged));
+        KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged, &merged, &inserted));
+        if (it < KCNA_MAX_ITERS) {
+            st->iter_join_ms[it] = c->phase_ms[KCNA_PHASE_JOIN] - j0;
+            st->iter_merge_ms[it] = c->phase_ms[KCNA_PHASE_MERGE] - m0;
+            st->iter_cand[it] = merged;
+            st->iter_inserted[it] = inserted;
+        }
         comps_total += comps;
         float delta = (float)((double)flagged / ((double)N * P.K));
         float recall = 0.f;

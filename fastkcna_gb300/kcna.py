@@ -63,7 +63,9 @@ class Stats(C.Structure):
         ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
         ("phase_ms", C.c_double * NUM_PHASES), ("phase_launches", C.c_uint64 * NUM_PHASES),
         ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
-        ("pool_entries_merged", C.c_uint64)]
+        ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
+        ("iter_join_ms", C.c_double * MAX_ITERS), ("iter_merge_ms", C.c_double * MAX_ITERS),
+        ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS)]
 
     def as_dict(self):
         it = self.iterations
@@ -81,7 +83,9 @@ class Stats(C.Structure):
                     phase_ms={PHASES[i]: self.phase_ms[i] for i in range(NUM_PHASES)},
                     phase_launches={PHASES[i]: int(self.phase_launches[i]) for i in range(NUM_PHASES)},
                     join_rows=self.join_rows, cand_emitted=self.cand_emitted, cand_merged=self.cand_merged,
-                    pool_entries_merged=self.pool_entries_merged)
+                    pool_entries_merged=self.pool_entries_merged, tree_attached=self.tree_attached,
+                    iter_join_ms=list(self.iter_join_ms[:it]), iter_merge_ms=list(self.iter_merge_ms[:it]),
+                    iter_cand=list(self.iter_cand[:it]), iter_inserted=list(self.iter_inserted[:it]))
 
 
 _lib = None

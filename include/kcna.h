@@ -134,6 +134,11 @@ typedef struct {
     uint64_t cand_emitted;     /* candidates written to buffers (join + P2K) */
     uint64_t cand_merged;      /* candidates read by the merges */
     uint64_t pool_entries_merged; /* pool entries rewritten by the merges */
+    uint64_t tree_attached;    /* edges added by tree_grow to reach unreached nodes */
+    double iter_join_ms[KCNA_MAX_ITERS];   /* device time of each NN-descent join */
+    double iter_merge_ms[KCNA_MAX_ITERS];  /* device time of each NN-descent merge */
+    uint64_t iter_cand[KCNA_MAX_ITERS];    /* candidates merged in each NN-descent iteration */
+    uint64_t iter_inserted[KCNA_MAX_ITERS]; /* of which inserted into pools */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;

@@ -49,7 +49,9 @@ class Stats(C.Structure):
         ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
         ("phase_ms", C.c_double * 12), ("phase_launches", C.c_uint64 * 12),
         ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
-        ("pool_entries_merged", C.c_uint64),
+        ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
+        ("iter_join_ms", C.c_double * MAX_ITERS), ("iter_merge_ms", C.c_double * MAX_ITERS),
+        ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
     ]
 
 
