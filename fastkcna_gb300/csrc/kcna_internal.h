@@ -116,6 +116,11 @@ kcna_status kcna_knn_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint
 // gathers rows ids[0..m) of X into dst (m x ld)
 kcna_status kcna_gather_rows(kcna_ctx *c, const uint32_t *d_ids, uint32_t m, float *dst);
 
+// kcna_tc.cu: BF16 tensor-core GEMM, C = A * B^T (+ beta * C)
+kcna_status kcna_tc_gemm(cudaStream_t s, const void *A, int64_t lda, int a_fp32, int a_trans, const void *B,
+                         int64_t ldb, int b_fp32, int b_trans, float *C, int64_t ldc, int M, int N, int K, float beta,
+                         int *err);
+
 // kcna_nnd.cu: NN-descent phases
 kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);

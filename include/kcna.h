@@ -243,6 +243,15 @@ kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n, uint32_t d
                                      const float *d_queries, uint32_t m, uint64_t q_stride_bytes, uint32_t k,
                                      uint32_t *d_out_ids, float *d_out_dists, void *stream);
 
+/* C[M x N] (FP32, row-major, pitch ldc) = A * B^T on the tcgen05 tensor cores
+ * in BF16 with FP32 accumulation.  Element (r, k) of A is A[r * lda + k]
+ * (a_trans = 1: A[k * lda + r]); a_fp32 selects FP32 (converted to BF16 with
+ * round-to-nearest-even) or BF16 storage; likewise B.  Device pointers, runs
+ * on `stream` and synchronises it.  No counterpart in the reference: the
+ * product primitive of the learned-seed encoder and the BF16 distance screen. */
+kcna_status kcna_gemm_bf16(const void *A, int64_t lda, int a_fp32, int a_trans, const void *B, int64_t ldb,
+                           int b_fp32, int b_trans, float *C, int64_t ldc, int M, int N, int K, void *stream);
+
 /* Writes the graph in the NSG/efanna format written by SaveNsg
  * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */
 kcna_status kcna_write_nsg(kcna_ctx *ctx, const char *path);
