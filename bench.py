@@ -236,11 +236,25 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.set_device(local)
     n = args.n
     X = synth.base("c2", n)
-    p = kcna.params(**FLAGS)
+    mode = dict(learned_seed=1, screen=1) if args.mode == "learned_bf16" else {}
+    p = kcna.params(**FLAGS, **mode)
+    p_plain = kcna.params(**FLAGS)
     ix = kcna.Index(local)
     stream = torch.cuda.ExternalStream(ix.stream, device=torch.device("cuda", local))
     ix.upload(X)
     for _ in range(args.warmup):
+        ix.build("nsg", p)
+    # the plain FP32 build, timed the same way, for the learned+BF16 vs plain comparison
+    plain_ms = None
+    if args.mode == "learned_bf16":
+        ix.build("nsg", p_plain)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plain_stats = [ix.build("nsg", p_plain) for _ in range(args.steps)]
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms = e0.elapsed_time(e1) / args.steps
         ix.build("nsg", p)
     # timed region: device-resident rows, one build per step
     clock = ClockSampler(local)
@@ -294,7 +308,8 @@ def run_gpu(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "c2 FastNSG 1M x 128 (integer-valued 256-cluster mixture)", "n": n,
-                   "mode": "plain FP32", "l2_policy": "inputs larger than L2 (rows 512 MB, pools 4 GB)",
+                   "mode": "learned seed + BF16" if args.mode == "learned_bf16" else "plain FP32",
+                   "l2_policy": "inputs larger than L2 (rows 512 MB, pools 4 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU", **FLAGS,
                    "knn_recall_at_K": round(final_recall, 4),
                    "nndescent_iterations": st["iterations"],
@@ -307,7 +322,12 @@ def run_gpu(args, ws, rank, local):
                    "iter_join_ms": [round(x, 1) for x in st["iter_join_ms"]],
                    "iter_merge_ms": [round(x, 1) for x in st["iter_merge_ms"]],
                    "iter_cand_M": [round(x / 1e6, 1) for x in st["iter_cand"]],
-                   "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]]},
+                   "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]],
+                   "bf16_rows": st["bf16_rows"], "seed_ms": round(st["seed_total_ms"], 1),
+                   "seed_recall": round(st["seed_recall"], 4),
+                   "plain_fp32_s": round(plain_ms / 1000.0, 4) if plain_ms else None,
+                   "plain_fp32_knn_recall_at_K": round(plain_stats[-1]["loop_recall"][-1], 4) if plain_ms else None,
+                   "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None},
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
                 "d2h_bytes_per_step": int(n * W * 4 + n * 4 + 8)},
@@ -335,6 +355,7 @@ def main():
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--cpu-n", type=int, default=50_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="learned_bf16", choices=["learned_bf16", "plain"])
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -18,6 +18,7 @@
 #include <set>
 #include <vector>
 
+#include "kcna_common.cuh"
 #include "kcna_internal.h"
 
 #ifndef KCNA_VERSION_STRING
@@ -156,6 +157,45 @@ static void free_state(kcna_ctx *c) {
 
 static kcna_status bind(kcna_ctx *c) { return kcna_cuda_check(c, cudaSetDevice(c->device), "cudaSetDevice"); }
 
+// A float is exactly representable in BF16 when its low 16 bits are zero.
+__global__ void bf16_inexact_kernel(const uint32_t *__restrict__ x, uint64_t n, unsigned long long *inexact) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long bad = 0;
+    for (; t < n; t += (uint64_t)gridDim.x * blockDim.x) bad += (x[t] & 0xFFFFu) ? 1 : 0;
+    bad = kcna_warp_sum(bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(inexact, bad);
+}
+__global__ void bf16_copy_kernel(const uint32_t *__restrict__ x, uint64_t n, uint16_t *__restrict__ out) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = (uint16_t)(x[t] >> 16);
+}
+
+// BF16 mode: when every value of the rows is exactly representable in BF16,
+// kernels read a BF16 copy (same floats, half the bytes).  Returns whether the
+// copy is in use.
+static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *used) {
+    *used = 0;
+    if (c->Xh) {
+        cudaFree(c->Xh);
+        c->Xh = nullptr;
+    }
+    if (!p || p->screen != KCNA_SCREEN_BF16) return KCNA_OK;
+    const uint64_t n = (uint64_t)c->n_total * c->ld;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 40, 0, 8, c->stream), "memset"));
+    bf16_inexact_kernel<<<std::max(1, c->num_sms) * 8, 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n,
+                                                                             c->counters + 40);
+    KCNA_LAUNCHED(c);
+    unsigned long long bad = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&bad, c->counters + 40, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bf16 check"));
+    if (bad) return KCNA_OK; // inexact data: FP32 rows
+    KCNA_TRY(kcna_alloc(c, &c->Xh, n, "bf16 rows"));
+    bf16_copy_kernel<<<kcna_div_up(n, 256), 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n, c->Xh);
+    KCNA_LAUNCHED(c);
+    *used = 1;
+    return kcna_cuda_check(c, cudaGetLastError(), "bf16 copy");
+}
+
 extern "C" {
 
 void kcna_params_default(kcna_params *p) {
@@ -215,6 +255,7 @@ void kcna_destroy(kcna_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_state(c);
     if (c->X) cudaFree(c->X);
+    if (c->Xh) cudaFree(c->Xh);
     if (c->scratch) cudaFree(c->scratch);
     if (c->scratch2) cudaFree(c->scratch2);
     if (c->d_err) cudaFree(c->d_err);
@@ -239,6 +280,8 @@ static kcna_status upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d
     free_state(c);
     if (c->X) cudaFree(c->X);
     c->X = nullptr;
+    if (c->Xh) cudaFree(c->Xh);
+    c->Xh = nullptr;
     c->d = d;
     c->ld = (d + 3) & ~3u;
     c->n_total = c->n = n;
@@ -343,6 +386,7 @@ kcna_status kcna_nndescent(kcna_ctx *c, const kcna_params *p, kcna_stats *st) {
     free_state(c);
     reset_phase_stats(c);
     c->t0 = kcna_now();
+    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows));
     KCNA_TRY(kcna_nndescent_run(c, p, st));
     float r = 0;
     KCNA_TRY(kcna_control_recall(c, c->cap, &r));
@@ -386,6 +430,7 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
     reset_phase_stats(c);
     c->t0 = kcna_now();
     kcna_params P = *p;
+    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows));
     KCNA_TRY(kcna_nndescent_run(c, &P, st));
     const uint32_t maxl = c->cap;
     if (c->n <= P.K) P.loop_i = 0; // clamping of src/kgraph.cpp:1320-1327
@@ -520,6 +565,8 @@ kcna_status kcna_prune(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
     if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "prune: null argument");
     KCNA_TRY(bind(c));
     uint64_t comps = 0;
+    uint32_t used = 0;
+    KCNA_TRY(prepare_rows(c, p, &used));
     KCNA_TRY(kcna_prune_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
     return kcna_check_device_err(c, "prune");
 }
@@ -528,6 +575,8 @@ kcna_status kcna_link(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
     if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "link: null argument");
     KCNA_TRY(bind(c));
     uint64_t comps = 0;
+    uint32_t used = 0;
+    KCNA_TRY(prepare_rows(c, p, &used));
     KCNA_TRY(kcna_link_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
     return kcna_check_device_err(c, "link");
 }

@@ -77,6 +77,49 @@ __device__ __forceinline__ float kcna_l2_ldg(const float *__restrict__ a, const 
 }
 
 // ---------------------------------------------------------------------------
+// Row storage.  RowsF32 reads the FP32 rows; RowsB16 reads a BF16 copy, used
+// only when every value of the data is exactly representable in BF16 (checked
+// when the build starts), so both give the same floats and hence the same
+// canonical distances with half the bytes.  ld4(r, k4) returns floats
+// 4*k4 .. 4*k4+3 of row r.
+// ---------------------------------------------------------------------------
+struct RowsF32 {
+    const float *p;
+    int ld;
+    __device__ __forceinline__ float4 ld4(uint64_t r, int k4) const {
+        return __ldg(reinterpret_cast<const float4 *>(p + r * (uint64_t)ld) + k4);
+    }
+};
+struct RowsB16 {
+    const uint16_t *p;
+    int ld;
+    __device__ __forceinline__ float4 ld4(uint64_t r, int k4) const {
+        const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p + r * (uint64_t)ld) + k4);
+        return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u), __uint_as_float(u.y << 16),
+                           __uint_as_float(u.y & 0xFFFF0000u));
+    }
+};
+// canonical distance between rows a and b of R
+template <class R>
+__device__ __forceinline__ float rows_l2(const R &rows, uint64_t a, uint64_t b) {
+    float acc = 0.f;
+    const int nv = rows.ld >> 2;
+    for (int k0 = 0; k0 < nv; k0 += 8) { // eight loads of each row in flight
+        float4 x[8], y[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const bool in = k0 + u < nv;
+            x[u] = in ? rows.ld4(a, k0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+            y[u] = in ? rows.ld4(b, k0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (k0 + u < nv) acc = kcna_acc4(acc, x[u], y[u]);
+    }
+    return acc;
+}
+
+// ---------------------------------------------------------------------------
 // Counter-based RNG (splitmix64) so that random draws depend only on
 // (seed, stream, index) and not on thread scheduling.
 // ---------------------------------------------------------------------------

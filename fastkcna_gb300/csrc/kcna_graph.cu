@@ -41,28 +41,22 @@ __device__ __forceinline__ bool occludes(const PruneRule &r, float td, float djk
     return djk < pd;
 }
 
-// Two-phase form of warp_prune with the same result.  Almost every candidate is
-// occluded by one of the first kept neighbours, so each batch of 32 candidates
-// is first tested against kept[0..3] with four independent FMA chains per lane
-// (the candidate row is read once); the few survivors are then tested one at
-// a time against kept[4..nk) with one lane per kept row.  With STAGED the kept
-// rows are copied into shared memory (pitch ld+4 floats, conflict-free float4
-// reads) as they are kept.  The in-batch resolution is the same as warp_prune.
-template <bool STAGED, typename GetFn>
-__device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracle, const PruneRule &rule, int first,
-                           int lim, int range, GetFn get, uint32_t *kid, float *kd, float *kr,
-                           unsigned long long *comps) {
+// Occlusion prune of one candidate list by one warp, in the reference's order
+// (kept[0] = first candidate; each later candidate p is dropped when a kept t
+// has the same id or occludes it; stop at `range` kept), with the same result
+// as the sequential scan.  Almost every candidate is occluded by one of the
+// first kept neighbours, so each batch of 32 candidates (one per lane) is first
+// tested against kept[0..3] with four independent FMA chains (the candidate row
+// is read once, eight loads in flight); the few survivors are then tested one
+// at a time against kept[4..nk) with one lane per kept row; finally the batch
+// is resolved in candidate order (the first unoccluded lane is kept and tests
+// the later lanes).  Rows are read through R (FP32 or exact BF16 copy).
+template <class R, typename GetFn>
+__device__ int warp_prune(const R &rows, uint32_t n_oracle, const PruneRule &rule, int first, int lim, int range,
+                          GetFn get, uint32_t *kid, float *kd, unsigned long long *comps) {
     const int lane = kcna_lane();
-    const int krp = ld + 4;
+    const int nv = rows.ld >> 2;
     if (first >= lim || range <= 0) return 0;
-    auto krow = [&](int t) -> const float * { return STAGED ? kr + (size_t)t * krp : X + (uint64_t)kid[t] * ld; };
-    auto stage = [&](int t, uint32_t id) {
-        if (STAGED) {
-            const float4 *src = reinterpret_cast<const float4 *>(X + (uint64_t)id * ld);
-            float4 *dst = reinterpret_cast<float4 *>(kr + (size_t)t * krp);
-            for (int k = lane; k < (ld >> 2); k += 32) dst[k] = __ldg(src + k);
-        }
-    };
     int nk = 0;
     {
         uint32_t id0;
@@ -72,8 +66,6 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
             kid[0] = id0;
             kd[0] = d0;
         }
-        __syncwarp();
-        stage(0, id0);
         nk = 1;
     }
     __syncwarp();
@@ -87,31 +79,24 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
             get(i, id, pd);
             live = id < n_oracle; // src/kgraph.cpp:1822 `if (p.id >= oracle.size()) continue;`
         }
-        const float *prow = X + (uint64_t)(live ? id : 0) * ld;
         bool occ = false;
         // phase 1: kept[0..min(nk,4)), four independent chains, candidate row read once
         const int t1 = min(nk, 4);
         if (live) {
+            const uint32_t k0 = kid[0], k1 = kid[t1 > 1 ? 1 : 0], k2 = kid[t1 > 2 ? 2 : 0], k3 = kid[t1 > 3 ? 3 : 0];
             float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-            const float4 *p4 = reinterpret_cast<const float4 *>(prow);
-            const float4 *k0 = reinterpret_cast<const float4 *>(krow(0));
-            const float4 *k1 = reinterpret_cast<const float4 *>(krow(t1 > 1 ? 1 : 0));
-            const float4 *k2 = reinterpret_cast<const float4 *>(krow(t1 > 2 ? 2 : 0));
-            const float4 *k3 = reinterpret_cast<const float4 *>(krow(t1 > 3 ? 3 : 0));
-            const int nv = ld >> 2;
-            for (int k0i = 0; k0i < nv; k0i += 8) { // eight independent row loads in flight
+            for (int b0 = 0; b0 < nv; b0 += 8) {
                 float4 pv[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    pv[u] = k0i + u < nv ? __ldg(p4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int u = 0; u < 8; ++u) pv[u] = b0 + u < nv ? rows.ld4(id, b0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    if (k0i + u >= nv) break;
-                    const int k = k0i + u;
-                    a0 = kcna_acc4(a0, k0[k], pv[u]);
-                    if (t1 > 1) a1 = kcna_acc4(a1, k1[k], pv[u]);
-                    if (t1 > 2) a2 = kcna_acc4(a2, k2[k], pv[u]);
-                    if (t1 > 3) a3 = kcna_acc4(a3, k3[k], pv[u]);
+                    if (b0 + u >= nv) break;
+                    const int k = b0 + u;
+                    a0 = kcna_acc4(a0, rows.ld4(k0, k), pv[u]);
+                    if (t1 > 1) a1 = kcna_acc4(a1, rows.ld4(k1, k), pv[u]);
+                    if (t1 > 2) a2 = kcna_acc4(a2, rows.ld4(k2, k), pv[u]);
+                    if (t1 > 3) a3 = kcna_acc4(a3, rows.ld4(k3, k), pv[u]);
                 }
             }
             const float ds[4] = {a0, a1, a2, a3};
@@ -136,7 +121,6 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
                 todo &= todo - 1;
                 const uint32_t bid = __shfl_sync(KCNA_FULL, id, b);
                 const float bd = __shfl_sync(KCNA_FULL, pd, b);
-                const float *brow = X + (uint64_t)bid * ld;
                 bool hit = false;
                 for (int t0 = 4; t0 < nk && !hit; t0 += 32) {
                     const int t = t0 + lane;
@@ -146,20 +130,7 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
                             h = true;
                         } else {
                             ++cc;
-                            const float4 *kt = reinterpret_cast<const float4 *>(krow(t)); // shared or global
-                            const float4 *b4 = reinterpret_cast<const float4 *>(brow);
-                            const int nv = ld >> 2;
-                            float acc = 0.f;
-                            for (int k0i = 0; k0i < nv; k0i += 8) {
-                                float4 bv[8];
-#pragma unroll
-                                for (int u = 0; u < 8; ++u)
-                                    bv[u] = k0i + u < nv ? __ldg(b4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                                for (int u = 0; u < 8; ++u)
-                                    if (k0i + u < nv) acc = kcna_acc4(acc, kt[k0i + u], bv[u]);
-                            }
-                            h = occludes(rule, kd[t], acc, bd);
+                            h = occludes(rule, kd[t], rows_l2(rows, kid[t], bid), bd);
                         }
                     }
                     hit = __ballot_sync(KCNA_FULL, h) != 0;
@@ -176,34 +147,17 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
                 kid[nk] = aid;
                 kd[nk] = ad;
             }
-            __syncwarp();
-            stage(nk, aid);
             ++nk;
             __syncwarp();
             rem &= ~((2u << a) - 1u); // lanes after a
-            bool mine = (rem >> lane) & 1u;
+            const bool mine = (rem >> lane) & 1u;
             bool o2 = false;
             if (mine) {
                 if (aid == id) {
                     o2 = true;
                 } else {
                     ++cc;
-                    // kept row a (staged copy when STAGED) against this lane's row, loads batched
-                    const float4 *ka = reinterpret_cast<const float4 *>(STAGED ? kr + (size_t)(nk - 1) * krp
-                                                                               : X + (uint64_t)aid * ld);
-                    const float4 *p4 = reinterpret_cast<const float4 *>(prow);
-                    const int nv = ld >> 2;
-                    float djk = 0.f;
-                    for (int k0i = 0; k0i < nv; k0i += 8) {
-                        float4 pv[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            pv[u] = k0i + u < nv ? __ldg(p4 + k0i + u) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            if (k0i + u < nv) djk = kcna_acc4(djk, ka[k0i + u], pv[u]);
-                    }
-                    o2 = occludes(rule, ad, djk, pd);
+                    o2 = occludes(rule, ad, rows_l2(rows, aid, id), pd);
                 }
             }
             rem &= ~__ballot_sync(KCNA_FULL, o2);
@@ -215,20 +169,20 @@ __device__ int warp_prune2(const float *__restrict__ X, int ld, uint32_t n_oracl
     return nk;
 }
 
-// Staged prune: one warp per node, kept rows in shared memory.
-template <bool STAGED>
-__global__ void prune2_kernel(const float *__restrict__ X, int ld, uint32_t N, const uint64_t *__restrict__ pool,
-                              const uint32_t *__restrict__ pool_cnt, uint32_t cap, PruneRule rule, int range, int maxc,
-                              uint32_t *__restrict__ g_ids, float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
-                              uint32_t W, unsigned long long *comps) {
+constexpr int PW = 4; // warps per prune block
+
+template <class R>
+__global__ void __launch_bounds__(PW * 32) prune_kernel(R rows, uint32_t N, const uint64_t *__restrict__ pool,
+                                                        const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                                        PruneRule rule, int range, int maxc,
+                                                        uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
+                                                        uint32_t *__restrict__ g_deg, uint32_t W,
+                                                        unsigned long long *comps) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
-    const size_t per_warp = (size_t)range * 2 * 4 + (STAGED ? (size_t)range * (ld + 4) * 4 : 0);
-    unsigned char *mine = smem + w * ((per_warp + 15) & ~(size_t)15);
-    float *kr = reinterpret_cast<float *>(mine);
-    uint32_t *kid = reinterpret_cast<uint32_t *>(mine + (STAGED ? (size_t)range * (ld + 4) * 4 : 0));
+    uint32_t *kid = reinterpret_cast<uint32_t *>(smem) + w * 2 * range;
     float *kd = reinterpret_cast<float *>(kid + range);
-    const uint32_t q = blockIdx.x * (blockDim.x >> 5) + w;
+    const uint32_t q = blockIdx.x * PW + w;
     if (q >= N) return;
     const uint64_t *pr = pool + (uint64_t)q * cap;
     const int cnt = (int)pool_cnt[q];
@@ -240,9 +194,7 @@ __global__ void prune2_kernel(const float *__restrict__ X, int ld, uint32_t N, c
         id = kcna_key_id(k);
         dd = kcna_key_dist(k);
     };
-    int nk = (first < cnt) ? warp_prune2<STAGED>(X, ld, N, rule, first, max(lim, first + 1), range, get, kid, kd, kr,
-                                                 comps)
-                           : 0;
+    const int nk = (first < cnt) ? warp_prune(rows, N, rule, first, max(lim, first + 1), range, get, kid, kd, comps) : 0;
     for (int j = lane; j < (int)W; j += 32) {
         g_ids[(uint64_t)q * W + j] = j < nk ? kid[j] : KCNA_NONE;
         g_dist[(uint64_t)q * W + j] = j < nk ? kd[j] : 0.f;
@@ -330,10 +282,11 @@ __global__ void scan_apply(const uint32_t *__restrict__ in, uint64_t n, const ui
 constexpr int LT = 128;
 constexpr int LCAP = 4096; // merged-list capacity per node in shared memory
 
-__global__ void __launch_bounds__(LT) link_merge_kernel(const float *__restrict__ X, int ld, uint32_t N,
-                                                       PruneRule rule, int range, uint32_t *__restrict__ g_ids,
-                                                       float *__restrict__ g_dist, uint32_t *__restrict__ g_deg,
-                                                       uint32_t W, const uint64_t *__restrict__ off,
+template <class R>
+__global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, PruneRule rule, int range,
+                                                       uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
+                                                       uint32_t *__restrict__ g_deg, uint32_t W,
+                                                       const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ rev,
                                                        unsigned long long *comps, int *err) {
     __shared__ uint64_t s_key[LCAP];   // sorting keys (rev ids; later (dist, position))
@@ -401,7 +354,7 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(const float *__restrict_
         if (flags & (1u << e)) {
             uint32_t src = (uint32_t)s_key[b + e];
             s_id[pos] = src;
-            s_d[pos] = kcna_l2_ldg(X + (uint64_t)src * ld, X + (uint64_t)q * ld, ld); // oracle(n, des)
+            s_d[pos] = rows_l2(rows, src, q); // oracle(n, des)
             ++pos;
         }
     const int total = deg + s_nk;
@@ -432,7 +385,7 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(const float *__restrict_
             get(0, id0, d0);
             if (id0 == q) first = 1;
         }
-        int nk = warp_prune2<false>(X, ld, 0xFFFFFFFFu, rule, first, total, range, get, s_kid, s_kd, nullptr, comps);
+        int nk = warp_prune(rows, 0xFFFFFFFFu, rule, first, total, range, get, s_kid, s_kd, comps);
         for (int j = lane; j < (int)W; j += 32) {
             g_ids[(uint64_t)q * W + j] = j < nk ? s_kid[j] : KCNA_NONE;
             g_dist[(uint64_t)q * W + j] = j < nk ? s_kd[j] : 0.f;
@@ -845,8 +798,8 @@ __global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint6
 // u, written as one run per (q, u) after one atomicAdd.
 constexpr int PJT = 256, PJC = 64, PJK = 32, PJP = PJK + 4, PJR = 128;
 
-template <int RI>
-__device__ void p2k_tile(const float *__restrict__ X, int ld, uint32_t N, const uint32_t *s_u, const uint8_t *s_unew,
+template <int RI, class R>
+__device__ void p2k_tile(const R &rows, int ld, uint32_t N, const uint32_t *s_u, const uint8_t *s_unew,
                          int nu, const uint32_t *s_w, const uint8_t *s_wnew, int nw, const float *__restrict__ radius,
                          uint64_t *__restrict__ cand, uint32_t *__restrict__ cand_cnt, uint32_t CB, float *s_As,
                          float *s_Bs, float *s_D, unsigned long long *s_cc) {
@@ -860,13 +813,13 @@ __device__ void p2k_tile(const float *__restrict__ X, int ld, uint32_t N, const 
         for (int idx = tid; idx < 32 * RI * (PJK / 4); idx += PJT) {
             int r = idx >> 3, c = (idx & 7) * 4;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r < nu && k0 + c < ld) v = __ldg(reinterpret_cast<const float4 *>(X + (uint64_t)s_u[r] * ld + k0 + c));
+            if (r < nu && k0 + c < ld) v = rows.ld4(s_u[r], (k0 + c) >> 2);
             *reinterpret_cast<float4 *>(s_As + r * PJP + c) = v;
         }
         for (int idx = tid; idx < PJC * (PJK / 4); idx += PJT) {
             int r = idx >> 3, c = (idx & 7) * 4;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r < nw && k0 + c < ld) v = __ldg(reinterpret_cast<const float4 *>(X + (uint64_t)s_w[r] * ld + k0 + c));
+            if (r < nw && k0 + c < ld) v = rows.ld4(s_w[r], (k0 + c) >> 2);
             *reinterpret_cast<float4 *>(s_Bs + r * PJP + c) = v;
         }
         __syncthreads();
@@ -938,8 +891,8 @@ constexpr size_t p2k_smem_bytes() {
 
 // RMAX = 32: nodes with at most 32 pushers (almost all), 22 KB of shared memory
 // so eight blocks fit per SM; RMAX = 128: the other nodes, in row tiles of 128.
-template <int RMAX>
-__global__ void __launch_bounds__(PJT) p2k_join_kernel(const float *__restrict__ X, int ld, uint32_t N,
+template <int RMAX, class R>
+__global__ void __launch_bounds__(PJT) p2k_join_kernel(R rows, int ld, uint32_t N,
                                                        const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ rnn,
                                                        const uint32_t *__restrict__ g_ids,
@@ -979,13 +932,13 @@ __global__ void __launch_bounds__(PJT) p2k_join_kernel(const float *__restrict__
             }
             __syncthreads();
             if (RMAX == 32 || nu <= 32)
-                p2k_tile<1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB, s_As, s_Bs, s_D,
+                p2k_tile<1>(rows, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB, s_As, s_Bs, s_D,
                             &s_cc);
             else if (nu <= 64)
-                p2k_tile<RMAX >= 64 ? 2 : 1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
+                p2k_tile<RMAX >= 64 ? 2 : 1>(rows, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
                                              s_As, s_Bs, s_D, &s_cc);
             else
-                p2k_tile<RMAX >= 128 ? 4 : 1>(X, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
+                p2k_tile<RMAX >= 128 ? 4 : 1>(rows, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB,
                                               s_As, s_Bs, s_D, &s_cc);
         }
     }
@@ -1020,6 +973,10 @@ kcna_status exclusive_scan(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t
 
 } // namespace
 
+kcna_status kcna_exclusive_scan_u32(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t *out, uint64_t *total_h) {
+    return exclusive_scan(c, in, n, out, total_h);
+}
+
 kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W) {
     const uint64_t N = c->n;
     if (c->W == W && c->g_ids) return KCNA_OK;
@@ -1043,28 +1000,17 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     KCNA_TRY(kcna_graph_alloc(c, std::max<uint32_t>(c->W, range + 8)));
     PruneRule rule = make_rule(p, kind);
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 16, 0, 8, c->stream), "memset"));
-    // kept rows in shared memory when a warp's share fits (ld <= ~256 at nsg_R 50)
-    const size_t ids_bytes = (size_t)range * 2 * 4;
-    const size_t rows_bytes = (size_t)range * (c->ld + 4) * 4;
-    const bool staged = false; // two-phase prune with kept rows read from L2: occupancy wins over staging
-    const size_t per_warp = ((staged ? ids_bytes + rows_bytes : ids_bytes) + 15) & ~(size_t)15;
-    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
-    const size_t sm = per_warp * wpb;
+    const size_t sm = (size_t)PW * 2 * range * 4;
     const int maxc = (int)std::min(p->search_K, c->cap);
     KCNA_TRY(kcna_phase_begin(c));
-    if (staged) {
-        KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune2_kernel<true>,
-                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)std::max<size_t>(sm, 48 * 1024)),
-                                 "prune smem attr"));
-        prune2_kernel<true><<<kcna_div_up(c->n, wpb), wpb * 32, sm, c->stream>>>(
-            c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids, c->g_dist,
-            c->g_deg, c->W, c->counters + 16);
-    } else {
-        prune2_kernel<false><<<kcna_div_up(c->n, wpb), wpb * 32, sm, c->stream>>>(
-            c->X, (int)c->ld, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids, c->g_dist,
-            c->g_deg, c->W, c->counters + 16);
-    }
+    if (c->Xh)
+        prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+            RowsB16{c->Xh, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
+            c->g_dist, c->g_deg, c->W, c->counters + 16);
+    else
+        prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+            RowsF32{c->X, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
+            c->g_dist, c->g_deg, c->W, c->counters + 16);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_PRUNE));
@@ -1107,9 +1053,14 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     KCNA_LAUNCHED(c);
     PruneRule rule = make_rule(p, kind);
     cudaMemsetAsync(c->counters + 17, 0, 8, c->stream);
-    link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(c->X, (int)c->ld, (uint32_t)N, rule, (int)p->nsg_R,
-                                                         c->g_ids, c->g_dist, c->g_deg, W, off, rev,
-                                                         c->counters + 17, c->d_err);
+    if (c->Xh)
+        link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(RowsB16{c->Xh, (int)c->ld}, (uint32_t)N, rule,
+                                                             (int)p->nsg_R, c->g_ids, c->g_dist, c->g_deg, W, off, rev,
+                                                             c->counters + 17, c->d_err);
+    else
+        link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(RowsF32{c->X, (int)c->ld}, (uint32_t)N, rule,
+                                                             (int)p->nsg_R, c->g_ids, c->g_dist, c->g_deg, W, off, rev,
+                                                             c->counters + 17, c->d_err);
     KCNA_LAUNCHED(c);
     s = kcna_cuda_check(c, cudaGetLastError(), "link kernels");
     unsigned long long h = 0;
@@ -1325,7 +1276,13 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     if ((s = kcna_alloc(c, &off, (uint64_t)N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
     uint64_t total_comps = 0;
     const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
-    if ((s = kcna_cuda_check(c, cudaFuncSetAttribute(p2k_join_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((s = kcna_cuda_check(c, cudaFuncSetAttribute(p2k_join_kernel<128, RowsF32>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)p2k_smem_bytes<128>()),
+                             "p2k smem attr")) != KCNA_OK)
+        return cleanup(), s;
+    if ((s = kcna_cuda_check(c, cudaFuncSetAttribute(p2k_join_kernel<128, RowsB16>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)p2k_smem_bytes<128>()),
                              "p2k smem attr")) != KCNA_OK)
         return cleanup(), s;
@@ -1376,12 +1333,23 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             pushes, np_all, off, cursor, rnn, N);
         KCNA_LAUNCHED(c);
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
-        p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
-            c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
-            c->CB, c->counters + 21);
-        p2k_join_kernel<128><<<N, PJT, p2k_smem_bytes<128>(), c->stream>>>(
-            c->X, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
-            c->CB, c->counters + 21);
+        if (c->Xh) {
+            const RowsB16 rows{c->Xh, (int)c->ld};
+            p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
+                rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+                c->CB, c->counters + 21);
+            p2k_join_kernel<128><<<N, PJT, p2k_smem_bytes<128>(), c->stream>>>(
+                rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+                c->CB, c->counters + 21);
+        } else {
+            const RowsF32 rows{c->X, (int)c->ld};
+            p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
+                rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+                c->CB, c->counters + 21);
+            p2k_join_kernel<128><<<N, PJT, p2k_smem_bytes<128>(), c->stream>>>(
+                rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
+                c->CB, c->counters + 21);
+        }
         c->launches++;
         KCNA_LAUNCHED(c);
         unsigned long long h = 0;

@@ -23,6 +23,9 @@ struct kcna_ctx {
     // rows: n_total x ld floats, ld = d rounded up to 4, padding zero
     float *X = nullptr;
     uint32_t n_total = 0, n = 0, d = 0, ld = 0;
+    // BF16 copy of the rows (n_total x ld), present only during a BF16-mode build
+    // of data whose every value is exactly representable in BF16
+    uint16_t *Xh = nullptr;
 
     // candidate pools: n x cap keys (kcna_common.cuh), counts, filter radius
     uint32_t cap = 0;
@@ -124,7 +127,7 @@ kcna_status kcna_tc_gemm(cudaStream_t s, const void *A, int64_t lda, int a_fp32,
 // kcna_nnd.cu: NN-descent phases
 kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
-kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);
+kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);  // iter 0: init lists
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr);
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);
@@ -133,7 +136,12 @@ kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall);
 kcna_status kcna_pools_set_radius(kcna_ctx *c, uint32_t limit);
 kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *p, kcna_stats *st);
 
+// kcna_seed.cu: learned seeding
+kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st);
+kcna_status kcna_seed_finish(kcna_ctx *c, const kcna_params *p);
+
 // kcna_graph.cu: prune / link / entry point / connectivity / P2K / search
+kcna_status kcna_exclusive_scan_u32(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t *out, uint64_t *total_h);
 kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W);
 kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
 kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);

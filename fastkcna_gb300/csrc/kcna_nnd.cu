@@ -155,8 +155,8 @@ __device__ void take_reverse(const uint32_t *src, uint32_t cnt, uint32_t RB, uin
     __syncthreads();
 }
 
-template <int RI> // rows per thread = RI, tile rows = 32 * RI
-__device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
+template <int RI, class R> // rows per thread = RI, tile rows = 32 * RI
+__device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
                            float *s_As, float *s_Bs, float *s_D, const float *s_radA, int *s_any,
                            unsigned *s_emit) {
     constexpr int RA = 32 * RI;
@@ -176,8 +176,7 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
             for (int idx = tid; idx < RA * (JKC / 4); idx += JT) {
                 int r = idx >> 3, c = (idx & 7) * 4;
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (r < rows_needed && k0 + c < ld)
-                    v = __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)s_A[r] * ld + k0 + c));
+                if (r < rows_needed && k0 + c < ld) v = rows.ld4(s_A[r], (k0 + c) >> 2);
                 *reinterpret_cast<float4 *>(s_As + r * JKP + c) = v;
             }
             for (int idx = tid; idx < JCOLS * (JKC / 4); idx += JT) {
@@ -186,7 +185,7 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (col < ncol && k0 + c < ld) {
                     uint32_t id = col < na ? s_A[col] : s_B[col - na];
-                    v = __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)id * ld + k0 + c));
+                    v = rows.ld4(id, (k0 + c) >> 2);
                 }
                 *reinterpret_cast<float4 *>(s_Bs + r * JKP + c) = v;
             }
@@ -300,7 +299,8 @@ __device__ void join_tiles(const JoinArgs &a, uint32_t node, const uint32_t *s_A
     }
 }
 
-__global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a) {
+template <class R>
+__global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
     extern __shared__ __align__(16) unsigned char smem[];
     float *s_As = reinterpret_cast<float *>(smem);                // 128 x JKP
     float *s_Bs = s_As + 128 * JKP;                               // JCOLS x JKP
@@ -339,11 +339,11 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a) {
         s_emit = 0;
     }
     if (na <= 32)
-        join_tiles<1>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+        join_tiles<1>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
     else if (na <= 64)
-        join_tiles<2>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+        join_tiles<2>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
     else
-        join_tiles<4>(a, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+        join_tiles<4>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
     if (threadIdx.x == 0) {
         a.found[node] = s_any ? 1 : 0;
         if (s_emit) atomicAdd(a.counters + 6, (unsigned long long)s_emit);
@@ -863,12 +863,18 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     a.capB = c->fwd_old_cap + c->RB;
     a.err = c->d_err;
     size_t sm = join_smem_bytes(a.capA, a.capB);
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel<RowsF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)std::max<size_t>(sm, 48 * 1024)),
+                             "join smem attr"));
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel<RowsB16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "join smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    join_kernel<<<c->n, JT, sm, c->stream>>>(a);
+    if (c->Xh)
+        join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsB16{c->Xh, (int)c->ld});
+    else
+        join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsF32{c->X, (int)c->ld});
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "join_kernel"));
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_JOIN));
@@ -1029,14 +1035,26 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
     st->maxl = maxl;
     KCNA_TRY(kcna_nnd_alloc(c, &P, maxl));
     KCNA_TRY(kcna_controls_setup(c, &P, maxl));
-    KCNA_TRY(kcna_nnd_init(c, &P));
+    // join iterations count from 1 when the first lists come from an update step
+    int iter_base = 0;
+    if (P.learned_seed) {
+        KCNA_TRY(kcna_seed_learned(c, &P, st));
+        KCNA_TRY(kcna_seed_finish(c, &P));
+        KCNA_TRY(kcna_control_recall(c, P.K, &st->seed_recall));
+        kcna_log(c, &P, "learned seed: %.1f ms (training %.1f ms), loss %.3f -> %.3f, recall %.4f", st->seed_total_ms,
+                 st->seed_train_ms, st->seed_loss_first, st->seed_loss_last, st->seed_recall);
+        KCNA_TRY(kcna_nnd_sample(c, &P, 0));
+        iter_base = 1;
+    } else {
+        KCNA_TRY(kcna_nnd_init(c, &P));
+    }
     uint64_t comps_total = 0;
     st->stop_condition = 0;
     st->iterations = 0;
     for (uint32_t it = 0; it < P.iterations; ++it) {
         uint64_t comps = 0, overflow = 0, flagged = 0, merged = 0, inserted = 0;
         const double j0 = c->phase_ms[KCNA_PHASE_JOIN], m0 = c->phase_ms[KCNA_PHASE_MERGE];
-        KCNA_TRY(kcna_nnd_join(c, &P, (int)it, &comps));
+        KCNA_TRY(kcna_nnd_join(c, &P, (int)it + iter_base, &comps));
         KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged, &merged, &inserted));
         if (it < KCNA_MAX_ITERS) {
             st->iter_join_ms[it] = c->phase_ms[KCNA_PHASE_JOIN] - j0;

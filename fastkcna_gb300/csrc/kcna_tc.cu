@@ -6,6 +6,8 @@
 // instructions (M = 128, N = 64, K = 16), the accumulator lives in TMEM and is
 // read back with tcgen05.ld.  Used by the learned-seed encoder (forward and
 // backward products) and exported as kcna_gemm_bf16 for tests and callers.
+#include <algorithm>
+
 #include "kcna_internal.h"
 #include "kcna_tc.cuh"
 
@@ -42,8 +44,10 @@ __device__ void stage(uint8_t *tile, const Operand &o, int64_t r0, int nrows, in
     }
 }
 
+// gridDim.z > 1 splits K: slice z covers [z*kslice, (z+1)*kslice) and adds its
+// partial product into C with atomicAdd (C cleared by the caller).
 __global__ void __launch_bounds__(128) tc_gemm_kernel(Operand A, Operand B, float *__restrict__ C, int64_t ldc,
-                                                      int M, int N, int K, float beta, int *err) {
+                                                      int M, int N, int K, float beta, int64_t kslice, int *err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t s_tmem;
@@ -65,9 +69,10 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(Operand A, Operand B, floa
     const uint32_t idesc = idesc_bf16(TM, TN);
     uint32_t phase = 0;
     bool ok = true;
-    for (int64_t k0 = 0; k0 < K; k0 += TK) {
-        stage(sA, A, m0, TM, M, k0, K);
-        stage(sB, B, n0, TN, N, k0, K);
+    const int64_t kbeg = (int64_t)blockIdx.z * kslice, kend = min((int64_t)K, kbeg + kslice);
+    for (int64_t k0 = kbeg; k0 < kend; k0 += TK) {
+        stage(sA, A, m0, TM, M, k0, kend);
+        stage(sB, B, n0, TN, N, k0, kend);
         fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
@@ -75,7 +80,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(Operand A, Operand B, floa
 #pragma unroll
             for (int kk = 0; kk < TK / 16; ++kk)
                 mma_bf16(tmem, desc_sw128(base_s + kk * 32), desc_sw128(base_s + TM * 128 + kk * 32), idesc,
-                         (k0 > 0 || kk > 0) ? 1u : 0u);
+                         (k0 > kbeg || kk > 0) ? 1u : 0u);
             mma_commit(&mbar);
         }
         ok = mbar_wait(&mbar, phase) && ok; // the MMAs have read the tiles: they may be overwritten
@@ -93,7 +98,10 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(Operand A, Operand B, floa
                 const int64_t col = n0 + c0 + i;
                 if (col < N) {
                     float *dst = C + row * ldc + col;
-                    *dst = beta != 0.f ? v[i] + beta * *dst : v[i];
+                    if (gridDim.z > 1)
+                        atomicAdd(dst, v[i]);
+                    else
+                        *dst = beta != 0.f ? v[i] + beta * *dst : v[i];
                 }
             }
         }
@@ -123,7 +131,19 @@ kcna_status kcna_tc_gemm(cudaStream_t s, const void *A, int64_t lda, int a_fp32,
     }
     Operand a{A, lda, a_fp32, a_trans}, b{B, ldb, b_fp32, b_trans};
     dim3 grid((M + TM - 1) / TM, (N + TN - 1) / TN);
-    tc_gemm_kernel<<<grid, 128, TC_SMEM, s>>>(a, b, C, ldc, M, N, K, beta, err);
+    // long reductions (K much larger than the output tile count) are split over K
+    int64_t kslice = ((int64_t)K + TK - 1) / TK * TK;
+    const int64_t tiles = (int64_t)grid.x * grid.y;
+    if (tiles < 64 && K >= 1024) {
+        const int64_t splits = std::min<int64_t>((K + 511) / 512, std::max<int64_t>(1, 256 / tiles));
+        kslice = ((K + splits - 1) / splits + TK - 1) / TK * TK;
+        grid.z = (unsigned)((K + kslice - 1) / kslice);
+    }
+    if (grid.z > 1) {
+        if (beta != 0.f) return KCNA_E_ARG;
+        if (cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)M, s) != cudaSuccess) return KCNA_E_CUDA;
+    }
+    tc_gemm_kernel<<<grid, 128, TC_SMEM, s>>>(a, b, C, ldc, M, N, K, beta, kslice, err);
     return cudaGetLastError() == cudaSuccess ? KCNA_OK : KCNA_E_CUDA;
 }
 

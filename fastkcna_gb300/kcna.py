@@ -65,7 +65,10 @@ class Stats(C.Structure):
         ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
         ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
         ("iter_join_ms", C.c_double * MAX_ITERS), ("iter_merge_ms", C.c_double * MAX_ITERS),
-        ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS)]
+        ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
+        ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
+        ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
+        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("pad_", C.c_uint32)]
 
     def as_dict(self):
         it = self.iterations
@@ -85,7 +88,11 @@ class Stats(C.Structure):
                     join_rows=self.join_rows, cand_emitted=self.cand_emitted, cand_merged=self.cand_merged,
                     pool_entries_merged=self.pool_entries_merged, tree_attached=self.tree_attached,
                     iter_join_ms=list(self.iter_join_ms[:it]), iter_merge_ms=list(self.iter_merge_ms[:it]),
-                    iter_cand=list(self.iter_cand[:it]), iter_inserted=list(self.iter_inserted[:it]))
+                    iter_cand=list(self.iter_cand[:it]), iter_inserted=list(self.iter_inserted[:it]),
+                    seed_train_ms=self.seed_train_ms, seed_total_ms=self.seed_total_ms,
+                    seed_loss_first=self.seed_loss_first, seed_loss_last=self.seed_loss_last,
+                    seed_input_scale=self.seed_input_scale, seed_recall=self.seed_recall,
+                    seed_comps=self.seed_comps, bf16_rows=self.bf16_rows)
 
 
 _lib = None

@@ -139,6 +139,15 @@ typedef struct {
     double iter_merge_ms[KCNA_MAX_ITERS];  /* device time of each NN-descent merge */
     uint64_t iter_cand[KCNA_MAX_ITERS];    /* candidates merged in each NN-descent iteration */
     uint64_t iter_inserted[KCNA_MAX_ITERS]; /* of which inserted into pools */
+    /* learned seed (kcna_params.learned_seed = 1) */
+    double seed_train_ms;      /* subsample NN-descent + encoder training */
+    double seed_total_ms;      /* training + encoding + hashing + initial pools */
+    float seed_loss_first, seed_loss_last; /* triplet loss of the first and last training batch */
+    float seed_input_scale;    /* 1 / RMS of the rows, folded into the first layer */
+    float seed_recall;         /* control recall@K of the seeded pools, before the first join */
+    uint64_t seed_comps;       /* distance evaluations of the initial pools */
+    uint32_t bf16_rows;        /* 1: BF16 mode read an exact BF16 copy of the rows */
+    uint32_t pad_;
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;
@@ -251,6 +260,16 @@ kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n, uint32_t d
  * product primitive of the learned-seed encoder and the BF16 distance screen. */
 kcna_status kcna_gemm_bf16(const void *A, int64_t lda, int a_fp32, int a_trans, const void *B, int64_t ldb,
                            int b_fp32, int b_trans, float *C, int64_t ldc, int M, int N, int K, void *stream);
+
+/* One forward + backward pass of the learned-seed encoder, for gradient checks.
+ * No counterpart in the reference.  rows = 3B host rows of dimension d laid
+ * out as [anchors | positives | negatives]; W1 256 x d, b1 256, W2 64 x 256,
+ * b2 64 (host, FP32, row-major).  Outputs (host): the mean triplet loss and the
+ * gradients of every parameter.  The products run in BF16 on the tensor cores
+ * with FP32 accumulation, as in training. */
+kcna_status kcna_encoder_grads(kcna_ctx *ctx, const float *rows, uint32_t n_rows, uint32_t d, const float *W1,
+                               const float *b1, const float *W2, const float *b2, float margin, float *loss,
+                               float *dW1, float *db1, float *dW2, float *db2);
 
 /* Writes the graph in the NSG/efanna format written by SaveNsg
  * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */

@@ -52,6 +52,9 @@ class Stats(C.Structure):
         ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
         ("iter_join_ms", C.c_double * MAX_ITERS), ("iter_merge_ms", C.c_double * MAX_ITERS),
         ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
+        ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
+        ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
+        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("pad_", C.c_uint32),
     ]
 
 

@@ -50,6 +50,17 @@ def test_gemm_integer_data_exact():
     assert torch.equal(got, ref)
 
 
+def test_gemm_split_k_long_reduction():
+    import torch
+
+    g = torch.Generator(device="cpu").manual_seed(9)
+    At = torch.randn(6144, 64, generator=g).cuda()   # stored K x M (fp32), the weight-gradient shape
+    Bt = torch.randn(6144, 256, generator=g).cuda()  # stored K x N
+    ref = At.to(torch.bfloat16).double().T @ Bt.to(torch.bfloat16).double()
+    got = gemm(At, Bt, a_trans=True, b_trans=True, M=64, N=256, K=6144)
+    torch.testing.assert_close(got.double(), ref, rtol=1e-3, atol=1e-2)
+
+
 def test_gemm_transposed_operands():
     import torch
 
