@@ -15,7 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libkcna.so")
-SOURCES = ["kcna_api.cu", "kcna_knn.cu", "kcna_nnd.cu", "kcna_graph.cu", "kcna_noalloc.cu", "kcna_tc.cu", "kcna_seed.cu"]
+SOURCES = ["kcna_api.cu", "kcna_knn.cu", "kcna_nnd.cu", "kcna_join_tc.cu", "kcna_graph.cu", "kcna_noalloc.cu",
+           "kcna_tc.cu", "kcna_seed.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -68,7 +69,50 @@ def build(verbose: bool = False, ptxas_v: bool = False) -> str:
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link of libkcna.so failed")
+    build_host(verbose)
     return LIB
+
+
+HOST = os.path.join(HERE, "host")
+FACADE = os.path.join(HERE, "libkgraph_gb300.so")
+BIN = os.path.join(HERE, "bin")
+TOOLS = {"fastnsg": 1, "fasttaumng": 2, "fastalphapg": 3, "fasthnsw": 4, "fastnsw": 5}
+
+
+def build_host(verbose: bool = False) -> None:
+    """The C++ kgraph::KGraph facade (libkgraph_gb300.so) and the five command
+    lines (bin/fast*), linked against libkcna.so."""
+    cxx = os.environ.get("CXX", "g++")
+    inc = ["-I", os.path.join(ROOT, "include")]
+    common = [cxx, "-O2", "-std=c++17", "-Wall", "-Wno-unused-result", *inc]
+    facade_src = os.path.join(HOST, "kgraph_facade.cpp")
+    cli_src = os.path.join(HOST, "fastkcna_cli.cpp")
+    headers = [os.path.join(ROOT, "include", h) for h in ("kcna.h", "kgraph_gb300.h", "kgraph_gb300_data.h")]
+
+    def stale(out, srcs):
+        return not os.path.exists(out) or any(os.path.getmtime(x) > os.path.getmtime(out) for x in srcs)
+
+    if stale(FACADE, [facade_src, LIB, *headers]):
+        cmd = common + ["-fPIC", "-shared", facade_src, "-o", FACADE, "-L", HERE, "-lkcna",
+                        "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed on kgraph_facade.cpp")
+    os.makedirs(BIN, exist_ok=True)
+    jobs = []
+    for tool, k in TOOLS.items():
+        out = os.path.join(BIN, tool)
+        if stale(out, [cli_src, FACADE, *headers]):
+            jobs.append((tool, common + [f"-DKCNA_CLI={k}", cli_src, "-o", out, "-L", HERE, "-lkgraph_gb300",
+                                         "-lkcna", "-Wl,-rpath,$ORIGIN/.."]))
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for tool, r in ex.map(lambda j: (j[0], subprocess.run(j[1], capture_output=True, text=True)), jobs):
+            if verbose or r.returncode != 0:
+                sys.stderr.write(r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError(f"g++ failed on {tool}")
 
 
 if __name__ == "__main__":

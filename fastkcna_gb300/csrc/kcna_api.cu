@@ -170,18 +170,50 @@ __global__ void bf16_copy_kernel(const uint32_t *__restrict__ x, uint64_t n, uin
     if (t < n) out[t] = (uint16_t)(x[t] >> 16);
 }
 
-// BF16 mode: when every value of the rows is exactly representable in BF16,
-// kernels read a BF16 copy (same floats, half the bytes).  Returns whether the
-// copy is in use.
-static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *used) {
-    *used = 0;
-    if (c->Xh) {
-        cudaFree(c->Xh);
-        c->Xh = nullptr;
+// Gram-exact check: every value an integer (BF16 exactness is checked
+// before), squared norms |x|^2 into norms[] (exact for integer rows) and the
+// largest one.  Warp per row.
+__global__ void gram_check_kernel(const float *__restrict__ X, uint32_t n, uint32_t ld, float *__restrict__ norms,
+                                  unsigned long long *nonint, unsigned *max_bits) {
+    const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    float acc = 0.f;
+    bool bad = false;
+    for (uint32_t k = lane; k < ld; k += 32) {
+        const float x = X[row * ld + k];
+        bad |= x != rintf(x);
+        acc = fmaf(x, x, acc);
     }
+    acc = kcna_warp_sum(acc);
+    bad = __any_sync(KCNA_FULL, bad);
+    if (lane == 0) {
+        norms[row] = acc;
+        if (bad) atomicAdd(nonint, 1ull);
+        atomicMax(max_bits, __float_as_uint(acc));
+    }
+}
+
+static void release_row_copies(kcna_ctx *c) {
+    if (c->Xh) cudaFree(c->Xh);
+    if (c->norms) cudaFree(c->norms);
+    c->Xh = nullptr;
+    c->norms = nullptr;
+    c->gram_exact = false;
+}
+
+// BF16 mode: when every value of the rows is exactly representable in BF16,
+// kernels read a BF16 copy (same floats, half the bytes).  When the rows are
+// moreover integers with squared norms below 2^23 (and d <= 128, a multiple of
+// 8), the local join runs on tensor-core Gram tiles whose distances are exact.
+// Returns whether the copy is in use and whether the Gram tiles are.
+static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *used, uint32_t *gram = nullptr) {
+    *used = 0;
+    if (gram) *gram = 0;
+    release_row_copies(c);
     if (!p || p->screen != KCNA_SCREEN_BF16) return KCNA_OK;
     const uint64_t n = (uint64_t)c->n_total * c->ld;
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 40, 0, 8, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 40, 0, 3 * 8, c->stream), "memset"));
     bf16_inexact_kernel<<<std::max(1, c->num_sms) * 8, 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n,
                                                                              c->counters + 40);
     KCNA_LAUNCHED(c);
@@ -192,8 +224,29 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     KCNA_TRY(kcna_alloc(c, &c->Xh, n, "bf16 rows"));
     bf16_copy_kernel<<<kcna_div_up(n, 256), 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n, c->Xh);
     KCNA_LAUNCHED(c);
+    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "bf16 copy"));
     *used = 1;
-    return kcna_cuda_check(c, cudaGetLastError(), "bf16 copy");
+    if ((c->ld & 7u) || c->ld > 128) return KCNA_OK;
+    KCNA_TRY(kcna_alloc(c, &c->norms, c->n_total, "row norms"));
+    unsigned *max_bits = reinterpret_cast<unsigned *>(c->counters + 42);
+    gram_check_kernel<<<kcna_div_up((uint64_t)c->n_total * 32, 256), 256, 0, c->stream>>>(c->X, c->n_total, c->ld,
+                                                                                          c->norms, c->counters + 41,
+                                                                                          max_bits);
+    KCNA_LAUNCHED(c);
+    unsigned long long h[2] = {};
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters + 41, 16, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "gram check"));
+    float maxn = 0.f;
+    const unsigned mb = (unsigned)(h[1] & 0xFFFFFFFFull);
+    memcpy(&maxn, &mb, 4);
+    if (h[0] == 0 && maxn < 8388608.f) { // 2^23: |x|^2 + |y|^2 stays below 2^24
+        c->gram_exact = true;
+        if (gram) *gram = 1;
+    } else {
+        cudaFree(c->norms);
+        c->norms = nullptr;
+    }
+    return KCNA_OK;
 }
 
 extern "C" {
@@ -255,7 +308,7 @@ void kcna_destroy(kcna_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_state(c);
     if (c->X) cudaFree(c->X);
-    if (c->Xh) cudaFree(c->Xh);
+    release_row_copies(c);
     if (c->scratch) cudaFree(c->scratch);
     if (c->scratch2) cudaFree(c->scratch2);
     if (c->d_err) cudaFree(c->d_err);
@@ -280,8 +333,7 @@ static kcna_status upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d
     free_state(c);
     if (c->X) cudaFree(c->X);
     c->X = nullptr;
-    if (c->Xh) cudaFree(c->Xh);
-    c->Xh = nullptr;
+    release_row_copies(c);
     c->d = d;
     c->ld = (d + 3) & ~3u;
     c->n_total = c->n = n;
@@ -386,7 +438,7 @@ kcna_status kcna_nndescent(kcna_ctx *c, const kcna_params *p, kcna_stats *st) {
     free_state(c);
     reset_phase_stats(c);
     c->t0 = kcna_now();
-    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows));
+    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows, &st->gram_tc));
     KCNA_TRY(kcna_nndescent_run(c, p, st));
     float r = 0;
     KCNA_TRY(kcna_control_recall(c, c->cap, &r));
@@ -430,7 +482,7 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
     reset_phase_stats(c);
     c->t0 = kcna_now();
     kcna_params P = *p;
-    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows));
+    KCNA_TRY(prepare_rows(c, p, &st->bf16_rows, &st->gram_tc));
     KCNA_TRY(kcna_nndescent_run(c, &P, st));
     const uint32_t maxl = c->cap;
     if (c->n <= P.K) P.loop_i = 0; // clamping of src/kgraph.cpp:1320-1327

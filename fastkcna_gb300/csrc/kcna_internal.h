@@ -26,6 +26,12 @@ struct kcna_ctx {
     // BF16 copy of the rows (n_total x ld), present only during a BF16-mode build
     // of data whose every value is exactly representable in BF16
     uint16_t *Xh = nullptr;
+    // Gram-exact BF16 mode: the rows are integers and every squared norm is
+    // below 2^23, so |x|^2 + |y|^2 - 2<x,y> evaluated by the tensor cores in
+    // FP32 equals the canonical FMA-chain distance bit for bit; the local join
+    // then runs on tcgen05 Gram tiles.  norms[i] = |x_i|^2 (n_total floats).
+    bool gram_exact = false;
+    float *norms = nullptr;
 
     // candidate pools: n x cap keys (kcna_common.cuh), counts, filter radius
     uint32_t cap = 0;

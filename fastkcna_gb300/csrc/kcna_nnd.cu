@@ -28,6 +28,7 @@
 #include <random>
 
 #include "kcna_internal.h"
+#include "kcna_join.cuh"
 #include "kcna_sort.cuh"
 
 namespace {
@@ -111,49 +112,6 @@ constexpr int JT = 256;      // threads per join block
 constexpr int JCOLS = 64;    // columns per tile chunk
 constexpr int JKC = 32;      // floats per k chunk
 constexpr int JKP = JKC + 4; // padded row pitch in shared memory
-
-struct JoinArgs {
-    const float *X;
-    int ld;
-    uint32_t N;
-    uint32_t iter;
-    uint64_t seed;
-    uint32_t R, RB;
-    const uint32_t *fwd_new, *fwd_new_cnt;
-    uint32_t fwd_new_cap;
-    const uint32_t *fwd_old, *fwd_old_cnt;
-    uint32_t fwd_old_cap;
-    const uint32_t *rnew, *rnew_cnt, *rold, *rold_cnt;
-    const float *radius;
-    uint64_t *cand;
-    uint32_t *cand_cnt;
-    uint32_t CB;
-    uint8_t *found;
-    unsigned long long *counters; // [0] pairs evaluated
-    uint32_t capA, capB;          // list capacities in shared memory (forward + RB)
-    int *err;
-};
-
-// copies up to R of cnt (capped at RB) reverse entries, a random subset when more
-__device__ void take_reverse(const uint32_t *src, uint32_t cnt, uint32_t RB, uint32_t R, uint64_t seed,
-                             uint64_t stream, uint32_t *dst, uint32_t *s_n) {
-    uint32_t m = min(cnt, RB);
-    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
-    if (m > R) {
-        if (threadIdx.x == 0) { // partial Fisher-Yates
-            for (uint32_t i = 0; i < R; ++i) {
-                uint32_t j = i + kcna_rand32(seed, stream, i) % (m - i);
-                uint32_t t = dst[i];
-                dst[i] = dst[j];
-                dst[j] = t;
-            }
-        }
-        m = R;
-    }
-    if (threadIdx.x == 0) *s_n = m;
-    __syncthreads();
-}
 
 template <int RI, class R> // rows per thread = RI, tile rows = 32 * RI
 __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
@@ -322,10 +280,10 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
     uint32_t rn = 0, ro = 0;
     if (a.iter > 0) {
         take_reverse(a.rnew + (uint64_t)node * a.RB, a.rnew_cnt[node], a.RB, a.R, a.seed,
-                     ((uint64_t)a.iter << 40) ^ ((uint64_t)node << 1), s_A + fn, &s_tmp);
+                     join_reverse_stream(a.iter, node, 0), s_A + fn, &s_tmp);
         rn = s_tmp;
         take_reverse(a.rold + (uint64_t)node * a.RB, a.rold_cnt[node], a.RB, a.R, a.seed,
-                     ((uint64_t)a.iter << 40) ^ ((uint64_t)node << 1) ^ 1ull, s_B + fo, &s_tmp);
+                     join_reverse_stream(a.iter, node, 1), s_B + fo, &s_tmp);
         ro = s_tmp;
     }
     // at most 128 rows per tile; the forward list alone is <= S + R < 128 in practice
@@ -720,10 +678,16 @@ __global__ void sample_lists_kernel(uint64_t *__restrict__ pool, uint32_t cap, u
         if (valid && id < N && dd > radiusM[id]) {
             if (isnew) {
                 uint32_t p = atomicAdd(rnew_cnt + id, 1u);
-                if (p < RB) rnew[(uint64_t)id * RB + p] = n;
+                if (p < RB)
+                    rnew[(uint64_t)id * RB + p] = n;
+                else
+                    atomicAdd(counters + 12, 1ull); // dropped: which ones depends on timing
             } else {
                 uint32_t p = atomicAdd(rold_cnt + id, 1u);
-                if (p < RB) rold[(uint64_t)id * RB + p] = n;
+                if (p < RB)
+                    rold[(uint64_t)id * RB + p] = n;
+                else
+                    atomicAdd(counters + 12, 1ull);
             }
         }
         cn += __popc(mn);
@@ -781,7 +745,9 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     c->cap = maxl;
     c->S = p->S;
     c->Rr = p->R;
-    c->RB = std::max<uint32_t>(2 * p->R, 32);
+    // reverse-list buffer: 2R entries (at most 4 per join thread, 1024)
+    const char *rb = getenv("KCNA_REV_CAP");
+    c->RB = std::min<uint32_t>(std::max<uint32_t>(rb ? (uint32_t)atoi(rb) : 2 * p->R, std::max<uint32_t>(p->R, 32)), 1024);
     const char *cb = getenv("KCNA_CAND_CAP");
     uint32_t CB = cb ? (uint32_t)atoi(cb) : 4 * std::max<uint32_t>(p->L, 64);
     CB = std::min<uint32_t>(std::max<uint32_t>(CB, 64), 8192);
@@ -871,12 +837,16 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
                              "join smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    if (c->Xh)
-        join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsB16{c->Xh, (int)c->ld});
-    else
-        join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsF32{c->X, (int)c->ld});
-    KCNA_LAUNCHED(c);
-    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "join_kernel"));
+    if (c->gram_exact) {
+        KCNA_TRY(kcna_join_tc_launch(c, a));
+    } else {
+        if (c->Xh)
+            join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsB16{c->Xh, (int)c->ld});
+        else
+            join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsF32{c->X, (int)c->ld});
+        KCNA_LAUNCHED(c);
+        KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "join_kernel"));
+    }
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_JOIN));
     unsigned long long h[8] = {};
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 8 * 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
@@ -1088,5 +1058,11 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
         KCNA_TRY(kcna_nnd_sample(c, &P, (int)it));
     }
     st->n_comps = comps_total;
+    st->screened_pairs = c->gram_exact ? comps_total : 0; // Gram tiles, exact: nothing to rescore
+    st->rescored_pairs = 0;
+    unsigned long long rev_drop = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&rev_drop, c->counters + 12, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));
+    st->rev_overflow = (uint32_t)std::min<unsigned long long>(rev_drop, 0xFFFFFFFFull);
     return KCNA_OK;
 }

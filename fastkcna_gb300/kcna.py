@@ -60,7 +60,7 @@ class Stats(C.Structure):
         ("n_comps", C.c_uint64), ("prune_comps", C.c_uint64), ("bridge_comps", C.c_uint64),
         ("screened_pairs", C.c_uint64), ("rescored_pairs", C.c_uint64),
         ("ep", C.c_uint32), ("width", C.c_uint32), ("aod", C.c_uint32),
-        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
+        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("rev_overflow", C.c_uint32), ("reserved", C.c_uint32 * 2),
         ("phase_ms", C.c_double * NUM_PHASES), ("phase_launches", C.c_uint64 * NUM_PHASES),
         ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
         ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
@@ -68,7 +68,7 @@ class Stats(C.Structure):
         ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
         ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
         ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
-        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("pad_", C.c_uint32)]
+        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32)]
 
     def as_dict(self):
         it = self.iterations
@@ -82,7 +82,7 @@ class Stats(C.Structure):
                     total_time=self.total_time, n_comps=self.n_comps, prune_comps=self.prune_comps,
                     bridge_comps=self.bridge_comps, screened_pairs=self.screened_pairs,
                     rescored_pairs=self.rescored_pairs, ep=self.ep, width=self.width, aod=self.aod,
-                    min_degree=self.min_degree, max_degree=self.max_degree,
+                    min_degree=self.min_degree, max_degree=self.max_degree, rev_overflow=self.rev_overflow,
                     phase_ms={PHASES[i]: self.phase_ms[i] for i in range(NUM_PHASES)},
                     phase_launches={PHASES[i]: int(self.phase_launches[i]) for i in range(NUM_PHASES)},
                     join_rows=self.join_rows, cand_emitted=self.cand_emitted, cand_merged=self.cand_merged,
@@ -92,7 +92,7 @@ class Stats(C.Structure):
                     seed_train_ms=self.seed_train_ms, seed_total_ms=self.seed_total_ms,
                     seed_loss_first=self.seed_loss_first, seed_loss_last=self.seed_loss_last,
                     seed_input_scale=self.seed_input_scale, seed_recall=self.seed_recall,
-                    seed_comps=self.seed_comps, bf16_rows=self.bf16_rows)
+                    seed_comps=self.seed_comps, bf16_rows=self.bf16_rows, gram_tc=self.gram_tc)
 
 
 _lib = None

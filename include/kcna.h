@@ -124,7 +124,8 @@ typedef struct {
     uint32_t width;            /* max out-degree */
     uint32_t aod;              /* average out-degree (CalculateNSG, :2273-2293) */
     uint32_t min_degree, max_degree;
-    uint32_t reserved[3];
+    uint32_t rev_overflow;     /* reverse-list entries dropped because a list was full (RB) */
+    uint32_t reserved[2];
     /* Device time per phase, measured with CUDA events on the context stream
      * (milliseconds, summed over the build), and kernel launches per phase.
      * Phases: see KCNA_PHASE_* below. */
@@ -147,7 +148,8 @@ typedef struct {
     float seed_recall;         /* control recall@K of the seeded pools, before the first join */
     uint64_t seed_comps;       /* distance evaluations of the initial pools */
     uint32_t bf16_rows;        /* 1: BF16 mode read an exact BF16 copy of the rows */
-    uint32_t pad_;
+    uint32_t gram_tc;          /* 1: the local join ran on tensor-core Gram tiles (integer rows,
+                                  squared norms < 2^23, d <= 128 and a multiple of 8) */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;

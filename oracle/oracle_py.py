@@ -46,7 +46,7 @@ class Stats(C.Structure):
         ("n_comps", C.c_uint64), ("prune_comps", C.c_uint64), ("bridge_comps", C.c_uint64),
         ("screened_pairs", C.c_uint64), ("rescored_pairs", C.c_uint64),
         ("ep", C.c_uint32), ("width", C.c_uint32), ("aod", C.c_uint32),
-        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("reserved", C.c_uint32 * 3),
+        ("min_degree", C.c_uint32), ("max_degree", C.c_uint32), ("rev_overflow", C.c_uint32), ("reserved", C.c_uint32 * 2),
         ("phase_ms", C.c_double * 12), ("phase_launches", C.c_uint64 * 12),
         ("join_rows", C.c_uint64), ("cand_emitted", C.c_uint64), ("cand_merged", C.c_uint64),
         ("pool_entries_merged", C.c_uint64), ("tree_attached", C.c_uint64),
@@ -54,7 +54,7 @@ class Stats(C.Structure):
         ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
         ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
         ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
-        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("pad_", C.c_uint32),
+        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32),
     ]
 
 
@@ -280,6 +280,24 @@ class Reference(_Lib):
                                C.c_uint32(g_ids.shape[1]), _ptr(Q), C.c_uint64(d), C.c_uint32(m), _ptr(init_ids),
                                C.c_uint32(L), C.c_uint32(k), _ptr(oi), _ptr(od))
         return oi, od
+
+    def getlevel(self, n, M, seed, max_levels=64):
+        """hnsw_dataload's level assignment: (data2file, points_num)."""
+        d2f = np.empty(n, np.int32)
+        pn = np.empty(max_levels, np.int32)
+        nl = C.c_uint32(0)
+        rc = self.fn("getlevel")(C.c_uint32(n), C.c_uint32(M), C.c_uint32(seed), _ptr(d2f), _ptr(pn),
+                                 C.c_uint32(max_levels), C.byref(nl))
+        assert rc == 0, rc
+        return d2f, pn[: nl.value].copy()
+
+    def build_hnsw(self, X, p, path, single_level=False, nthreads=8, quiet=True):
+        """Layered HNSW build (fasthnsw / fastnsw orchestration) into an hnswlib file."""
+        X = _f32(X)
+        n, d = X.shape
+        rc = self.fn("build_hnsw")(_ptr(X), C.c_uint64(d), C.c_uint32(n), C.c_uint32(d), C.byref(p),
+                                   C.c_int(nthreads), C.c_int(int(single_level)), path.encode(), C.c_int(int(quiet)))
+        assert rc == 0, rc
 
     def build(self, kind, X, p, nthreads=8, quiet=True):
         """Runs buildFast* and returns (graph rows as lists, ep, width, csv text)."""

@@ -273,4 +273,102 @@ int kref_build(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d
     return 0;
 }
 
+// Level assignment of hnsw_dataload (Matrix::getlevel, src/kgraph-data.h:186-222):
+// data2file[n] (storage row -> file row) and points_num per level.
+int kref_getlevel(uint32_t n, uint32_t M, uint32_t seed, int *data2file, int *points_num, uint32_t max_levels,
+                  uint32_t *nlevels) {
+    Matrix<float> m;
+    std::vector<int> d2f, f2d, pn;
+    m.getlevel(n, d2f, f2d, pn, M, seed);
+    if (pn.size() > max_levels) return 1;
+    std::copy(d2f.begin(), d2f.end(), data2file);
+    std::copy(pn.begin(), pn.end(), points_num);
+    *nlevels = (uint32_t)pn.size();
+    return 0;
+}
+
+// Layered HNSW build through the reference's public API, orchestrated as its
+// fasthnsw tool does (src/fasthnsw.cpp:204-342): rows stored in level order,
+// one buildFastHNSW per level on the prefix of rows that reach it (nsg_R
+// doubled at level 0), FatherSwapHNSWLayer0, then the hnswlib file.  X is in
+// file order; single_level = 1 gives fastnsw (everything on level 0).
+int kref_build_hnsw(const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p, int nthreads,
+                    int single_level, const char *path, int quiet) {
+    std::streambuf *old = quiet ? std::cout.rdbuf(nullptr) : nullptr;
+    omp_set_num_threads(nthreads);
+    KGraph::IndexParams q = to_params(p);
+    Matrix<float> lv;
+    std::vector<int> labels, file2data, points_num;
+    lv.getlevel(n, labels, file2data, points_num, q.nsg_R, q.seed);
+    if (single_level) points_num.assign(1, (int)n);
+    Matrix<float> M;
+    M.resize(n, d);
+    M.zero();
+    for (uint32_t i = 0; i < n; ++i) std::memcpy(M[i], X + (uint64_t)labels[i] * stride, (size_t)d * 4);
+    std::vector<int> levels;
+    for (int l = (int)points_num.size() - 1; l >= 0; --l)
+        for (int j = 0; j < points_num[l]; ++j) levels.push_back(l);
+    const size_t maxM = q.nsg_R, maxM0 = 2 * (size_t)q.nsg_R, Mlinks = q.nsg_R;
+    const size_t links = maxM * 4 + 4, links0 = maxM0 * 4 + 4;
+    const size_t per = links0 + 4 * (size_t)d + 8, label_off = links0 + 4 * (size_t)d, data_off = links0;
+    std::vector<char *> ll(n, nullptr);
+    for (uint32_t i = 0; i < n && levels[i] > 0; ++i) ll[i] = (char *)calloc(links * levels[i] + 1, 1);
+    RefOracle O(M);
+    KGraph *kg = KGraph::create();
+    KGraph::IndexInfo info;
+    unsigned ep = 0, layer_ep = 0, size = 0;
+    char *level0 = nullptr;
+    for (int level = (int)points_num.size() - 1; level >= 0; --level) {
+        size += points_num[level];
+        O.set_size(size);
+        if (size == 1 && level > 0) {
+            std::memset(ll[0] + (size_t)(level - 1) * links, 0, 2);
+            if (level == (int)points_num.size() - 1) ep = 0;
+            continue;
+        }
+        if (level > 0) {
+            kg->buildFastHNSW(O, q, &info, "", "", level0, ll.data(), (unsigned)level, &layer_ep);
+        } else {
+            q.nsg_R *= 2;
+            kg->buildFastHNSW(O, q, &info, "", "", level0, ll.data(), 0, &layer_ep, per);
+            level0 = (char *)calloc((size_t)n * per, 1);
+            kg->FatherSwapHNSWLayer0(O, q, level0);
+        }
+        if (level == (int)points_num.size() - 1) ep = layer_ep;
+    }
+    delete kg;
+    for (uint32_t i = 0; i < n; ++i) {
+        const size_t label = (size_t)labels[i];
+        std::memcpy(level0 + (size_t)i * per + data_off, M[i], (size_t)d * 4);
+        std::memcpy(level0 + (size_t)i * per + label_off, &label, sizeof label);
+    }
+    std::ofstream out(path, std::ios::binary);
+    const size_t zero = 0, nn = n, efc = q.search_K;
+    const int maxlevel = levels.empty() ? 0 : levels[0];
+    const double mult = 1 / std::log(1.0 * Mlinks);
+    out.write((const char *)&zero, 8);
+    out.write((const char *)&nn, 8);
+    out.write((const char *)&nn, 8);
+    out.write((const char *)&per, 8);
+    out.write((const char *)&label_off, 8);
+    out.write((const char *)&data_off, 8);
+    out.write((const char *)&maxlevel, 4);
+    out.write((const char *)&ep, 4);
+    out.write((const char *)&maxM, 8);
+    out.write((const char *)&maxM0, 8);
+    out.write((const char *)&Mlinks, 8);
+    out.write((const char *)&mult, 8);
+    out.write((const char *)&efc, 8);
+    out.write(level0, (std::streamsize)((size_t)n * per));
+    for (uint32_t i = 0; i < n; ++i) {
+        const unsigned sz = levels[i] > 0 ? (unsigned)(links * levels[i]) : 0u;
+        out.write((const char *)&sz, 4);
+        if (sz) out.write(ll[i], sz);
+    }
+    free(level0);
+    for (char *x : ll) free(x);
+    if (quiet) std::cout.rdbuf(old);
+    return out ? 0 : 1;
+}
+
 } // extern "C"

@@ -1,0 +1,99 @@
+"""The C++ drop-in end to end on the GPU: the fast* command lines read an
+lshkit file, build through the kgraph::KGraph facade and write the index
+files.  Scored against the reference's own builds of the same data and flags
+(tests/golden/ref_cli_c1.npz, made by tests/golden/make_golden_cli.py with the
+reference compiled from its sources) by search recall@10 with the same host
+searcher and start nodes."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from fastkcna_gb300 import build as kbuild
+from fastkcna_gb300 import index_io, synth
+from graph_search import beam_search, hnsw_search, seeded_entries
+
+pytestmark = pytest.mark.gpu
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_cli_c1.npz"))
+TOL = 0.01  # recall@10 below the reference's by at most this much
+FLAGS = ["-K", "100", "-L", "100", "-S", "10", "-R", "100", "-I", "6", "--search_L", "40", "--nsg_R", "32",
+         "--search_K", "100", "--massq_S", "10", "--angle", "60", "--tau", "0.1"]
+
+
+def _run(tool, *args):
+    r = subprocess.run([os.path.join(kbuild.BIN, tool), *args], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    return r.stdout
+
+
+def _truth(X, Q, k=10):
+    d = ((Q[:, None, :].astype(np.float64) - X[None, :, :]) ** 2).sum(-1)
+    return np.argsort(d, axis=1, kind="stable")[:, :k]
+
+
+def _recall(found, truth):
+    return np.mean([len(set(f[:10].tolist()) & set(t[:10].tolist())) / 10 for f, t in zip(found, truth)])
+
+
+def _nsg_recall(path, X, Q, truth, ef=60):
+    rows, ep, width = index_io.read_nsg(path)
+    assert len(rows) == X.shape[0]
+    start = seeded_entries(X.shape[0], ep, ef)
+    found = [beam_search(X, rows, start, q, ef, 10) for q in Q]
+    return _recall(found, truth), rows, width
+
+
+@pytest.fixture(scope="module")
+def c1_files():
+    X = synth.base("c1", 20000)
+    Q = synth.queries("c1", 200)
+    td = tempfile.mkdtemp()
+    path = os.path.join(td, "c1.lshkit")
+    synth.write_lshkit(path, X)
+    return td, path, X, Q, _truth(X, Q)
+
+
+@pytest.mark.parametrize("tool", ["fastnsg", "fasttaumng", "fastalphapg"])
+def test_cli_nsg_family(c1_files, tool):
+    td, data, X, Q, truth = c1_files
+    out, res = os.path.join(td, tool + ".nsg"), os.path.join(td, tool + ".csv")
+    _run(tool, data, out, "--result", res, *FLAGS)
+    rec, rows, width = _nsg_recall(out, X, Q, truth)
+    assert max(len(r) for r in rows) == width
+    csv = open(res).read()
+    assert csv.startswith("PG_type,K,L,S,R,I,searchL,searchK,nsgR,massqS,tau,angle,step")
+    assert "con time" in csv and "AOD" in csv
+    assert rec >= float(GOLD[f"recall_{tool[4:]}"]) - TOL, (rec, float(GOLD[f"recall_{tool[4:]}"]))
+    assert rec >= 0.9
+
+
+@pytest.mark.parametrize("tool", ["fasthnsw", "fastnsw"])
+def test_cli_hnsw(c1_files, tool):
+    td, data, X, Q, truth = c1_files
+    out = os.path.join(td, tool + ".bin")
+    _run(tool, data, out, "--result", os.path.join(td, tool + ".csv"), *FLAGS)
+    idx = index_io.read_hnswlib(out)
+    n = X.shape[0]
+    assert idx["cur_element_count"] == n and idx["maxM"] == 32 and idx["maxM0"] == 64
+    assert np.array_equal(idx["data"], X[idx["labels"].astype(np.int64)])
+    assert max(len(a) for a in idx["level0"]) <= 64 and min(len(a) for a in idx["level0"]) >= 1
+    if tool == "fastnsw":
+        assert idx["maxlevel"] == 0 and not idx["upper"]
+    else:
+        assert idx["maxlevel"] >= 1 and idx["levels"][idx["enterpoint"]] == idx["maxlevel"]
+        for l, rows in idx["upper"].items():
+            top = int((idx["levels"] >= l).sum())
+            assert all(len(ids) <= 32 and (ids < top).all() for _, ids in rows)
+    found = hnsw_search(idx, Q, ef=60, k=10, extra_entries=59 if tool == "fastnsw" else 0)
+    rec = _recall(found, truth)
+    tag = tool[4:]
+    # same level assignment and storage order as the reference's hnsw_dataload
+    if tool == "fasthnsw":
+        d2f, pn = GOLD["levels_data2file"], GOLD["levels_points_num"]
+        assert np.array_equal(idx["labels"].astype(np.int64), d2f.astype(np.int64))
+        assert idx["maxlevel"] == len(pn) - 1 == int(GOLD["maxlevel_hnsw"])
+        assert np.array_equal(idx["levels"], np.repeat(np.arange(len(pn) - 1, -1, -1), pn[::-1]))
+    assert rec >= float(GOLD[f"recall_{tag}"]) - TOL, (rec, float(GOLD[f"recall_{tag}"]))
