@@ -61,10 +61,15 @@ __device__ void take_reverse(const uint32_t *src, uint32_t cnt, uint32_t RB, uin
             v[e] = i < m ? dst[i] : 0u;
             rk[e] = 0u;
         }
-        for (uint32_t j = 0; j < m; ++j) { // rank = position in (id, index) order
-            const uint32_t w = dst[j];
 #pragma unroll
-            for (int e = 0; e < PER; ++e) rk[e] += (w < v[e] || (w == v[e] && j < threadIdx.x + e * blockDim.x)) ? 1u : 0u;
+        for (int e = 0; e < PER; ++e) { // rank = position in (id, index) order
+            const uint32_t i = threadIdx.x + e * blockDim.x;
+            if (e * blockDim.x >= m) break;
+            if (i < m)
+                for (uint32_t j = 0; j < m; ++j) {
+                    const uint32_t w = dst[j];
+                    rk[e] += (w < v[e] || (w == v[e] && j < i)) ? 1u : 0u;
+                }
         }
         __syncthreads();
 #pragma unroll

@@ -320,6 +320,10 @@ kcna_status kcna_join_tc_launch(kcna_ctx *c, const JoinArgs &a) {
     const size_t sm = 1024 + TILES + (size_t)colcap * 12;
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                              "join_tc smem attr"));
+    // all of the unified L1 as shared memory, so that two blocks fit per SM
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                     (int)cudaSharedmemCarveoutMaxShared),
+                             "join_tc carveout"));
     int per_sm = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_tc_kernel, TJ, sm),
                              "join_tc occupancy"));
