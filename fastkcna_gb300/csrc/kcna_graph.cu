@@ -673,16 +673,6 @@ __global__ void mark_frontier_kernel(const uint32_t *__restrict__ f, uint32_t nf
     if (i < nf) atomicOr(visited + (f[i] >> 5), 1u << (f[i] & 31));
 }
 
-__global__ void degree_stats_kernel(const uint32_t *__restrict__ g_deg, uint32_t N, unsigned long long *out) {
-    // out[0] sum, out[1] max, out[2] min
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    uint32_t d = g_deg[i];
-    atomicAdd(out + 0, (unsigned long long)d);
-    atomicMax(out + 1, (unsigned long long)d);
-    atomicMin(out + 2, (unsigned long long)d);
-}
-
 // ---- UpdateNhoods ---------------------------------------------------------
 __global__ void update_nhoods_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg,
                                      uint32_t *__restrict__ g_old, uint32_t *__restrict__ g_old_deg,
@@ -796,7 +786,7 @@ __global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint6
 // accumulators.  Pair (u, w) is skipped when u == w or both are old
 // (src/kgraph.cpp:2639-2641); survivors within u's radius become candidates of
 // u, written as one run per (q, u) after one atomicAdd.
-constexpr int PJT = 256, PJC = 64, PJK = 32, PJP = PJK + 4, PJR = 128;
+constexpr int PJT = 256, PJC = 64, PJK = 32, PJP = PJK + 4;
 
 template <int RI, class R>
 __device__ void p2k_tile(const R &rows, int ld, uint32_t N, const uint32_t *s_u, const uint8_t *s_unew,
@@ -1333,7 +1323,9 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             pushes, np_all, off, cursor, rnn, N);
         KCNA_LAUNCHED(c);
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
-        if (c->Xh) {
+        if (c->gram_exact && c->W <= 256) {
+            if ((s = kcna_p2k_tc_launch(c, off, rnn, c->counters + 21)) != KCNA_OK) return cleanup(), s;
+        } else if (c->Xh) {
             const RowsB16 rows{c->Xh, (int)c->ld};
             p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
                 rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
@@ -1350,8 +1342,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
                 rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
                 c->CB, c->counters + 21);
         }
-        c->launches++;
-        KCNA_LAUNCHED(c);
+        if (!(c->gram_exact && c->W <= 256)) c->launches += 2; // the FP32 pair
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, c->counters + 21, 8, cudaMemcpyDeviceToHost, c->stream);
         if ((s = kcna_phase_end(c, KCNA_PHASE_P2K)) != KCNA_OK) return cleanup(), s;

@@ -11,23 +11,35 @@
 // tile distance is the canonical FMA-chain distance bit for bit and the join
 // emits exactly the candidates of the FP32 kernel.
 //
-// Block layout (persistent; one node at a time per block, 8 warps):
-//   set         A (na <= 128 new ids) followed by B (old ids), ncol entries.
-//   operands    M side: the set in tiles of 128 rows; N side: A (NA = na
-//               rounded up to 16 columns), staged once per node.  Every TMEM
-//               lane (a set member) then meets only real new-list columns, so
-//               the emission work is ncol x NA pair checks, not 128 x ncol.
-//   staging     cp.async 16-byte gathers of BF16 rows into the 128-byte
-//               swizzled K-major layout; tiles rotate through two slots, the
-//               slot of tile r+2 being gathered while tile r is emitted.
-//   MMA         one thread issues 4 (K=16) x 2 (64-element K blocks)
-//               tcgen05.mma (M = 128, N = NA) per tile into one of two
-//               128-column TMEM buffers and commits to that buffer's mbarrier.
-//   emission    warp w reads TMEM lanes 32*(w%4).. (set members) and column
-//               groups of 16 with parity w/4; a set member's candidates are
-//               counted per thread, a new member's by warp ballots; one
+// Block layout: persistent, one block per SM, warp-specialised; the roles
+// hand work to each other through mbarriers only, so no role waits for a
+// block-wide barrier:
+//   warp 0      producer: the bulk-copy engine brings node n+2's four lists
+//               into a raw ring while node n is handled; assembles node n's
+//               set (new list A, na <= 128, then the old list B; ncol entries)
+//               in a node slot, gathers A's BF16
+//               rows with cp.async into the slot, then the set in tiles of 128
+//               rows into a ring of row stages (freed as soon as the tile's
+//               products are done) and the radius/norm of each row into a
+//               deeper ring the epilogue frees; every gather lands as an
+//               mbarrier arrival.
+//   warp 1      MMA issuer (one thread): per tile, 4 (K=16) x 2 (64-element K
+//               blocks) tcgen05.mma with M = 128 set rows and N = NA = na
+//               rounded up to 16 new-list columns into one of four 128-column
+//               TMEM accumulators; commits release the row stage and mark the
+//               accumulator full.
+//   warps 2-9   epilogue: warp w reads TMEM lanes 32*(w%4).. (set members) and
+//               column groups of 16 of parity (w-2)/4; distance
+//               |x|^2 + |y|^2 - 2<x,y>, pair rule of the reference join
+//               (A x A with i < j, A x B); a set member's candidates are
+//               counted per thread, a new member's by warp ballots; an
 //               atomicAdd per target and tile reserves a contiguous run in the
-//               target's candidate buffer.
+//               target's candidate buffer (a row's run per column half, a
+//               column's run per lane quarter: no barrier between epilogue
+//               warps), the distances are read again from TMEM for the writes;
+//               the last warp to finish a node writes its found flag.
+// Every wait is bounded; a wait that gives up stops the block, sets the error
+// word and lets in-flight products finish before TMEM is released.
 #include <algorithm>
 
 #include "kcna_internal.h"
@@ -38,21 +50,53 @@ using namespace kcna_tc;
 
 namespace {
 
-constexpr int TJ = 256;                      // threads per block
-constexpr int TROWS = 128;                   // set rows per tile (MMA M), max new-list columns
-constexpr uint32_t KBB = 128;                // bytes of a row inside one 64-element K block
-constexpr uint32_t TILE = TROWS * KBB * 2;   // 128 rows, two K blocks (d <= 128): 32 KiB
-constexpr uint32_t TILES = 3 * TILE;         // new-list rows + two rotating set tiles
-constexpr uint32_t TMEM_COLS = 2 * TROWS;    // two accumulator buffers
-constexpr int MAXG = TROWS / 16 / 2;         // column groups of 16 per warp half
+constexpr int EPI_WARPS = 16;                 // epilogue warps: 4 per TMEM lane quarter
+constexpr int WS_WARPS = 2 + EPI_WARPS;       // producer, MMA, epilogue
+constexpr int WS_THREADS = WS_WARPS * 32;
+constexpr int TROWS = 128;                    // set rows per tile (MMA M), max new-list columns
+constexpr uint32_t KBB = 128;                 // bytes of a row inside one 64-element K block
+constexpr uint32_t TILE = TROWS * KBB * 2;    // 128 rows, two K blocks (d <= 128): 32 KiB
+constexpr int NS = 2;                         // node slots
+constexpr int TS = 4;                         // tile row stages (released by the MMA)
+constexpr int MS = 8;                         // tile metadata entries (released by the epilogue)
+constexpr int NACC = 4;                       // TMEM accumulators of 128 columns
+constexpr int NR = 4;                         // raw list entries (prefetched two nodes ahead)
 
-// Gathers rows first..first+count-1 of the column list into rows 0..count-1 of
-// a 128-row region (K block kb of row r at kb*128*128 + swizzle).
-__device__ __forceinline__ void stage_rows(uint32_t region, const uint32_t *s_col, int first, int count,
-                                           const uint16_t *__restrict__ Xh, int ldh, int nc16) {
-    for (int idx = threadIdx.x; idx < count * nc16; idx += TJ) {
+// Layout of one raw list entry: the four lists of a node copied whole.
+struct RawLayout {
+    uint32_t o_rnew, o_old, o_rold, words; // offsets (in u32) after the forward-new list
+};
+__host__ __device__ inline RawLayout raw_layout(uint32_t fwd_new_cap, uint32_t rc, uint32_t fwd_old_cap) {
+    RawLayout r;
+    r.o_rnew = fwd_new_cap;
+    r.o_old = r.o_rnew + rc;
+    r.o_rold = r.o_old + fwd_old_cap;
+    r.words = r.o_rold + rc;
+    return r;
+}
+
+struct SlotMeta {
+    uint32_t node, na, NA, ncol;
+};
+
+// Shared-memory carve-up (after the 1024-aligned tiles: NS slots + TS stages)
+struct WsShared {
+    uint64_t node_full[NS], node_empty[NS], tile_full[TS], tile_empty[TS], meta_full[MS], meta_empty[MS];
+    uint64_t acc_full[NACC], acc_empty[NACC], ids_full[NR];
+    SlotMeta meta[NS];
+    uint32_t tmem;
+    volatile int abort_flag;
+    unsigned emit[NS], done[NS];
+    float a_rad[NS][TROWS], a_nrm[NS][TROWS];
+    float t_rad[MS][TROWS], t_nrm[MS][TROWS];
+};
+
+// rows [first, first+count) of ids -> rows 0..count-1 of a 128-row region; lane-strided
+__device__ __forceinline__ void gather_rows(uint32_t region, const uint32_t *ids, int first, int count,
+                                            const uint16_t *__restrict__ Xh, int ldh, int nc16, int lane) {
+    for (int idx = lane; idx < count * nc16; idx += 32) {
         const int r = idx / nc16, c = idx - r * nc16;
-        const uint16_t *src = Xh + (uint64_t)s_col[first + r] * (uint64_t)ldh + c * 8;
+        const uint16_t *src = Xh + (uint64_t)ids[first + r] * (uint64_t)ldh + c * 8;
         cp_async16(region + (uint32_t)(c >> 3) * TROWS * KBB + sw128_off((uint32_t)r, (uint32_t)(c & 7)), src);
     }
 }
@@ -67,270 +111,362 @@ __device__ __forceinline__ void issue_tile(uint32_t tmem_d, uint32_t a_base, uin
                      desc_sw128(b_base + kb * TROWS * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
 }
 
-__global__ void __launch_bounds__(TJ, 2) join_tc_kernel(JoinArgs a, const uint16_t *__restrict__ Xh, int ldh,
-                                                        const float *__restrict__ norms, uint32_t colcap) {
+__global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, const uint16_t *__restrict__ Xh, int ldh,
+                                                                const float *__restrict__ norms, uint32_t colcap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ uint64_t mbar[2];
-    __shared__ uint32_t s_tmem, s_tmp;
-    __shared__ unsigned s_emit;
-    __shared__ uint8_t s_rcnt[2][TROWS], s_ccnt[4][TROWS];
-    __shared__ uint32_t s_rbase[2][TROWS], s_cbase[4][TROWS];
     const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u; // swizzled tiles need 1024-byte alignment
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
-    uint32_t *s_col = reinterpret_cast<uint32_t *>(tiles + TILES); // set ids: A then B
-    float *s_rad = reinterpret_cast<float *>(s_col + colcap);      // radius of each set id
-    float *s_nrm = s_rad + colcap;                                 // squared norm of each set id
-    const uint32_t tA = tiles_s, tS = tiles_s + TILE;
+    WsShared &S = *reinterpret_cast<WsShared *>(tiles + (NS + TS) * TILE);
+    uint32_t *set_ids = reinterpret_cast<uint32_t *>(&S + 1); // NS x colcap
+    // raw list ring: NR entries, 16-byte aligned
+    const uint32_t rc = (min(a.R, a.RB) + 3) & ~3u;
+    const RawLayout RL = raw_layout(a.fwd_new_cap, rc, a.fwd_old_cap);
+    uint32_t *raw_ring = reinterpret_cast<uint32_t *>(
+        (reinterpret_cast<uintptr_t>(set_ids + (size_t)NS * colcap) + 15) & ~(uintptr_t)15);
+    const uint32_t slotA = tiles_s, stage0 = tiles_s + NS * TILE;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int q = warp & 3, h = warp >> 2; // TMEM lane quarter, column-group parity
     const int nc16 = ldh >> 3, nkb = (ldh + 63) >> 6;
 
     // K padding beyond ldh is never written by the gathers and must read as zero
-    for (int i = tid; i < (int)(TILES / 16); i += TJ) reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
-    if (warp == 0) tmem_alloc(&s_tmem, TMEM_COLS);
+    for (int i = tid; i < (int)((NS + TS) * TILE / 16); i += WS_THREADS)
+        reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 1) tmem_alloc(&S.tmem, NACC * TROWS);
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int i = 0; i < NS; ++i) {
+            mbar_init(&S.node_full[i], 33);  // 32 producer lanes' copies + the producer's metadata
+            mbar_init(&S.node_empty[i], EPI_WARPS);
+            S.emit[i] = 0;
+            S.done[i] = 0;
+        }
+        for (int i = 0; i < TS; ++i) {
+            mbar_init(&S.tile_full[i], 32);  // producer lanes' copies
+            mbar_init(&S.tile_empty[i], 1);  // MMA commit
+        }
+        for (int i = 0; i < MS; ++i) {
+            mbar_init(&S.meta_full[i], 32);  // producer lanes' copies
+            mbar_init(&S.meta_empty[i], EPI_WARPS);
+        }
+        for (int i = 0; i < NR; ++i) mbar_init(&S.ids_full[i], 1); // producer's expect_tx + bulk copies
+        for (int i = 0; i < NACC; ++i) {
+            mbar_init(&S.acc_full[i], 1);    // MMA commit
+            mbar_init(&S.acc_empty[i], EPI_WARPS);
+        }
+        S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_emit = 0;
     }
     fence_proxy_async();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = s_tmem;
-    uint32_t phase = 0u; // bit b: parity of the next completion of buffer b's mbarrier
-    uint32_t pend = 0u;  // bit b: buffer b has a commit not yet waited for
+    const uint32_t tmem = S.tmem;
     bool ok = true;
-    unsigned long long pairs = 0, rows_g = 0, emitted = 0;
 
-    for (uint32_t node = blockIdx.x; node < a.N && ok; node += gridDim.x) {
-        // new list: forward new, then a random subset (<= R) of reverse new
-        const uint32_t fn = min(a.fwd_new_cnt[node], a.fwd_new_cap);
-        for (uint32_t i = tid; i < fn; i += TJ) s_col[i] = a.fwd_new[(uint64_t)node * a.fwd_new_cap + i];
-        __syncthreads();
-        uint32_t rn = 0;
-        if (a.iter > 0) {
-            take_reverse(a.rnew + (uint64_t)node * a.RB, a.rnew_cnt[node], a.RB, a.R, a.seed,
-                         join_reverse_stream(a.iter, node, 0), s_col + fn, &s_tmp);
-            rn = s_tmp;
-        }
-        const int na = (int)min(fn + rn, (uint32_t)TROWS);
-        // old list after A: forward old, then a random subset of reverse old
-        const uint32_t fo = min(a.fwd_old_cnt[node], a.fwd_old_cap);
-        for (uint32_t i = tid; i < fo; i += TJ) s_col[na + i] = a.fwd_old[(uint64_t)node * a.fwd_old_cap + i];
-        __syncthreads();
-        uint32_t ro = 0;
-        if (a.iter > 0) {
-            take_reverse(a.rold + (uint64_t)node * a.RB, a.rold_cnt[node], a.RB, a.R, a.seed,
-                         join_reverse_stream(a.iter, node, 1), s_col + na + fo, &s_tmp);
-            ro = s_tmp;
-        }
-        const int nb = (int)(fo + ro), ncol = na + nb;
-        if (na == 0) {
-            __syncthreads();
-            continue;
-        }
-        for (int j = tid; j < ncol; j += TJ) {
-            const uint32_t id = s_col[j];
-            s_rad[j] = __ldg(a.radius + id);
-            s_nrm[j] = __ldg(norms + id);
-        }
-        if (tid == 0) {
-            pairs += (unsigned long long)na * (na - 1) / 2 + (unsigned long long)na * nb;
-            rows_g += (unsigned long long)ncol;
-        }
-        const int NA = (na + 15) & ~15, G = NA >> 4; // MMA N and its column groups
-        const uint32_t idesc = idesc_bf16(TROWS, NA);
-        const int ntile = (ncol + TROWS - 1) / TROWS;
-        stage_rows(tA, s_col, 0, na, Xh, ldh, nc16);
-        stage_rows(tS, s_col, 0, min(ncol, TROWS), Xh, ldh, nc16);
-        if (ntile > 1) stage_rows(tS + TILE, s_col, TROWS, min(ncol - TROWS, TROWS), Xh, ldh, nc16);
-        cp_async_wait_all();
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            issue_tile(tmem, tS, tA, idesc, nkb);
-            mma_commit(&mbar[0]);
-            if (ntile > 1) {
-                issue_tile(tmem + TROWS, tS + TILE, tA, idesc, nkb);
-                mma_commit(&mbar[1]);
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer
+        unsigned long long pairs = 0, rows_g = 0;
+        uint32_t tcount = 0;
+        // the four lists of node number kk (grid-stride) copied whole by the
+        // bulk-copy engine into raw entry kk % NR; lane 0 issues
+        auto prefetch = [&](int kk) {
+            const uint32_t nd = blockIdx.x + (uint32_t)kk * gridDim.x;
+            if (nd >= a.N || lane != 0) return;
+            uint32_t *r = raw_ring + (size_t)(kk % NR) * RL.words;
+            uint64_t *bar = &S.ids_full[kk % NR];
+            const uint32_t bytes = RL.words * 4 - (a.iter > 0 ? 0u : 2u * rc * 4);
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_copy_g2s(smem_u32(r), a.fwd_new + (uint64_t)nd * a.fwd_new_cap, a.fwd_new_cap * 4, bar);
+            bulk_copy_g2s(smem_u32(r + RL.o_old), a.fwd_old + (uint64_t)nd * a.fwd_old_cap, a.fwd_old_cap * 4, bar);
+            if (a.iter > 0) {
+                bulk_copy_g2s(smem_u32(r + RL.o_rnew), a.rnew + (uint64_t)nd * a.RB, rc * 4, bar);
+                bulk_copy_g2s(smem_u32(r + RL.o_rold), a.rold + (uint64_t)nd * a.RB, rc * 4, bar);
             }
-        }
-        pend = ntile > 1 ? 3u : 1u;
-        for (int r = 0; r < ntile; ++r) {
-            const int b = r & 1;
-            if (mbar_wait(&mbar[b], (phase >> b) & 1u)) {
-                phase ^= 1u << b;
-                pend &= ~(1u << b);
-            } else {
-                ok = false;
+        };
+        // list lengths, loaded two nodes ahead into registers
+        uint32_t c_fn[3] = {0, 0, 0}, c_rn[3] = {0, 0, 0}, c_fo[3] = {0, 0, 0}, c_ro[3] = {0, 0, 0};
+        auto load_counts = [&](int kk, int slot) { // raw values; clamped where used
+            const uint32_t nd = blockIdx.x + (uint32_t)kk * gridDim.x;
+            if (nd >= a.N) return;
+            c_fn[slot] = a.fwd_new_cnt[nd];
+            c_fo[slot] = a.fwd_old_cnt[nd];
+            if (a.iter > 0) {
+                c_rn[slot] = a.rnew_cnt[nd];
+                c_ro[slot] = a.rold_cnt[nd];
             }
-            fence_after();
-            // tile r+2 goes to slot b, free now that tile r's products are done
-            if (r + 2 < ntile) {
-                const int first = (r + 2) * TROWS;
-                stage_rows(tS + b * TILE, s_col, first, min(ncol - first, TROWS), Xh, ldh, nc16);
-            }
-            const int j = r * TROWS + 32 * q + lane; // this thread's set member
-            const bool warp_live = r * TROWS + 32 * q < ncol;
-            const bool rowv = j < ncol;
-            const uint32_t id_j = rowv ? s_col[j] : 0u;
-            const float rad_j = rowv ? s_rad[j] : -1.f;
-            const float n_j = rowv ? s_nrm[j] : 0.f;
-            const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TROWS);
-            uint64_t rmask = 0;
-            uint32_t cmA = 0, cmB = 0; // ballot masks of this warp's local columns lane and lane+32
-            if (warp_live) {
-#pragma unroll 1
-                for (int k = 0; k < MAXG; ++k) {
-                    const int g = h + 2 * k;
-                    if (g >= G) break;
-                    uint32_t raw[16];
-                    tmem_ld16_async(trow + 16 * g, raw);
-                    tmem_wait_ld16(raw);
-#pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const int i = 16 * g + t; // new-list column
-                        const int ii = min(i, na - 1);
-                        const float dd = __fsub_rn(__fadd_rn(n_j, s_nrm[ii]), 2.f * __uint_as_float(raw[t]));
-                        const bool pv = rowv && i < na && (j >= na || i < j) && s_col[ii] != id_j;
-                        rmask |= (uint64_t)(pv && dd <= rad_j) << (16 * k + t);
-                        const unsigned m = __ballot_sync(KCNA_FULL, pv && dd <= s_rad[ii]);
-                        const int c = 16 * k + t; // local column
-                        if (lane == (c & 31)) {
-                            if (c < 32)
-                                cmA = m;
-                            else
-                                cmB = m;
-                        }
-                    }
+        };
+        prefetch(0);
+        prefetch(1);
+        load_counts(0, 0);
+        load_counts(1, 1);
+        int k = 0;
+        for (uint32_t node = blockIdx.x; node < a.N; node += gridDim.x, ++k) {
+            const int sl = k & 1;
+            const uint32_t fn = min(c_fn[0], a.fwd_new_cap), rn = a.iter > 0 ? min(c_rn[0], a.R) : 0u;
+            const uint32_t fo = min(c_fo[0], a.fwd_old_cap), ro = a.iter > 0 ? min(c_ro[0], a.R) : 0u;
+            c_fn[0] = c_fn[1], c_rn[0] = c_rn[1], c_fo[0] = c_fo[1], c_ro[0] = c_ro[1];
+            c_fn[1] = c_fn[2], c_rn[1] = c_rn[2], c_fo[1] = c_fo[2], c_ro[1] = c_ro[2];
+            load_counts(k + 2, 1);
+            if (!mbar_wait(&S.ids_full[k % NR], (k / NR) & 1)) { ok = false; break; }
+            if (k >= NS && !mbar_wait(&S.node_empty[sl], ((k >> 1) - 1) & 1)) { ok = false; break; }
+            if (S.abort_flag) break;
+            // compact the node's set from its raw entry: A (new list, <= 128), then B
+            const uint32_t *raw = raw_ring + (size_t)(k % NR) * RL.words;
+            uint32_t *ids = set_ids + (size_t)sl * colcap;
+            const uint32_t na = min(fn + rn, (uint32_t)TROWS);
+            const uint32_t ncol = na + fo + ro;
+            for (uint32_t i = lane; i < fn && i < na; i += 32) ids[i] = raw[i];
+            for (uint32_t i = lane; i < rn && fn + i < na; i += 32) ids[fn + i] = raw[RL.o_rnew + i];
+            for (uint32_t i = lane; i < fo; i += 32) ids[na + i] = raw[RL.o_old + i];
+            for (uint32_t i = lane; i < ro; i += 32) ids[na + fo + i] = raw[RL.o_rold + i];
+            __syncwarp();
+            prefetch(k + 2); // raw entry (k+2) % NR was compacted two nodes ago
+            if (lane == 0) {
+                S.meta[sl].node = node;
+                S.meta[sl].na = na;
+                S.meta[sl].NA = (na + 15) & ~15u;
+                S.meta[sl].ncol = ncol;
+                if (na) {
+                    pairs += (unsigned long long)na * (na - 1) / 2 + (unsigned long long)na * (ncol - na);
+                    rows_g += ncol;
                 }
             }
-            s_rcnt[h][32 * q + lane] = (uint8_t)__popcll(rmask);
-            // column counts of this quarter: local column c = 16k + t <-> column 16(h + 2k) + t
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int c = lane + 32 * half, k = c >> 4;
-                const int i = 16 * (h + 2 * k) + (c & 15);
-                if (k < MAXG && h + 2 * k < G) s_ccnt[q][i] = (uint8_t)__popc(half ? cmB : cmA);
+            gather_rows(slotA + sl * TILE, ids, 0, (int)na, Xh, ldh, nc16, lane);
+            for (uint32_t i = lane; i < na; i += 32) {
+                cp_async4(smem_u32(&S.a_rad[sl][i]), a.radius + ids[i]);
+                cp_async4(smem_u32(&S.a_nrm[sl][i]), norms + ids[i]);
             }
-            __syncthreads();
-            // one reservation per target: set members by threads 0..127, new-list columns by 128..255
-            if (tid < TROWS) {
-                const uint32_t tot = (uint32_t)s_rcnt[0][tid] + s_rcnt[1][tid];
-                if (tot) {
-                    const uint32_t base = atomicAdd(a.cand_cnt + s_col[r * TROWS + tid], tot);
-                    s_rbase[0][tid] = base;
-                    s_rbase[1][tid] = base + s_rcnt[0][tid];
-                    atomicAdd(&s_emit, tot);
-                }
-            } else {
-                const int i = tid - TROWS;
-                if (i < na) {
-                    const uint32_t c0 = s_ccnt[0][i], c1 = s_ccnt[1][i], c2 = s_ccnt[2][i], c3 = s_ccnt[3][i];
-                    const uint32_t tot = c0 + c1 + c2 + c3;
-                    if (tot) {
-                        const uint32_t base = atomicAdd(a.cand_cnt + s_col[i], tot);
-                        s_cbase[0][i] = base;
-                        s_cbase[1][i] = base + c0;
-                        s_cbase[2][i] = base + c0 + c1;
-                        s_cbase[3][i] = base + c0 + c1 + c2;
-                        atomicAdd(&s_emit, tot);
-                    }
-                }
+            // padding columns na..NA-1: a NaN norm makes every distance NaN, so no pair passes
+            for (uint32_t i = na + lane; i < ((na + 15) & ~15u); i += 32) {
+                S.a_nrm[sl][i] = __uint_as_float(0x7FC00000u);
+                S.a_rad[sl][i] = 0.f;
             }
-            __syncthreads();
-            if (warp_live) { // writes; the distances are read again from TMEM
-                const uint32_t flags = (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
-                uint32_t p = s_rbase[h][32 * q + lane];
-                uint64_t *dst = a.cand + (uint64_t)id_j * a.CB;
-#pragma unroll 1
-                for (int k = 0; k < MAXG; ++k) {
-                    const int g = h + 2 * k;
-                    if (g >= G) break;
-                    const uint32_t gm = (uint32_t)(rmask >> (16 * k)) & 0xFFFFu;
-                    const uint32_t cm = k < 2 ? cmA : cmB;
-                    if (!__any_sync(KCNA_FULL, gm != 0u || cm != 0u)) continue;
-                    uint32_t raw[16];
-                    tmem_ld16_async(trow + 16 * g, raw);
-                    tmem_wait_ld16(raw);
-#pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const int i = 16 * g + t;
-                        const int ii = min(i, na - 1);
-                        const float dd = __fsub_rn(__fadd_rn(n_j, s_nrm[ii]), 2.f * __uint_as_float(raw[t]));
-                        if ((gm >> t) & 1u) {
-                            if (p < a.CB) dst[p] = kcna_key(dd, s_col[ii], flags);
-                            ++p;
-                        }
-                        const int c = 16 * k + t;
-                        const unsigned m = __shfl_sync(KCNA_FULL, c < 32 ? cmA : cmB, c & 31);
-                        if ((m >> lane) & 1u) {
-                            const uint32_t pc = s_cbase[q][ii] + __popc(m & kcna_lanemask_lt());
-                            if (pc < a.CB) a.cand[(uint64_t)s_col[ii] * a.CB + pc] = kcna_key(dd, id_j, flags);
-                        }
-                    }
+            mbar_arrive_cp_async(&S.node_full[sl]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.node_full[sl]);
+            const int ntile = na ? (int)((ncol + TROWS - 1) / TROWS) : 0;
+            for (int t = 0; t < ntile; ++t, ++tcount) {
+                const int st = (int)(tcount % TS), mt = (int)(tcount % MS);
+                if (tcount >= (uint32_t)MS && !mbar_wait(&S.meta_empty[mt], ((tcount / MS) - 1) & 1)) {
+                    ok = false;
+                    break;
                 }
-            }
-            // slot b gathered and TMEM buffer b read by every thread: tile r+2 may start
-            cp_async_wait_all();
-            fence_proxy_async();
-            fence_before();
-            ok = __syncthreads_and(ok) != 0;
-            if (ok && r + 2 < ntile) {
-                if (tid == 0) {
-                    fence_after();
-                    issue_tile(tmem + b * TROWS, tS + b * TILE, tA, idesc, nkb);
-                    mma_commit(&mbar[b]);
+                const int first = t * TROWS, cnt = min((int)ncol - first, TROWS);
+                for (int i = lane; i < cnt; i += 32) {
+                    cp_async4(smem_u32(&S.t_rad[mt][i]), a.radius + ids[first + i]);
+                    cp_async4(smem_u32(&S.t_nrm[mt][i]), norms + ids[first + i]);
                 }
-                pend |= 1u << b;
+                mbar_arrive_cp_async(&S.meta_full[mt]);
+                if (tcount >= (uint32_t)TS && !mbar_wait(&S.tile_empty[st], ((tcount / TS) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                gather_rows(stage0 + st * TILE, ids, first, cnt, Xh, ldh, nc16, lane);
+                mbar_arrive_cp_async(&S.tile_full[st]);
             }
             if (!ok) break;
         }
-        // found: this node's join emitted a candidate
-        if (tid == 0) {
-            a.found[node] = s_emit ? 1 : 0;
-            emitted += s_emit;
-            s_emit = 0;
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        // bulk copies still in flight (prefetched lists of nodes not processed) land before exit
+        for (int kk = k; kk <= k + 2; ++kk) {
+            const uint32_t nd = blockIdx.x + (uint32_t)kk * gridDim.x;
+            if (nd < a.N) (void)mbar_wait(&S.ids_full[kk % NR], (kk / NR) & 1, 1u << 16);
         }
-    }
-    // after a wait gave up: wait (bounded) for the products still in flight
-    // before the accumulator columns are released
-    for (int b = 0; b < 2; ++b)
-        if ((pend >> b) & 1u) (void)mbar_wait(&mbar[b], (phase >> b) & 1u);
-    if (tid == 0) {
-        atomicAdd(a.counters + 0, pairs);
-        atomicAdd(a.counters + 5, rows_g);
-        atomicAdd(a.counters + 6, emitted);
+        if (!ok) S.abort_flag = 1;
+        if (lane == 0) {
+            atomicAdd(a.counters + 0, pairs);
+            atomicAdd(a.counters + 5, rows_g);
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            uint32_t tcount = 0, acount = 0;
+            int k = 0;
+            for (uint32_t node = blockIdx.x; node < a.N; node += gridDim.x, ++k) {
+                const int sl = k & 1;
+                if (!mbar_wait(&S.node_full[sl], (k >> 1) & 1) || S.abort_flag) { ok = false; break; }
+                const uint32_t na = S.meta[sl].na, NA = S.meta[sl].NA, ncol = S.meta[sl].ncol;
+                const int ntile = na ? (int)((ncol + TROWS - 1) / TROWS) : 0;
+                const uint32_t idesc = idesc_bf16(TROWS, (int)NA);
+                for (int t = 0; t < ntile; ++t, ++tcount, ++acount) {
+                    const int st = (int)(tcount % TS), b = (int)(acount % NACC);
+                    if (!mbar_wait(&S.tile_full[st], (tcount / TS) & 1)) { ok = false; break; }
+                    if (acount >= (uint32_t)NACC && !mbar_wait(&S.acc_empty[b], ((acount / NACC) - 1) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    issue_tile(tmem + (uint32_t)(b * TROWS), stage0 + st * TILE, slotA + sl * TILE, idesc, nkb);
+                    mma_commit(&S.acc_full[b]);
+                    mma_commit(&S.tile_empty[st]);
+                }
+                if (!ok) break;
+            }
+            if (!ok) {
+                S.abort_flag = 1;
+                // products still in flight finish before TMEM is released
+                for (uint32_t b = 0; b < (uint32_t)NACC; ++b)
+                    if (acount > b) {
+                        const uint32_t last = b + (acount - 1 - b) / NACC * NACC; // last tile issued to b
+                        (void)mbar_wait(&S.acc_full[b], (last / NACC) & 1u, 1u << 16);
+                    }
+            }
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column-group phase (0..3)
+        const int rr = 32 * q + lane;                // this thread's row of a tile
+        unsigned long long emitted = 0;
+        uint32_t tcount = 0;
+        int k = 0;
+        for (uint32_t node = blockIdx.x; node < a.N; node += gridDim.x, ++k) {
+            const int sl = k & 1;
+            bool mine = mbar_wait(&S.node_full[sl], (k >> 1) & 1) && !S.abort_flag;
+            if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
+            const int na = (int)S.meta[sl].na, NA = (int)S.meta[sl].NA, ncol = (int)S.meta[sl].ncol;
+            const int G = NA >> 4;
+            const int ntile = na ? (ncol + TROWS - 1) / TROWS : 0;
+            const uint32_t *ids = set_ids + (size_t)sl * colcap;
+            const float *arad = S.a_rad[sl], *anrm = S.a_nrm[sl]; // anrm is NaN on columns na..NA-1
+            for (int t = 0; t < ntile; ++t, ++tcount) {
+                const int mt = (int)(tcount % MS), b = (int)(tcount % NACC);
+                mine = mbar_wait(&S.acc_full[b], (tcount / NACC) & 1) && mbar_wait(&S.meta_full[mt], (tcount / MS) & 1);
+                fence_after();
+                const int j = t * TROWS + rr; // set member
+                const bool warp_live = t * TROWS + 32 * q < ncol && h < G;
+                const bool rowv = j < ncol && mine;
+                const uint32_t id_j = rowv ? ids[j] : 0u;
+                const float rad_j = rowv ? S.t_rad[mt][rr] : 0.f;
+                const float n_j = rowv ? S.t_nrm[mt][rr] : __uint_as_float(0x7FC00000u); // NaN: no pair passes
+                // rows of the new list meet only earlier new-list columns (each pair once)
+                const bool tri = t == 0 && 32 * q < na;
+                const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TROWS);
+                uint32_t rmask = 0, cm = 0; // cm: ballot of local column `lane`
+                if (warp_live) {
+#pragma unroll 1
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const int g = h + 4 * kk;
+                        if (g >= G) break;
+                        uint32_t raw[16];
+                        tmem_ld16_async(trow + 16 * g, raw);
+                        tmem_wait_ld16(raw);
+#pragma unroll
+                        for (int u = 0; u < 16; ++u) {
+                            const int i = 16 * g + u; // new-list column
+                            const float dd = __fsub_rn(__fadd_rn(n_j, anrm[i]), 2.f * __uint_as_float(raw[u]));
+                            bool rp = dd <= rad_j, cp = dd <= arad[i];
+                            if (tri && i >= j) rp = cp = false;
+                            if ((rp || cp) && ids[i] == id_j) rp = cp = false; // an id in both lists
+                            rmask |= (uint32_t)rp << (16 * kk + u);
+                            const unsigned m = __ballot_sync(KCNA_FULL, cp);
+                            if (lane == 16 * kk + u) cm = m;
+                        }
+                    }
+                }
+                // reservations without barriers between warps: each thread
+                // reserves its row's run for this warp's columns, lane c the
+                // run of local column c for this lane quarter
+                const int nr = __popc(rmask), nc = __popc(cm);
+                uint32_t p = nr ? atomicAdd(a.cand_cnt + id_j, (uint32_t)nr) : 0u;
+                const uint32_t cb =
+                    nc ? atomicAdd(a.cand_cnt + ids[16 * (h + 4 * (lane >> 4)) + (lane & 15)], (uint32_t)nc) : 0u;
+                const unsigned wtot = kcna_warp_sum((unsigned)(nr + nc));
+                if (lane == 0 && wtot) atomicAdd(&S.emit[sl], wtot);
+                if (wtot) { // writes; the distances are read again from TMEM
+                    const uint32_t flags = (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
+                    uint64_t *dst = a.cand + (uint64_t)id_j * a.CB;
+#pragma unroll 1
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const int g = h + 4 * kk;
+                        if (g >= G) break;
+                        const uint32_t gm = (rmask >> (16 * kk)) & 0xFFFFu;
+                        const uint32_t cmk = (lane >> 4) == kk ? cm : 0u;
+                        if (!__any_sync(KCNA_FULL, gm != 0u || cmk != 0u)) continue;
+                        uint32_t raw[16];
+                        tmem_ld16_async(trow + 16 * g, raw);
+                        tmem_wait_ld16(raw);
+#pragma unroll
+                        for (int u = 0; u < 16; ++u) {
+                            const int i = 16 * g + u;
+                            const int c = 16 * kk + u;
+                            const unsigned m = __shfl_sync(KCNA_FULL, cm, c);
+                            const uint32_t cbc = __shfl_sync(KCNA_FULL, cb, c);
+                            if (((gm >> u) & 1u) || ((m >> lane) & 1u)) {
+                                const float dd =
+                                    __fsub_rn(__fadd_rn(n_j, anrm[i]), 2.f * __uint_as_float(raw[u]));
+                                if ((gm >> u) & 1u) {
+                                    if (p < a.CB) dst[p] = kcna_key(dd, ids[i], flags);
+                                    ++p;
+                                }
+                                if ((m >> lane) & 1u) {
+                                    const uint32_t pc = cbc + __popc(m & kcna_lanemask_lt());
+                                    if (pc < a.CB) a.cand[(uint64_t)ids[i] * a.CB + pc] = kcna_key(dd, id_j, flags);
+                                }
+                            }
+                        }
+                    }
+                }
+                if (!mine) ok = false;
+                // accumulator and metadata entry released by each epilogue warp
+                fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(&S.acc_empty[b]);
+                    mbar_arrive(&S.meta_empty[mt]);
+                }
+                if (!__all_sync(KCNA_FULL, ok)) {
+                    ok = false;
+                    break;
+                }
+            }
+            if (!ok) break;
+            // found: this node's join emitted a candidate; the last epilogue
+            // warp to finish the node writes it
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                if (atomicAdd(&S.done[sl], 1u) == (unsigned)(EPI_WARPS - 1)) {
+                    __threadfence_block();
+                    const unsigned e = atomicExch(&S.emit[sl], 0u);
+                    if (na > 0) a.found[S.meta[sl].node] = e ? 1 : 0;
+                    emitted += e;
+                    S.done[sl] = 0;
+                }
+                mbar_arrive(&S.node_empty[sl]);
+            }
+        }
+        if (!ok) S.abort_flag = 1;
+        if (lane == 0 && emitted) atomicAdd(a.counters + 6, emitted);
     }
     fence_before();
     __syncthreads();
-    if (warp == 0) tmem_free(tmem, TMEM_COLS);
-    if (!ok && tid == 0) kcna_set_err(a.err, KCNA_DERR_SPIN);
+    if (warp == 1) tmem_free(tmem, NACC * TROWS);
+    if (!ok) kcna_set_err(a.err, KCNA_DERR_SPIN);
 }
 
 } // namespace
+
+static size_t join_tc_smem(const JoinArgs &a) {
+    const uint32_t colcap = std::max<uint32_t>(a.capA, TROWS + a.capB);
+    const uint32_t rc = (std::min(a.R, a.RB) + 3) & ~3u;
+    const RawLayout RL = raw_layout(a.fwd_new_cap, rc, a.fwd_old_cap);
+    return 1024 + (size_t)(NS + TS) * TILE + sizeof(WsShared) + (size_t)NS * colcap * 4 + 16 + (size_t)NR * RL.words * 4;
+}
+
+bool kcna_join_tc_fits(const JoinArgs &a) {
+    return join_tc_smem(a) <= 227 * 1024 && !((a.fwd_new_cap | a.fwd_old_cap | a.RB) & 3u);
+}
 
 kcna_status kcna_join_tc_launch(kcna_ctx *c, const JoinArgs &a) {
     if (!c->gram_exact || !c->Xh || !c->norms || (c->ld & 7u) || c->ld > 128)
         return kcna_fail(c, KCNA_E_STATE, "Gram-tile join needs exact BF16 rows with d <= 128");
     const uint32_t colcap = std::max<uint32_t>(a.capA, TROWS + a.capB);
-    const size_t sm = 1024 + TILES + (size_t)colcap * 12;
+    if (!kcna_join_tc_fits(a)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile join: lists too long for shared memory");
+    const size_t sm = join_tc_smem(a);
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                              "join_tc smem attr"));
-    // all of the unified L1 as shared memory, so that two blocks fit per SM
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                     (int)cudaSharedmemCarveoutMaxShared),
-                             "join_tc carveout"));
-    int per_sm = 0;
-    KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, join_tc_kernel, TJ, sm),
-                             "join_tc occupancy"));
-    per_sm = std::min(std::max(per_sm, 1), 2); // 2 x 256 TMEM columns fill one SM's 512
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(a.N, (uint64_t)std::max(c->num_sms, 1) * per_sm);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(a.N, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
-    join_tc_kernel<<<grid, TJ, sm, c->stream>>>(a, c->Xh, (int)c->ld, c->norms, colcap);
+    join_tc_kernel<<<grid, WS_THREADS, sm, c->stream>>>(a, c->Xh, (int)c->ld, c->norms, colcap);
     KCNA_LAUNCHED(c);
     return kcna_cuda_check(c, cudaGetLastError(), "join_tc_kernel");
 }

@@ -266,7 +266,6 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
     float *s_radA = s_D + 128 * (JCOLS + 1);                      // capA
     uint32_t *s_A = reinterpret_cast<uint32_t *>(s_radA + a.capA); // capA
     uint32_t *s_B = s_A + a.capA;                                 // capB
-    __shared__ uint32_t s_na, s_nb, s_tmp;
     __shared__ int s_any;
     __shared__ unsigned s_emit;
     const uint32_t node = blockIdx.x;
@@ -279,12 +278,9 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
     __syncthreads();
     uint32_t rn = 0, ro = 0;
     if (a.iter > 0) {
-        take_reverse(a.rnew + (uint64_t)node * a.RB, a.rnew_cnt[node], a.RB, a.R, a.seed,
-                     join_reverse_stream(a.iter, node, 0), s_A + fn, &s_tmp);
-        rn = s_tmp;
-        take_reverse(a.rold + (uint64_t)node * a.RB, a.rold_cnt[node], a.RB, a.R, a.seed,
-                     join_reverse_stream(a.iter, node, 1), s_B + fo, &s_tmp);
-        ro = s_tmp;
+        rn = take_reverse(a.rnew + (uint64_t)node * a.RB, a.rnew_cnt[node], a.R, s_A + fn);
+        ro = take_reverse(a.rold + (uint64_t)node * a.RB, a.rold_cnt[node], a.R, s_B + fo);
+        __syncthreads();
     }
     // at most 128 rows per tile; the forward list alone is <= S + R < 128 in practice
     const int na = (int)min(fn + rn, 128u), nb = (int)(fo + ro);
@@ -700,6 +696,47 @@ __global__ void sample_lists_kernel(uint64_t *__restrict__ pool, uint32_t cap, u
     }
 }
 
+// Random subset of R reverse entries (the reference shuffles rnn_* and keeps
+// R, src/kgraph.cpp:1183-1201): each entry gets the priority
+// hash(seed, iteration, node, id) and the R smallest priorities stay, in
+// priority order.  The subset depends only on the set of entries, not on the
+// order in which sample_lists_kernel's atomics appended them, so a run is
+// reproducible as long as no list overflows RB.  Warp per list; lists of at
+// most R entries are left as they are.
+constexpr int SEL_WARPS = 8;
+__global__ void __launch_bounds__(SEL_WARPS * 32) select_reverse_kernel(uint32_t *__restrict__ rnew,
+                                                                       uint32_t *__restrict__ rnew_cnt,
+                                                                       uint32_t *__restrict__ rold,
+                                                                       uint32_t *__restrict__ rold_cnt, uint32_t N,
+                                                                       uint32_t RB, uint32_t R, uint64_t seed,
+                                                                       uint32_t iter, int P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint64_t *s = reinterpret_cast<uint64_t *>(smem) + (size_t)w * P;
+    const uint64_t item = (uint64_t)blockIdx.x * SEL_WARPS + w; // list index: node * 2 + old
+    if (item >= 2ull * N) return;
+    const uint32_t node = (uint32_t)(item >> 1), old = (uint32_t)(item & 1);
+    uint32_t *list = (old ? rold : rnew) + (uint64_t)node * RB;
+    uint32_t *cnt = (old ? rold_cnt : rnew_cnt) + node;
+    const uint32_t m = min(*cnt, RB);
+    if (m <= R) {
+        if (lane == 0) *cnt = m; // never more than the stored entries
+        return;
+    }
+    const uint64_t stream = join_reverse_stream(iter, node, old);
+    for (int i = lane; i < P; i += 32) {
+        if (i < (int)m) {
+            const uint32_t id = list[i];
+            s[i] = ((uint64_t)kcna_rand32(seed, stream, id) << 32) | id;
+        } else {
+            s[i] = KCNA_EMPTY_KEY;
+        }
+    }
+    kcna_warp_bitonic(s, P);
+    for (uint32_t i = lane; i < R; i += 32) list[i] = (uint32_t)(s[i] & 0xFFFFFFFFull);
+    if (lane == 0) *cnt = R;
+}
+
 // control recall: |pool[0..min(cnt,K)) ∩ exact[0..K)| per control
 __global__ void control_recall_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
                                       uint32_t cap, const uint32_t *__restrict__ controls,
@@ -748,12 +785,13 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     // reverse-list buffer: 2R entries (at most 4 per join thread, 1024)
     const char *rb = getenv("KCNA_REV_CAP");
     c->RB = std::min<uint32_t>(std::max<uint32_t>(rb ? (uint32_t)atoi(rb) : 2 * p->R, std::max<uint32_t>(p->R, 32)), 1024);
+    c->RB = (c->RB + 3) & ~3u; // rows of 16-byte multiples (bulk copies in the Gram-tile join)
     const char *cb = getenv("KCNA_CAND_CAP");
     uint32_t CB = cb ? (uint32_t)atoi(cb) : 4 * std::max<uint32_t>(p->L, 64);
     CB = std::min<uint32_t>(std::max<uint32_t>(CB, 64), 8192);
     c->CB = (uint32_t)kcna_pow2_ceil((int)CB);
-    c->fwd_new_cap = std::max<uint32_t>(2 * p->S, 64);
-    c->fwd_old_cap = std::max<uint32_t>(p->L, 1);
+    c->fwd_new_cap = (std::max<uint32_t>(2 * p->S, 64) + 3) & ~3u;
+    c->fwd_old_cap = (std::max<uint32_t>(p->L, 1) + 3) & ~3u;
     KCNA_TRY(kcna_alloc(c, &c->pool, N * c->cap, "pool"));
     KCNA_TRY(kcna_alloc(c, &c->pool_cnt, N, "pool_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->radius, N, "radius"));
@@ -825,8 +863,8 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     a.CB = c->CB;
     a.found = c->found;
     a.counters = c->counters;
-    a.capA = c->fwd_new_cap + c->RB;
-    a.capB = c->fwd_old_cap + c->RB;
+    a.capA = c->fwd_new_cap + std::min(p->R, c->RB);
+    a.capB = c->fwd_old_cap + std::min(p->R, c->RB);
     a.err = c->d_err;
     size_t sm = join_smem_bytes(a.capA, a.capB);
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_kernel<RowsF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -837,7 +875,7 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
                              "join smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    if (c->gram_exact) {
+    if (c->gram_exact && kcna_join_tc_fits(a)) {
         KCNA_TRY(kcna_join_tc_launch(c, a));
     } else {
         if (c->Xh)
@@ -900,7 +938,6 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
 }
 
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter) {
-    (void)iter;
     cudaStream_t s = c->stream;
     KCNA_TRY(kcna_phase_begin(c));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->rnew_cnt, 0, (size_t)c->n * 4, s), "memset"));
@@ -912,6 +949,13 @@ kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter) {
                                                               c->fwd_new_cap, c->fwd_new_cnt, c->fwd_old,
                                                               c->fwd_old_cap, c->fwd_old_cnt, c->rnew, c->rnew_cnt,
                                                               c->rold, c->rold_cnt, c->RB, c->counters);
+    KCNA_LAUNCHED(c);
+    const int P = kcna_pow2_ceil((int)c->RB);
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(select_reverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     SEL_WARPS * P * 8),
+                             "select smem attr"));
+    select_reverse_kernel<<<kcna_div_up(2ull * c->n, SEL_WARPS), SEL_WARPS * 32, (size_t)SEL_WARPS * P * 8, s>>>(
+        c->rnew, c->rnew_cnt, c->rold, c->rold_cnt, c->n, c->RB, p->R, p->seed, (uint32_t)iter, P);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "sample kernels"));
     return kcna_phase_end(c, KCNA_PHASE_SAMPLE);
@@ -1013,7 +1057,7 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
         KCNA_TRY(kcna_control_recall(c, P.K, &st->seed_recall));
         kcna_log(c, &P, "learned seed: %.1f ms (training %.1f ms), loss %.3f -> %.3f, recall %.4f", st->seed_total_ms,
                  st->seed_train_ms, st->seed_loss_first, st->seed_loss_last, st->seed_recall);
-        KCNA_TRY(kcna_nnd_sample(c, &P, 0));
+        KCNA_TRY(kcna_nnd_sample(c, &P, 1));
         iter_base = 1;
     } else {
         KCNA_TRY(kcna_nnd_init(c, &P));
@@ -1055,7 +1099,7 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
             break;
         }
         if (it + 1 >= P.iterations) break;
-        KCNA_TRY(kcna_nnd_sample(c, &P, (int)it));
+        KCNA_TRY(kcna_nnd_sample(c, &P, (int)it + 1 + iter_base));
     }
     st->n_comps = comps_total;
     st->screened_pairs = c->gram_exact ? comps_total : 0; // Gram tiles, exact: nothing to rescore

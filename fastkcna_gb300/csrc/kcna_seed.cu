@@ -386,7 +386,6 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     cudaMemcpyAsync(W1, hW1.data(), nW1 * 4, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(W2, hW2.data(), nW2 * 4, cudaMemcpyHostToDevice, s);
     // rows scaled to unit RMS: the encoder's first layer absorbs the data range
-    float *Xs_scaled = Xs; // in place
     {
         std::vector<float> probe((size_t)std::min<uint32_t>(ns, 1024) * ld);
         cudaMemcpyAsync(probe.data(), Xs, probe.size() * 4, cudaMemcpyDeviceToHost, s);
@@ -414,7 +413,6 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     KCNA_TRY(dev.get(&w.dY, (size_t)R * H2, "dY"));
     KCNA_TRY(dev.get(&w.dG, (size_t)R * H1, "dG"));
     KCNA_TRY(dev.get(&w.loss, 1, "loss"));
-    (void)Xs_scaled;
     float first_loss = -1.f, last_loss = 0.f;
     for (int it = 0; it < steps; ++it) {
         make_triplets_kernel<<<kcna_div_up(B, 256), 256, 0, s>>>(sc->pool, sc->pool_cnt, sc->cap, ns, kp, B,

@@ -138,6 +138,41 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// mbarrier arrive (release, CTA scope) by this thread.
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+// Arrive on mbar once every cp.async this thread issued so far has landed
+// (the arrival counts towards the barrier's expected count).
+__device__ __forceinline__ void mbar_arrive_cp_async(uint64_t *mbar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+// mbarrier arrive by this thread that also raises the barrier's expected
+// transaction count by `bytes` (bulk copies then complete them).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.release.cta.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_u32(mbar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Bulk (TMA engine) copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned) global -> shared, completing `bytes` transactions on mbar.
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
+// Named barrier over `count` threads (a multiple of 32), id 1..15.
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// 4-byte asynchronous copy global -> shared (through L1).
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+
 // 16-byte asynchronous copy global -> shared (L2 only), and the wait for all
 // of this thread's copies.
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {

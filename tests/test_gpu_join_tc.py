@@ -98,8 +98,9 @@ def test_gram_exact_mode_rejects_unsafe_rows(index):
 
 
 def test_tc_join_build_matches_fp32_build(index, monkeypatch):
-    """Whole FastNSG build: with identical pools the prune, link, P2K and
-    tree_grow steps see identical inputs, so the graphs agree."""
+    """Whole FastNSG build: with identical pools the prune, link, P2K (also on
+    Gram tiles here) and tree_grow steps see identical inputs, so the graphs
+    agree."""
     _roomy(monkeypatch)
     X = synth.base("c2", 15000)
     kw = dict(K=100, L=100, S=10, R=100, iterations=5, search_L=40, nsg_R=32, search_K=100, controls=50,
@@ -114,3 +115,5 @@ def test_tc_join_build_matches_fp32_build(index, monkeypatch):
     assert np.array_equal(deg0, deg1)
     assert rows_equal_as_sets(g0, deg0, g1, deg1) == 0
     assert st0["loop_recall"][-1] == st1["loop_recall"][-1]
+    # the P2K join on Gram tiles evaluates the same pairs as the FP32 one
+    assert st0["bridge_comps"] == st1["bridge_comps"] and st0["n_comps"] == st1["n_comps"]
