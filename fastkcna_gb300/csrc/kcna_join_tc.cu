@@ -17,8 +17,8 @@
 //   warp 0      producer: the bulk-copy engine brings node n+2's four lists
 //               into a raw ring while node n is handled; assembles node n's
 //               set (new list A, na <= 128, then the old list B; ncol entries)
-//               in a node slot, gathers A's BF16
-//               rows with cp.async into the slot, then the set in tiles of 128
+//               in a node slot, gathers A's BF16 rows into the slot with TMA
+//               (tile::gather4, 128-byte swizzle), then the set in tiles of 128
 //               rows into a ring of row stages (freed as soon as the tile's
 //               products are done) and the radius/norm of each row into a
 //               deeper ring the epilogue frees; every gather lands as an
@@ -41,6 +41,8 @@
 // Every wait is bounded; a wait that gives up stops the block, sets the error
 // word and lets in-flight products finish before TMEM is released.
 #include <algorithm>
+
+#include <cuda.h>
 
 #include "kcna_internal.h"
 #include "kcna_join.cuh"
@@ -91,14 +93,20 @@ struct WsShared {
     float t_rad[MS][TROWS], t_nrm[MS][TROWS];
 };
 
-// rows [first, first+count) of ids -> rows 0..count-1 of a 128-row region; lane-strided
-__device__ __forceinline__ void gather_rows(uint32_t region, const uint32_t *ids, int first, int count,
-                                            const uint16_t *__restrict__ Xh, int ldh, int nc16, int lane) {
-    for (int idx = lane; idx < count * nc16; idx += 32) {
-        const int r = idx / nc16, c = idx - r * nc16;
-        const uint16_t *src = Xh + (uint64_t)ids[first + r] * (uint64_t)ldh + c * 8;
-        cp_async16(region + (uint32_t)(c >> 3) * TROWS * KBB + sw128_off((uint32_t)r, (uint32_t)(c & 7)), src);
+// rows [first, first+count) of ids -> rows 0..count-1 of a 128-row region by
+// TMA gather4 (four rows of one K block per instruction; the last group
+// repeats its last row), lane-strided.  Returns the transaction bytes.
+__device__ __forceinline__ uint32_t tma_rows(uint32_t region, const uint32_t *ids, int first, int count,
+                                             const void *tmap, int nkb, uint64_t *bar, int lane) {
+    const int ng = (count + 3) >> 2;
+    for (int e = lane; e < ng * nkb; e += 32) {
+        const int g = nkb == 2 ? e >> 1 : e, kb = nkb == 2 ? e & 1 : 0;
+        const int r = 4 * g, last = first + count - 1;
+        tma_gather4(region + (uint32_t)kb * TROWS * KBB + (uint32_t)r * KBB, tmap, 64 * kb, (int)ids[first + r],
+                    (int)ids[min(first + r + 1, last)], (int)ids[min(first + r + 2, last)],
+                    (int)ids[min(first + r + 3, last)], bar);
     }
+    return (uint32_t)(ng * 4 * nkb) * KBB;
 }
 
 // D[128 x N] = rows(a) . rows(b)^T over nkb K blocks of 64 elements.
@@ -111,8 +119,9 @@ __device__ __forceinline__ void issue_tile(uint32_t tmem_d, uint32_t a_base, uin
                      desc_sw128(b_base + kb * TROWS * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
 }
 
-__global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, const uint16_t *__restrict__ Xh, int ldh,
-                                                                const float *__restrict__ norms, uint32_t colcap) {
+__global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                                int ldh, const float *__restrict__ norms,
+                                                                uint32_t colcap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u; // swizzled tiles need 1024-byte alignment
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
@@ -125,7 +134,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
         (reinterpret_cast<uintptr_t>(set_ids + (size_t)NS * colcap) + 15) & ~(uintptr_t)15);
     const uint32_t slotA = tiles_s, stage0 = tiles_s + NS * TILE;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nc16 = ldh >> 3, nkb = (ldh + 63) >> 6;
+    const int nkb = (ldh + 63) >> 6;
+    const void *tm = &tmap;
 
     // K padding beyond ldh is never written by the gathers and must read as zero
     for (int i = tid; i < (int)((NS + TS) * TILE / 16); i += WS_THREADS)
@@ -133,13 +143,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
     if (warp == 1) tmem_alloc(&S.tmem, NACC * TROWS);
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
-            mbar_init(&S.node_full[i], 33);  // 32 producer lanes' copies + the producer's metadata
+            mbar_init(&S.node_full[i], 33);  // 32 producer lanes' copies + the producer's expect_tx (metadata, A rows)
             mbar_init(&S.node_empty[i], EPI_WARPS);
             S.emit[i] = 0;
             S.done[i] = 0;
         }
         for (int i = 0; i < TS; ++i) {
-            mbar_init(&S.tile_full[i], 32);  // producer lanes' copies
+            mbar_init(&S.tile_full[i], 1);   // producer's expect_tx; the TMA gathers complete it
             mbar_init(&S.tile_empty[i], 1);  // MMA commit
         }
         for (int i = 0; i < MS; ++i) {
@@ -229,7 +239,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                     rows_g += ncol;
                 }
             }
-            gather_rows(slotA + sl * TILE, ids, 0, (int)na, Xh, ldh, nc16, lane);
             for (uint32_t i = lane; i < na; i += 32) {
                 cp_async4(smem_u32(&S.a_rad[sl][i]), a.radius + ids[i]);
                 cp_async4(smem_u32(&S.a_nrm[sl][i]), norms + ids[i]);
@@ -241,7 +250,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
             }
             mbar_arrive_cp_async(&S.node_full[sl]);
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.node_full[sl]);
+            if (lane == 0) mbar_arrive_expect_tx(&S.node_full[sl], (uint32_t)((na + 3) / 4 * 4 * nkb) * KBB);
+            __syncwarp();
+            if (na) tma_rows(slotA + sl * TILE, ids, 0, (int)na, tm, nkb, &S.node_full[sl], lane);
             const int ntile = na ? (int)((ncol + TROWS - 1) / TROWS) : 0;
             for (int t = 0; t < ntile; ++t, ++tcount) {
                 const int st = (int)(tcount % TS), mt = (int)(tcount % MS);
@@ -259,8 +270,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                     ok = false;
                     break;
                 }
-                gather_rows(stage0 + st * TILE, ids, first, cnt, Xh, ldh, nc16, lane);
-                mbar_arrive_cp_async(&S.tile_full[st]);
+                if (lane == 0) mbar_arrive_expect_tx(&S.tile_full[st], (uint32_t)((cnt + 3) / 4 * 4 * nkb) * KBB);
+                __syncwarp();
+                tma_rows(stage0 + st * TILE, ids, first, cnt, tm, nkb, &S.tile_full[st], lane);
             }
             if (!ok) break;
         }
@@ -466,7 +478,9 @@ kcna_status kcna_join_tc_launch(kcna_ctx *c, const JoinArgs &a) {
                              "join_tc smem attr"));
     const uint32_t grid = (uint32_t)std::min<uint64_t>(a.N, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
-    join_tc_kernel<<<grid, WS_THREADS, sm, c->stream>>>(a, c->Xh, (int)c->ld, c->norms, colcap);
+    alignas(64) CUtensorMap tmap;
+    KCNA_TRY(kcna_rows_tmap(c, &tmap));
+    join_tc_kernel<<<grid, WS_THREADS, sm, c->stream>>>(a, tmap, (int)c->ld, c->norms, colcap);
     KCNA_LAUNCHED(c);
     return kcna_cuda_check(c, cudaGetLastError(), "join_tc_kernel");
 }

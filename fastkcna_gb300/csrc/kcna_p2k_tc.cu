@@ -21,14 +21,16 @@
 // join (kcna_join_tc.cu):
 //   warp 0      producer: walks the block's range of nodes, packs tiles, copies
 //               pusher / neighbour ids into the tile stage with cp.async, then
-//               gathers their BF16 rows and radius / norm; a tile with no rows
-//               ends the stream.
+//               gathers their BF16 rows with TMA (tile::gather4) and radius /
+//               norm with cp.async; a tile with no rows ends the stream.
 //   warp 1      MMA issuer: M = 128, N = columns used rounded up to 16.
 //   warps 2-9   epilogue: warp w reads TMEM lanes 32*(w%4).. (pushers) and
 //               every second 16-column group of the span its lanes' nodes
 //               cover; per thread a count pass, one atomicAdd on the pusher's
 //               candidate count, and a write pass reading TMEM again.
 #include <algorithm>
+
+#include <cuda.h>
 
 #include "kcna_internal.h"
 #include "kcna_tc.cuh"
@@ -83,30 +85,37 @@ struct P2kArgs {
 };
 
 // rows of `count` ids (masked to 31 bits) -> a region whose K blocks are
-// `rrows` rows apart; lane-strided cp.async
-__device__ __forceinline__ void gather(uint32_t region, uint32_t rrows, const uint32_t *ids, int count,
-                                       const uint16_t *__restrict__ Xh, int ldh, int nc16, int lane) {
-    for (int idx = lane; idx < count * nc16; idx += 32) {
-        const int r = idx / nc16, c = idx - r * nc16;
-        const uint16_t *src = Xh + (uint64_t)(ids[r] & 0x7FFFFFFFu) * (uint64_t)ldh + c * 8;
-        cp_async16(region + (uint32_t)(c >> 3) * rrows * KBB + sw128_off((uint32_t)r, (uint32_t)(c & 7)), src);
+// `rrows` rows apart, by TMA gather4 (four rows of one K block per
+// instruction; the last group repeats its last row); lane-strided.  Returns
+// the transaction bytes.
+__device__ __forceinline__ uint32_t tma_rows(uint32_t region, uint32_t rrows, const uint32_t *ids, int count,
+                                             const void *tmap, int nkb, uint64_t *bar, int lane) {
+    const int ng = (count + 3) >> 2;
+    for (int e = lane; e < ng * nkb; e += 32) {
+        const int g = nkb == 2 ? e >> 1 : e, kb = nkb == 2 ? e & 1 : 0;
+        const int r = 4 * g, last = count - 1;
+        tma_gather4(region + (uint32_t)kb * rrows * KBB + (uint32_t)r * KBB, tmap, 64 * kb,
+                    (int)(ids[r] & 0x7FFFFFFFu), (int)(ids[min(r + 1, last)] & 0x7FFFFFFFu),
+                    (int)(ids[min(r + 2, last)] & 0x7FFFFFFFu), (int)(ids[min(r + 3, last)] & 0x7FFFFFFFu), bar);
     }
+    return (uint32_t)(ng * 4 * nkb) * KBB;
 }
 
-__global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
+__global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u;
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
     PwShared &S = *reinterpret_cast<PwShared *>(tiles + TS * STAGE);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nc16 = a.ldh >> 3, nkb = (a.ldh + 63) >> 6;
+    const int nkb = (a.ldh + 63) >> 6;
+    const void *tm = &tmap;
 
     for (int i = tid; i < (int)(TS * STAGE / 16); i += PW_THREADS)
         reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
     if (warp == 1) tmem_alloc(&S.tmem, NACC * PN);
     if (tid == 0) {
         for (int i = 0; i < TS; ++i) {
-            mbar_init(&S.tile_full[i], 33); // producer lanes' copies + the producer's metadata
+            mbar_init(&S.tile_full[i], 33); // producer lanes' copies + the producer's expect_tx (metadata, rows)
             mbar_init(&S.tile_empty[i], 9); // MMA commit + epilogue warps
         }
         for (int i = 0; i < NACC; ++i) {
@@ -143,8 +152,6 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
             __syncwarp();
             const uint32_t base = tiles_s + st * STAGE;
-            gather(base, PM, M->row_id, (int)rows, a.Xh, a.ldh, nc16, lane);
-            gather(base + ROWS_A, PN, M->col_id, (int)cols, a.Xh, a.ldh, nc16, lane);
             for (uint32_t i = lane; i < rows; i += 32) {
                 const uint32_t u = M->row_id[i] & 0x7FFFFFFFu;
                 cp_async4(smem_u32(&M->row_rad[i]), a.radius + u);
@@ -166,7 +173,14 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             }
             mbar_arrive_cp_async(&S.tile_full[st]);
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.tile_full[st]);
+            if (lane == 0)
+                mbar_arrive_expect_tx(&S.tile_full[st],
+                                      rows ? (uint32_t)(((rows + 3) / 4 + (cols + 3) / 4) * 4 * nkb) * KBB : 0u);
+            __syncwarp();
+            if (rows) {
+                tma_rows(base, PM, M->row_id, (int)rows, tm, nkb, &S.tile_full[st], lane);
+                tma_rows(base + ROWS_A, PN, M->col_id, (int)cols, tm, nkb, &S.tile_full[st], lane);
+            }
             ++tcount;
         };
         ok = open_tile();
@@ -356,7 +370,9 @@ kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t 
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(p2k_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                              "p2k_tc smem attr"));
     const uint32_t grid = (uint32_t)std::max(c->num_sms, 1);
-    p2k_tc_kernel<<<grid, PW_THREADS, sm, c->stream>>>(a);
+    alignas(64) CUtensorMap tmap;
+    KCNA_TRY(kcna_rows_tmap(c, &tmap));
+    p2k_tc_kernel<<<grid, PW_THREADS, sm, c->stream>>>(a, tmap);
     KCNA_LAUNCHED(c);
     return kcna_cuda_check(c, cudaGetLastError(), "p2k_tc_kernel");
 }

@@ -164,6 +164,19 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uin
                  : "memory");
 }
 
+// TMA row gather (tile::gather4): rows r0..r3 of a 2-D tensor map whose box
+// is 64 elements x 1 row, starting at element column x (a multiple of 64),
+// land as 4 x 128 bytes at dst in the map's 128-byte swizzle; completes
+// 512 transaction bytes on mbar.
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const void *tmap, int x, int r0, int r1, int r2, int r3,
+                                            uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(tmap), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // Named barrier over `count` threads (a multiple of 32), id 1..15.
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
