@@ -378,7 +378,10 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
             const uint32_t kept = run;
             const uint32_t newcnt = min(a.limit, np + kept);
             unsigned long long flagged = 0;
-            for (uint32_t i = lane; i < np; i += 32) {
+            // nothing new (every candidate already in the pool or a repeat): the
+            // pool stays as it is in memory
+            for (uint32_t i = kept ? np : lane; i < np && i < a.K; i += 32) flagged += (s_pool[i] & KCNA_FLAG_NEW) ? 1 : 0;
+            for (uint32_t i = kept ? lane : np; i < np; i += 32) {
                 uint64_t k = s_pool[i];
                 int lb = kcna_lower_bound(s_c, cp, kcna_key_noflags(k));
                 uint32_t r = i + s_keep[lb];
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                     if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
                 }
             }
-            for (int j = lane; j < cp; j += 32) {
+            for (int j = kept ? lane : cp; j < cp; j += 32) {
                 if (s_keep[j + 1] == s_keep[j]) continue;
                 uint64_t k = s_c[j];
                 uint32_t r = s_keep[j] + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
@@ -406,8 +409,8 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
                 a.pool_cnt[node] = newcnt;
                 a.cand_cnt[node] = 0;
-                a.radius[node] =
-                    newcnt >= a.limit ? kcna_key_dist(gp[a.limit - 1]) : __uint_as_float(0x7F800000u);
+                a.radius[node] = newcnt >= a.limit ? kcna_key_dist(kept ? gp[a.limit - 1] : s_pool[a.limit - 1])
+                                                   : __uint_as_float(0x7F800000u);
             }
         }
     }
@@ -512,6 +515,23 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
         for (uint32_t i = threadIdx.x; i <= np; i += MT) s_off[i] = s_hist[i];
         __syncthreads();
         const uint32_t total = block_exclusive_scan(s_off, (int)np + 1, s_warp); // s_off[np+1] = total
+        if (total == 0) { // nothing new: the pool stays as it is in memory
+            unsigned long long f = 0;
+            for (uint32_t i = threadIdx.x; i < np && i < a.K; i += MT) f += (s_pool[i] & KCNA_FLAG_NEW) ? 1 : 0;
+            f = kcna_warp_sum(f);
+            if ((threadIdx.x & 31) == 0 && f) atomicAdd(&s_flagged, f);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                atomicAdd(a.counters + 1, s_flagged);
+                if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
+                atomicAdd(a.counters + 7, (unsigned long long)nc);
+                atomicAdd(a.counters + 9, (unsigned long long)np);
+                a.pool_cnt[node] = np;
+                a.cand_cnt[node] = 0;
+                a.radius[node] = np >= a.limit ? kcna_key_dist(s_pool[a.limit - 1]) : __uint_as_float(0x7F800000u);
+            }
+            continue;
+        }
         for (uint32_t i = threadIdx.x; i <= np; i += MT) s_hist[i] = 0;
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < nc; j += MT) {
