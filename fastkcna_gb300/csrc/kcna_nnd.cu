@@ -320,20 +320,25 @@ struct MergeArgs {
     unsigned long long *counters; // [1] flagged in top-K, [2] overflow, [3] inserted
 };
 
-// Warp-per-node merge for nodes with at most MW_SMALL candidates (most nodes
-// in late NN-descent iterations and in every P2K round).  Nodes with more
-// candidates are queued for merge_big_kernel.  Same result as the block merge.
-constexpr int MW_WARPS = 8, MW_SMALL = 256;
+// Warp-per-node merge, survivors first.  Every candidate is looked up in the
+// node's sorted pool by binary search (shared memory): a candidate equal to a
+// pool entry, or one that would land at rank >= limit, is dropped.  In a
+// converging NN-descent almost every candidate is such a repeat, so only the
+// few survivors are sorted, deduplicated and merged, and only the pool entries
+// they displace are written.  A node with more than MW_SURV survivors is
+// queued for the block merge (merge_kernel).  Same result as merging all
+// candidates.
+constexpr int MW_WARPS = 8, MW_SURV = 512;
 
 __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, uint32_t N, uint32_t *big_list,
                                                                   uint32_t *big_cnt) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
-    const size_t per_warp = (size_t)MW_SMALL * 8 + (size_t)a.cap * 8 + (MW_SMALL + 1) * 4;
-    unsigned char *base = smem + w * ((per_warp + 15) & ~(size_t)15);
-    uint64_t *s_c = reinterpret_cast<uint64_t *>(base);
-    uint64_t *s_pool = s_c + MW_SMALL;
-    uint32_t *s_keep = reinterpret_cast<uint32_t *>(s_pool + a.cap);
+    const size_t per_warp = ((size_t)a.cap * 8 + (size_t)MW_SURV * 8 + 16 + 15) & ~(size_t)15;
+    unsigned char *base = smem + w * per_warp;
+    uint64_t *s_pool = reinterpret_cast<uint64_t *>(base);
+    uint64_t *s_sv = s_pool + a.cap;         // survivors (keys without flags)
+    uint64_t *s_last = s_sv + MW_SURV;       // key landing at rank limit-1
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
     if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
     __syncthreads();
@@ -343,60 +348,77 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
-        if (nc > (uint32_t)MW_SMALL) {
+        const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+        for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
+        __syncwarp();
+        // survivors: not in the pool, landing below limit
+        uint32_t ns = 0;
+        for (uint32_t b0 = 0; b0 < nc; b0 += 32) {
+            const uint32_t j = b0 + lane;
+            bool surv = false;
+            uint64_t k = 0;
+            if (j < nc) {
+                k = kcna_key_noflags(gc[j]);
+                if (k != KCNA_EMPTY_KEY_NOFLAGS) {
+                    const int b = kcna_lower_bound(s_pool, (int)np, k);
+                    surv = (uint32_t)b < a.limit && !(b < (int)np && (s_pool[b] >> 2) == (k >> 2));
+                }
+            }
+            const unsigned m = __ballot_sync(KCNA_FULL, surv);
+            const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
+            if (surv && pos < (uint32_t)MW_SURV) s_sv[pos] = k;
+            ns += __popc(m);
+        }
+        if (ns > (uint32_t)MW_SURV) {
             if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = node;
-        } else if (nc == 0) {
-            unsigned long long f = 0;
-            for (uint32_t i = lane; i < min(np, a.K); i += 32) f += (gp[i] & KCNA_FLAG_NEW) ? 1 : 0;
-            f = kcna_warp_sum(f);
-            if (lane == 0 && f) atomicAdd(&s_stat[0], f);
         } else {
-            for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
-            const int cp = kcna_pow2_ceil_d((int)nc);
-            const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
-            for (int i = lane; i < cp; i += 32) s_c[i] = i < (int)nc ? kcna_key_noflags(gc[i]) : KCNA_EMPTY_KEY;
-            kcna_warp_bitonic(s_c, cp);
-            // keep flags + exclusive scan, 32 at a time
-            uint32_t run = 0;
-            for (int b0 = 0; b0 < cp; b0 += 32) {
-                const int j = b0 + lane;
-                bool keep = false;
-                if (j < cp) {
-                    uint64_t k = s_c[j];
-                    keep = k != KCNA_EMPTY_KEY && (j == 0 || (s_c[j - 1] >> 2) != (k >> 2));
-                    if (keep) {
-                        int lb = kcna_lower_bound(s_pool, (int)np, k);
-                        if (lb < (int)np && (s_pool[lb] >> 2) == (k >> 2)) keep = false;
-                    }
+            uint32_t nu = 0; // distinct survivors
+            if (ns > 0) {
+                const int p2 = kcna_pow2_ceil_d((int)ns);
+                for (int i = (int)ns + lane; i < p2; i += 32) s_sv[i] = KCNA_EMPTY_KEY;
+                __syncwarp();
+                kcna_warp_bitonic(s_sv, p2);
+                // drop repeats among survivors (same distance and id are adjacent);
+                // compaction moves entries down, so the previous key comes from
+                // registers, not from the array being rewritten
+                uint64_t carry = KCNA_EMPTY_KEY;
+                for (uint32_t b0 = 0; b0 < ns; b0 += 32) {
+                    const uint32_t j = b0 + lane;
+                    const uint64_t k = j < ns ? s_sv[j] : KCNA_EMPTY_KEY;
+                    uint64_t prev = __shfl_up_sync(KCNA_FULL, k, 1);
+                    if (lane == 0) prev = carry;
+                    const bool keep = j < ns && (j == 0 || (prev >> 2) != (k >> 2));
+                    const unsigned m = __ballot_sync(KCNA_FULL, keep);
+                    carry = __shfl_sync(KCNA_FULL, k, 31);
+                    __syncwarp();
+                    if (keep) s_sv[nu + __popc(m & kcna_lanemask_lt())] = k;
+                    nu += __popc(m);
+                    __syncwarp();
                 }
-                unsigned mk = __ballot_sync(KCNA_FULL, keep);
-                if (j < cp) s_keep[j] = run + __popc(mk & kcna_lanemask_lt());
-                run += __popc(mk);
             }
-            if (lane == 0) s_keep[cp] = run;
-            __syncwarp();
-            const uint32_t kept = run;
-            const uint32_t newcnt = min(a.limit, np + kept);
+            const uint32_t newcnt = min(a.limit, np + nu);
             unsigned long long flagged = 0;
-            // nothing new (every candidate already in the pool or a repeat): the
-            // pool stays as it is in memory
-            for (uint32_t i = kept ? np : lane; i < np && i < a.K; i += 32) flagged += (s_pool[i] & KCNA_FLAG_NEW) ? 1 : 0;
-            for (uint32_t i = kept ? lane : np; i < np; i += 32) {
-                uint64_t k = s_pool[i];
-                int lb = kcna_lower_bound(s_c, cp, kcna_key_noflags(k));
-                uint32_t r = i + s_keep[lb];
+            if (lane == 0) *s_last = KCNA_EMPTY_KEY;
+            __syncwarp();
+            // pool entries: shifted by the survivors below them
+            for (uint32_t i = lane; i < np; i += 32) {
+                const uint64_t k = s_pool[i];
+                const uint32_t sh = nu ? (uint32_t)kcna_lower_bound(s_sv, (int)nu, kcna_key_noflags(k)) : 0u;
+                const uint32_t r = i + sh;
                 if (r < newcnt) {
-                    gp[r] = k;
+                    if (sh) gp[r] = k;
                     if (r < a.K && (k & KCNA_FLAG_NEW)) ++flagged;
+                    if (r + 1 == a.limit) *s_last = k;
                 }
             }
-            for (int j = kept ? lane : cp; j < cp; j += 32) {
-                if (s_keep[j + 1] == s_keep[j]) continue;
-                uint64_t k = s_c[j];
-                uint32_t r = s_keep[j] + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
+            // survivors at their rank
+            for (uint32_t j = lane; j < nu; j += 32) {
+                const uint64_t k = s_sv[j];
+                const uint32_t r = j + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
                 if (r < newcnt) {
                     gp[r] = k | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
                     if (r < a.K) ++flagged;
+                    if (r + 1 == a.limit) *s_last = k;
                 }
             }
             flagged = kcna_warp_sum(flagged);
@@ -409,8 +431,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
                 a.pool_cnt[node] = newcnt;
                 a.cand_cnt[node] = 0;
-                a.radius[node] = newcnt >= a.limit ? kcna_key_dist(kept ? gp[a.limit - 1] : s_pool[a.limit - 1])
-                                                   : __uint_as_float(0x7F800000u);
+                a.radius[node] = newcnt >= a.limit ? kcna_key_dist(*s_last) : __uint_as_float(0x7F800000u);
             }
         }
     }
@@ -932,7 +953,7 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "merge smem attr"));
-    const size_t smw = (((size_t)MW_SMALL * 8 + (size_t)c->cap * 8 + (MW_SMALL + 1) * 4 + 15) & ~(size_t)15) * MW_WARPS;
+    const size_t smw = (((size_t)c->cap * 8 + (size_t)MW_SURV * 8 + 16 + 15) & ~(size_t)15) * MW_WARPS;
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(smw, 48 * 1024)),
                              "merge smem attr"));
