@@ -12,6 +12,7 @@
 //   UpdateNhoods :3537-3584                -> update_nhoods_kernel
 //   BridgeView :2478-2663                  -> bridge_* kernels + the shared merge
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <random>
 #include <set>
@@ -993,16 +994,20 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     const size_t sm = (size_t)PW * 2 * range * 4;
     const int maxc = (int)std::min(p->search_K, c->cap);
     KCNA_TRY(kcna_phase_begin(c));
-    if (c->Xh)
-        prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
-            RowsB16{c->Xh, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
-            c->g_dist, c->g_deg, c->W, c->counters + 16);
-    else
-        prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
-            RowsF32{c->X, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
-            c->g_dist, c->g_deg, c->W, c->counters + 16);
-    KCNA_LAUNCHED(c);
-    KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
+    if (getenv("KCNA_PRUNE_TC") && kcna_prune_tc_ok(c, (int)range)) { // Gram-tile prune: opt-in while it is slower
+        KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, rule.thr, (int)range, maxc, c->counters + 16));
+    } else {
+        if (c->Xh)
+            prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+                RowsB16{c->Xh, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
+                c->g_dist, c->g_deg, c->W, c->counters + 16);
+        else
+            prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+                RowsF32{c->X, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
+                c->g_dist, c->g_deg, c->W, c->counters + 16);
+        KCNA_LAUNCHED(c);
+        KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
+    }
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_PRUNE));
     unsigned long long h = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 16, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));

@@ -138,6 +138,10 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr);
 // TMA tensor map (128 bytes, a CUtensorMap) of the BF16 rows (kcna_tmap.cu).
 kcna_status kcna_rows_tmap(kcna_ctx *c, void *out128);
+// Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
+bool kcna_prune_tc_ok(const kcna_ctx *c, int range);
+kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
+                                 unsigned long long *comps);
 // P2K join on tcgen05 Gram tiles (kcna_p2k_tc.cu); requires c->gram_exact.
 kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, unsigned long long *comps);
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);
