@@ -197,28 +197,35 @@ def run_reference(args, ws, rank):
     }), flush=True)
 
 
-def roofline(st, hbm_gbs, ld):
-    """Dominant device phase with its algorithmic bytes per launch."""
+def roofline(st, hbm_gbs, ld, n, search_k):
+    """Dominant device phase with its algorithmic bytes per launch.
+
+    join:  every gathered row once (BF16 or FP32) + every candidate key written once
+    merge: candidates read once, pool entries read and written once
+    prune: every candidate row of every node read once (min(pool, search_K) rows)
+    """
     ph, launches = st["phase_ms"], st["phase_launches"]
+    rb = 2 if st["bf16_rows"] else 4
     models = {
-        # join: every gathered row once + every candidate written once
-        "join": st["join_rows"] * ld * 4 + st["cand_emitted"] * 8,
-        # merge: candidates read once, pool entries read and written once
+        "join": st["join_rows"] * ld * rb + st["cand_emitted"] * 8,
         "merge": st["cand_merged"] * 8 + st["pool_entries_merged"] * 16,
+        "prune": launches["prune"] * n * min(search_k, st["maxl"]) * ld * rb,
     }
+    kernels = {"join": "join_tc_kernel" if st["gram_tc"] else "join_kernel", "merge": "merge_warp_kernel",
+               "prune": "prune_kernel"}
     name = max(models, key=lambda k: ph.get(k, 0.0))
     ms, nl = ph[name], max(launches[name], 1)
     per_launch_bytes = models[name] / nl
     per_launch_s = ms / 1000.0 / nl
     achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     return name, {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
-                  "frac": round(achieved / hbm_gbs, 4), "traffic": traffic_from_profile(name),
-                  "kernel": f"{name}_kernel", "launches_per_step": int(nl)}
+                  "frac": round(achieved / hbm_gbs, 4), "traffic": traffic_from_profile(kernels[name]),
+                  "kernel": kernels[name], "phase": name, "launches_per_step": int(nl)}
 
 
 def traffic_from_profile(name):
     """DRAM bytes per launch from the committed ncu summary, when present."""
-    path = os.path.join(ROOT, "profiles", f"{name}_kernel_c2.txt")
+    path = os.path.join(ROOT, "profiles", f"{name}_c2.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch_full_size:"):
@@ -300,7 +307,7 @@ def run_gpu(args, ws, rank, local):
     e2e_s = max_over_ranks(ws, statistics.median(e2e))
     st = stats[-1]
     hbm, bf16, src = peaks()
-    kname, roof = roofline(st, hbm, (X.shape[1] + 3) // 4 * 4)
+    kname, roof = roofline(st, hbm, (X.shape[1] + 3) // 4 * 4, n, FLAGS["search_K"])
     roof["peak_source"] = f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
     final_recall = st["loop_recall"][-1]
     line = {

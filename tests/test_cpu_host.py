@@ -153,3 +153,21 @@ def test_bench_two_rank_gloo_max_over_ranks():
         p.join(120)
     got = sorted(q.get(timeout=5) for _ in ps)
     assert got == [(0, 11.0), (1, 11.0)]
+
+
+def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
+    import bench
+
+    st = {"phase_ms": {"join": 300.0, "merge": 100.0, "prune": 200.0}, "phase_launches": {"join": 6, "merge": 10, "prune": 3},
+          "bf16_rows": 1, "gram_tc": 1, "join_rows": 6_000_000, "cand_emitted": 1_000_000, "cand_merged": 2_000_000,
+          "pool_entries_merged": 500_000, "maxl": 500}
+    name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
+    assert name == "join" and r["kernel"] == "join_tc_kernel" and r["launches_per_step"] == 6
+    per_launch = (6_000_000 * 128 * 2 + 1_000_000 * 8) / 6
+    assert r["achieved"] == pytest.approx(per_launch / (0.3 / 6) / 1e9, abs=0.06)  # rounded to 0.1 GB/s
+    assert r["frac"] == pytest.approx(r["achieved"] / 6782.4, abs=1e-4)
+    st["phase_ms"]["prune"] = 400.0
+    st["bf16_rows"] = 0
+    name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
+    assert name == "prune" and r["kernel"] == "prune_kernel"
+    assert r["achieved"] == pytest.approx((3 * 1000 * 500 * 128 * 4 / 3) / (0.4 / 3) / 1e9, abs=0.06)
