@@ -19,8 +19,9 @@
 //      occluded by an earlier kept one is dead;
 //   3. Gram tile chunk x chunk: thread p builds the 128-bit mask of the
 //      earlier chunk candidates that would occlude it;
-//   4. one thread scans the chunk in order: p is kept when alive and no kept
-//      chunk candidate is in its mask; the scan stops at range;
+//   4. one warp scans the chunk in order, a mask word at a time: p is kept
+//      when alive and no kept chunk candidate is in its mask; the scan stops
+//      at range;
 //   5. the newly kept rows are copied into the kept tile for the next chunk.
 // Waits are bounded; a wait that gives up sets the error word and ends the
 // block after its products have finished.
@@ -67,7 +68,7 @@ __device__ __forceinline__ bool occl(int kind, float t3, float thr, float td, fl
     return djk < pd;
 }
 
-__global__ void __launch_bounds__(PT) prune_tc_kernel(PruneTcArgs a, const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(PT, 3) prune_tc_kernel(PruneTcArgs a, const __grid_constant__ CUtensorMap tmap,
                                                       int ldh) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ uint64_t bar_rows, bar_mma;
@@ -221,32 +222,48 @@ __global__ void __launch_bounds__(PT) prune_tc_kernel(PruneTcArgs a, const __gri
                 fence_before();
                 __syncthreads();
                 fence_after();
-                // 4. the scan, in candidate order
-                if (tid == 0) {
-                    uint32_t k0 = 0u, k1 = 0u, k2 = 0u, k3 = 0u; // kept chunk candidates
+                // 4. the scan, in candidate order, by warp 0: 32 candidates (one word
+                // of the masks) at a time; lane p first tests the kept words of
+                // earlier blocks, then the block is resolved in order with the
+                // block's own mask word broadcast lane by lane
+                if (warp == 0) {
+                    uint32_t kw0 = 0u, kw1 = 0u, kw2 = 0u, kw3 = 0u; // kept chunk candidates
                     int nkl = nk, newk = 0;
-                    for (int p = 0; p < m && nkl < a.range; ++p) {
-                        const int wp = p >> 5;
-                        const uint32_t bit = 1u << (p & 31);
-                        const bool al_p = (s_alive[wp] & bit) != 0u;
-                        if (c0 + p != first) { // the first candidate is always kept
-                            if (!al_p) continue;
-                            const uint4 mk4 = *reinterpret_cast<const uint4 *>(s_mask[p]);
-                            if ((mk4.x & k0) | (mk4.y & k1) | (mk4.z & k2) | (mk4.w & k3)) continue;
+                    for (int b = 0; b * 32 < m && nkl < a.range; ++b) {
+                        const int p = 32 * b + lane;
+                        const bool is_first = c0 + p == first;
+                        const bool al_p = p < m && (is_first || ((s_alive[b] >> lane) & 1u));
+                        const uint4 mk4 = *reinterpret_cast<const uint4 *>(s_mask[min(p, PT - 1)]);
+                        const bool pre = ((mk4.x & kw0) | (mk4.y & kw1) | (mk4.z & kw2) | (mk4.w & kw3)) == 0u;
+                        const uint32_t own = b == 0 ? mk4.x : b == 1 ? mk4.y : b == 2 ? mk4.z : mk4.w;
+                        const unsigned cand = __ballot_sync(KCNA_FULL, al_p && pre);
+                        uint32_t kb = 0u;
+                        int cnt = nkl;
+                        for (int i = 0; i < 32; ++i) {
+                            const uint32_t wi = __shfl_sync(KCNA_FULL, own, i);
+                            if (((cand >> i) & 1u) && !(wi & kb) && cnt < a.range) {
+                                kb |= 1u << i;
+                                ++cnt;
+                            }
                         }
-                        k0 |= wp == 0 ? bit : 0u;
-                        k1 |= wp == 1 ? bit : 0u;
-                        k2 |= wp == 2 ? bit : 0u;
-                        k3 |= wp == 3 ? bit : 0u;
-                        k_id[nkl] = s_id[p];
-                        k_pd[nkl] = s_pd[p];
-                        k_nrm[nkl] = s_nrm[p];
-                        s_kfrom[newk] = p;
-                        ++nkl;
-                        ++newk;
+                        if ((kb >> lane) & 1u) {
+                            const int r = __popc(kb & kcna_lanemask_lt());
+                            k_id[nkl + r] = s_id[p];
+                            k_pd[nkl + r] = s_pd[p];
+                            k_nrm[nkl + r] = s_nrm[p];
+                            s_kfrom[newk + r] = p;
+                        }
+                        if (b == 0) kw0 = kb;
+                        if (b == 1) kw1 = kb;
+                        if (b == 2) kw2 = kb;
+                        if (b == 3) kw3 = kb;
+                        nkl += __popc(kb);
+                        newk += __popc(kb);
                     }
-                    s_nk = nkl;
-                    s_newk = newk;
+                    if (lane == 0) {
+                        s_nk = nkl;
+                        s_newk = newk;
+                    }
                 }
                 __syncthreads();
                 // 5. newly kept rows into the kept tile (rows nk.., swizzled like the chunk)
@@ -309,6 +326,9 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int
     const size_t sm = 1024 + CHUNK + KEPT;
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                              "prune_tc smem attr"));
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                     (int)cudaSharedmemCarveoutMaxShared),
+                             "prune_tc carveout"));
     int per_sm = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prune_tc_kernel, PT, sm),
                              "prune_tc occupancy"));
