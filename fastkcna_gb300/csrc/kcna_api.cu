@@ -18,6 +18,8 @@
 #include <set>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "kcna_common.cuh"
 #include "kcna_internal.h"
 
@@ -199,7 +201,25 @@ static void release_row_copies(kcna_ctx *c) {
     if (c->norms) cudaFree(c->norms);
     c->Xh = nullptr;
     c->norms = nullptr;
-    c->gram_exact = false;
+    c->gram_exact = c->bf16_exact = c->bf16_screen = false;
+}
+
+// BF16 copy rounded to nearest (even) and the squared norms of the rounded
+// rows, for screening inexact data; warp per row.
+__global__ void bf16_round_kernel(const float *__restrict__ X, uint32_t n, uint32_t ld, uint16_t *__restrict__ Xh,
+                                  float *__restrict__ norms) {
+    const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    float acc = 0.f;
+    for (uint32_t k = lane; k < ld; k += 32) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(X[row * ld + k]);
+        Xh[row * ld + k] = *reinterpret_cast<const uint16_t *>(&b);
+        const float v = __bfloat162float(b);
+        acc = fmaf(v, v, acc);
+    }
+    acc = kcna_warp_sum(acc);
+    if (lane == 0) norms[row] = acc;
 }
 
 // BF16 mode: when every value of the rows is exactly representable in BF16,
@@ -220,8 +240,19 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     unsigned long long bad = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&bad, c->counters + 40, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bf16 check"));
-    if (bad) return KCNA_OK; // inexact data: FP32 rows
+    if (bad) { // inexact data: FP32 rows everywhere; the join screens on a rounded copy
+        if ((c->ld & 7u) || c->ld > 128) return KCNA_OK;
+        KCNA_TRY(kcna_alloc(c, &c->Xh, n, "bf16 rows (rounded)"));
+        KCNA_TRY(kcna_alloc(c, &c->norms, c->n_total, "row norms"));
+        bf16_round_kernel<<<kcna_div_up((uint64_t)c->n_total * 32, 256), 256, 0, c->stream>>>(c->X, c->n_total, c->ld,
+                                                                                              c->Xh, c->norms);
+        KCNA_LAUNCHED(c);
+        c->bf16_screen = true;
+        if (gram) *gram = 2;
+        return kcna_cuda_check(c, cudaGetLastError(), "bf16 round");
+    }
     KCNA_TRY(kcna_alloc(c, &c->Xh, n, "bf16 rows"));
+    c->bf16_exact = true;
     bf16_copy_kernel<<<kcna_div_up(n, 256), 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n, c->Xh);
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "bf16 copy"));

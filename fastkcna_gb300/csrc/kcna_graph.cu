@@ -997,7 +997,7 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     if (getenv("KCNA_PRUNE_TC") && kcna_prune_tc_ok(c, (int)range)) { // Gram-tile prune: opt-in while it is slower
         KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, rule.thr, (int)range, maxc, c->counters + 16));
     } else {
-        if (c->Xh)
+        if (c->bf16_exact)
             prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
                 RowsB16{c->Xh, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
                 c->g_dist, c->g_deg, c->W, c->counters + 16);
@@ -1048,7 +1048,7 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     KCNA_LAUNCHED(c);
     PruneRule rule = make_rule(p, kind);
     cudaMemsetAsync(c->counters + 17, 0, 8, c->stream);
-    if (c->Xh)
+    if (c->bf16_exact)
         link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(RowsB16{c->Xh, (int)c->ld}, (uint32_t)N, rule,
                                                              (int)p->nsg_R, c->g_ids, c->g_dist, c->g_deg, W, off, rev,
                                                              c->counters + 17, c->d_err);
@@ -1330,7 +1330,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
         if (c->gram_exact && c->W <= 256) {
             if ((s = kcna_p2k_tc_launch(c, off, rnn, c->counters + 21)) != KCNA_OK) return cleanup(), s;
-        } else if (c->Xh) {
+        } else if (c->bf16_exact) {
             const RowsB16 rows{c->Xh, (int)c->ld};
             p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
                 rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,

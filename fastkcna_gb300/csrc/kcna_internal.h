@@ -32,6 +32,12 @@ struct kcna_ctx {
     // then runs on tcgen05 Gram tiles.  norms[i] = |x_i|^2 (n_total floats).
     bool gram_exact = false;
     float *norms = nullptr;
+    // bf16_exact: Xh holds the rows' values exactly (kernels may read it in
+    // place of X).  bf16_screen: the rows are not exact in BF16; Xh holds them
+    // rounded to nearest and norms their squared norms, and the local join
+    // screens pairs on Gram tiles of the rounded rows with a bound on the
+    // rounding error, then recomputes every emitted pair in FP32 (rescore).
+    bool bf16_exact = false, bf16_screen = false;
 
     // candidate pools: n x cap keys (kcna_common.cuh), counts, filter radius
     uint32_t cap = 0;

@@ -59,8 +59,8 @@ constexpr int TROWS = 128;                    // set rows per tile (MMA M), max 
 constexpr uint32_t KBB = 128;                 // bytes of a row inside one 64-element K block
 constexpr uint32_t TILE = TROWS * KBB * 2;    // 128 rows, two K blocks (d <= 128): 32 KiB
 constexpr int NS = 2;                         // node slots
-constexpr int TS = 4;                         // tile row stages (released by the MMA)
-constexpr int MS = 8;                         // tile metadata entries (released by the epilogue)
+constexpr int TS = 3;                         // tile row stages (released by the MMA)
+constexpr int MS = 6;                         // tile metadata entries (released by the epilogue)
 constexpr int NACC = 4;                       // TMEM accumulators of 128 columns
 constexpr int NR = 4;                         // raw list entries (prefetched two nodes ahead)
 
@@ -91,6 +91,9 @@ struct WsShared {
     unsigned emit[NS], done[NS];
     float a_rad[NS][TROWS], a_nrm[NS][TROWS];
     float t_rad[MS][TROWS], t_nrm[MS][TROWS];
+    // screening bound terms (BF16 screen mode): sqrt(radius (1 + 2^-15)) and
+    // the norm of the rounded row
+    float a_rr[NS][TROWS], a_aa[NS][TROWS], t_rr[MS][TROWS], t_aa[MS][TROWS];
 };
 
 // rows [first, first+count) of ids -> rows 0..count-1 of a 128-row region by
@@ -119,9 +122,24 @@ __device__ __forceinline__ void issue_tile(uint32_t tmem_d, uint32_t a_base, uin
                      desc_sw128(b_base + kb * TROWS * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
 }
 
+// Screening bound of a rounded-row Gram distance (BF16 screen mode): with
+// x~ the rows rounded to BF16 (relative error <= 2^-8 per element), a pair
+// whose FP32 distance is <= radius has Gram distance
+//   ds <= (sqrt(radius (1 + 2^-15)) + 2^-7 (|x~_i| + |x~_j|))^2 + 2^-14 (|x~_i|^2 + |x~_j|^2)
+// (rounding of the rows, of the FP32 chain and of the FP32 accumulation, each
+// bound doubled).  Pairs below the bound are emitted and recomputed in FP32.
+constexpr float SCREEN_CE = 0.0078125f;     // 2^-7
+constexpr float SCREEN_CG = 6.103515625e-05f; // 2^-14
+__device__ __forceinline__ float screen_bound(float rr, float aa_sum, float nn_sum) {
+    const float t = __fmaf_rn(SCREEN_CE, aa_sum, rr);
+    return __fmaf_rn(t, t, SCREEN_CG * nn_sum);
+}
+
+template <bool SCREEN>
 __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, const __grid_constant__ CUtensorMap tmap,
                                                                 int ldh, const float *__restrict__ norms,
-                                                                uint32_t colcap) {
+                                                                const float *__restrict__ rr,
+                                                                const float *__restrict__ aa, uint32_t colcap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u; // swizzled tiles need 1024-byte alignment
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
@@ -242,6 +260,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
             for (uint32_t i = lane; i < na; i += 32) {
                 cp_async4(smem_u32(&S.a_rad[sl][i]), a.radius + ids[i]);
                 cp_async4(smem_u32(&S.a_nrm[sl][i]), norms + ids[i]);
+                if (SCREEN) {
+                    cp_async4(smem_u32(&S.a_rr[sl][i]), rr + ids[i]);
+                    cp_async4(smem_u32(&S.a_aa[sl][i]), aa + ids[i]);
+                }
             }
             // padding columns na..NA-1: a NaN norm makes every distance NaN, so no pair passes
             for (uint32_t i = na + lane; i < ((na + 15) & ~15u); i += 32) {
@@ -264,6 +286,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                 for (int i = lane; i < cnt; i += 32) {
                     cp_async4(smem_u32(&S.t_rad[mt][i]), a.radius + ids[first + i]);
                     cp_async4(smem_u32(&S.t_nrm[mt][i]), norms + ids[first + i]);
+                    if (SCREEN) {
+                        cp_async4(smem_u32(&S.t_rr[mt][i]), rr + ids[first + i]);
+                        cp_async4(smem_u32(&S.t_aa[mt][i]), aa + ids[first + i]);
+                    }
                 }
                 mbar_arrive_cp_async(&S.meta_full[mt]);
                 if (tcount >= (uint32_t)TS && !mbar_wait(&S.tile_empty[st], ((tcount / TS) - 1) & 1)) {
@@ -326,7 +352,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
     } else {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column-group phase (0..3)
-        const int rr = 32 * q + lane;                // this thread's row of a tile
+        const int rw = 32 * q + lane;                // this thread's row of a tile
         unsigned long long emitted = 0;
         uint32_t tcount = 0;
         int k = 0;
@@ -343,12 +369,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                 const int mt = (int)(tcount % MS), b = (int)(tcount % NACC);
                 mine = mbar_wait(&S.acc_full[b], (tcount / NACC) & 1) && mbar_wait(&S.meta_full[mt], (tcount / MS) & 1);
                 fence_after();
-                const int j = t * TROWS + rr; // set member
+                const int j = t * TROWS + rw; // set member
                 const bool warp_live = t * TROWS + 32 * q < ncol && h < G;
                 const bool rowv = j < ncol && mine;
                 const uint32_t id_j = rowv ? ids[j] : 0u;
-                const float rad_j = rowv ? S.t_rad[mt][rr] : 0.f;
-                const float n_j = rowv ? S.t_nrm[mt][rr] : __uint_as_float(0x7FC00000u); // NaN: no pair passes
+                const float rad_j = rowv ? S.t_rad[mt][rw] : 0.f;
+                const float n_j = rowv ? S.t_nrm[mt][rw] : __uint_as_float(0x7FC00000u); // NaN: no pair passes
+                const float rr_j = SCREEN && rowv ? S.t_rr[mt][rw] : 0.f, aa_j = SCREEN && rowv ? S.t_aa[mt][rw] : 0.f;
+                const float *arr = S.a_rr[sl], *aaa = S.a_aa[sl];
                 // rows of the new list meet only earlier new-list columns (each pair once)
                 const bool tri = t == 0 && 32 * q < na;
                 const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TROWS);
@@ -364,8 +392,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
 #pragma unroll
                         for (int u = 0; u < 16; ++u) {
                             const int i = 16 * g + u; // new-list column
-                            const float dd = __fsub_rn(__fadd_rn(n_j, anrm[i]), 2.f * __uint_as_float(raw[u]));
-                            bool rp = dd <= rad_j, cp = dd <= arad[i];
+                            const float nn = __fadd_rn(n_j, anrm[i]);
+                            const float dd = __fsub_rn(nn, 2.f * __uint_as_float(raw[u]));
+                            bool rp, cp;
+                            if (SCREEN) {
+                                const float as = __fadd_rn(aa_j, aaa[i]);
+                                rp = dd <= screen_bound(rr_j, as, nn);
+                                cp = dd <= screen_bound(arr[i], as, nn);
+                            } else {
+                                rp = dd <= rad_j;
+                                cp = dd <= arad[i];
+                            }
                             if (tri && i >= j) rp = cp = false;
                             if ((rp || cp) && ids[i] == id_j) rp = cp = false; // an id in both lists
                             rmask |= (uint32_t)rp << (16 * kk + u);
@@ -403,8 +440,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                             const unsigned m = __shfl_sync(KCNA_FULL, cm, c);
                             const uint32_t cbc = __shfl_sync(KCNA_FULL, cb, c);
                             if (((gm >> u) & 1u) || ((m >> lane) & 1u)) {
-                                const float dd =
-                                    __fsub_rn(__fadd_rn(n_j, anrm[i]), 2.f * __uint_as_float(raw[u]));
+                                // emitted with the Gram distance (exact in Gram-exact mode;
+                                // recomputed in FP32 by the rescore in screen mode)
+                                const float dd = fmaxf(
+                                    __fsub_rn(__fadd_rn(n_j, anrm[i]), 2.f * __uint_as_float(raw[u])), 0.f);
                                 if ((gm >> u) & 1u) {
                                     if (p < a.CB) dst[p] = kcna_key(dd, ids[i], flags);
                                     ++p;
@@ -468,19 +507,42 @@ bool kcna_join_tc_fits(const JoinArgs &a) {
     return join_tc_smem(a) <= 227 * 1024 && !((a.fwd_new_cap | a.fwd_old_cap | a.RB) & 3u);
 }
 
+// sqrt(radius (1 + 2^-15)) and sqrt(norm) for the screening bound
+__global__ void screen_terms_kernel(const float *__restrict__ radius, const float *__restrict__ norms, uint32_t n,
+                                    float *__restrict__ rr, float *__restrict__ aa) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rr[i] = __fsqrt_ru(__fmul_ru(radius[i], 1.000030517578125f));
+    aa[i] = __fsqrt_ru(norms[i]);
+}
+
 kcna_status kcna_join_tc_launch(kcna_ctx *c, const JoinArgs &a) {
-    if (!c->gram_exact || !c->Xh || !c->norms || (c->ld & 7u) || c->ld > 128)
-        return kcna_fail(c, KCNA_E_STATE, "Gram-tile join needs exact BF16 rows with d <= 128");
+    if (!(c->gram_exact || c->bf16_screen) || !c->Xh || !c->norms || (c->ld & 7u) || c->ld > 128)
+        return kcna_fail(c, KCNA_E_STATE, "Gram-tile join needs BF16 rows with d <= 128");
     const uint32_t colcap = std::max<uint32_t>(a.capA, TROWS + a.capB);
     if (!kcna_join_tc_fits(a)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile join: lists too long for shared memory");
     const size_t sm = join_tc_smem(a);
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sm),
+                             "join_tc smem attr"));
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(join_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sm),
                              "join_tc smem attr"));
     const uint32_t grid = (uint32_t)std::min<uint64_t>(a.N, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
     alignas(64) CUtensorMap tmap;
     KCNA_TRY(kcna_rows_tmap(c, &tmap));
-    join_tc_kernel<<<grid, WS_THREADS, sm, c->stream>>>(a, tmap, (int)c->ld, c->norms, colcap);
+    if (c->bf16_screen) {
+        float *rr = nullptr, *aa = nullptr;
+        KCNA_TRY(kcna_scratch(c, (size_t)c->n * 8, reinterpret_cast<void **>(&rr)));
+        aa = rr + c->n;
+        screen_terms_kernel<<<kcna_div_up(c->n, 256), 256, 0, c->stream>>>(a.radius, c->norms, c->n, rr, aa);
+        KCNA_LAUNCHED(c);
+        join_tc_kernel<true><<<grid, WS_THREADS, sm, c->stream>>>(a, tmap, (int)c->ld, c->norms, rr, aa, colcap);
+    } else {
+        join_tc_kernel<false><<<grid, WS_THREADS, sm, c->stream>>>(a, tmap, (int)c->ld, c->norms, nullptr, nullptr,
+                                                                  colcap);
+    }
     KCNA_LAUNCHED(c);
     return kcna_cuda_check(c, cudaGetLastError(), "join_tc_kernel");
 }

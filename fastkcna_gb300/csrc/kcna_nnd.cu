@@ -778,6 +778,40 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) select_reverse_kernel(uint32_t
     if (lane == 0) *cnt = R;
 }
 
+// BF16 screen mode: every candidate the screening join emitted is recomputed
+// with the canonical FP32 chain from the FP32 rows; a candidate beyond the
+// target's radius becomes an empty key (the merges skip those).  Warp per
+// target, the target's row in shared memory, lane per candidate.
+__global__ void __launch_bounds__(256) rescore_kernel(const float *__restrict__ X, int ld, uint32_t N,
+                                                      uint64_t *__restrict__ cand, const uint32_t *__restrict__ cand_cnt,
+                                                      uint32_t CB, const float *__restrict__ radius,
+                                                      unsigned long long *rescored) {
+    extern __shared__ __align__(16) float s_rows[]; // 8 warps x ld
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t t = blockIdx.x * 8 + w;
+    if (t >= N) return;
+    float *xt = s_rows + (size_t)w * ld;
+    for (int k = lane; k < ld; k += 32) xt[k] = X[(uint64_t)t * ld + k];
+    __syncwarp();
+    const uint32_t nc = min(cand_cnt[t], CB);
+    const float rad = radius[t];
+    uint64_t *buf = cand + (uint64_t)t * CB;
+    const float4 *x4 = reinterpret_cast<const float4 *>(xt);
+    unsigned long long n = 0;
+    for (uint32_t j = lane; j < nc; j += 32) {
+        const uint64_t k = buf[j];
+        if (kcna_key_noflags(k) == KCNA_EMPTY_KEY_NOFLAGS) continue;
+        const uint32_t id = kcna_key_id(k);
+        const float4 *xc = reinterpret_cast<const float4 *>(X + (uint64_t)id * ld);
+        float d = 0.f;
+        for (int q = 0; q < (ld >> 2); ++q) d = kcna_acc4(d, x4[q], __ldg(xc + q));
+        buf[j] = d <= rad ? kcna_key(d, id, kcna_key_flags(k)) : KCNA_EMPTY_KEY;
+        ++n;
+    }
+    n = kcna_warp_sum(n);
+    if (lane == 0 && n) atomicAdd(rescored, n);
+}
+
 // control recall: |pool[0..min(cnt,K)) ∩ exact[0..K)| per control
 __global__ void control_recall_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
                                       uint32_t cap, const uint32_t *__restrict__ controls,
@@ -916,10 +950,16 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
                              "join smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    if (c->gram_exact && kcna_join_tc_fits(a)) {
+    if ((c->gram_exact || c->bf16_screen) && kcna_join_tc_fits(a)) {
         KCNA_TRY(kcna_join_tc_launch(c, a));
+        if (c->bf16_screen) {
+            rescore_kernel<<<kcna_div_up(c->n, 8), 256, (size_t)8 * c->ld * 4, c->stream>>>(
+                c->X, (int)c->ld, c->n, c->cand, c->cand_cnt, c->CB, c->radius, c->counters + 13);
+            KCNA_LAUNCHED(c);
+            KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "rescore_kernel"));
+        }
     } else {
-        if (c->Xh)
+        if (c->bf16_exact)
             join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsB16{c->Xh, (int)c->ld});
         else
             join_kernel<<<c->n, JT, sm, c->stream>>>(a, RowsF32{c->X, (int)c->ld});
@@ -1143,8 +1183,11 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
         KCNA_TRY(kcna_nnd_sample(c, &P, (int)it + 1 + iter_base));
     }
     st->n_comps = comps_total;
-    st->screened_pairs = c->gram_exact ? comps_total : 0; // Gram tiles, exact: nothing to rescore
-    st->rescored_pairs = 0;
+    // pairs screened on Gram tiles; in screen mode the candidates among them were recomputed in FP32
+    st->screened_pairs = (c->gram_exact || c->bf16_screen) ? comps_total : 0;
+    unsigned long long resc = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&resc, c->counters + 13, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    st->rescored_pairs = resc;
     unsigned long long rev_drop = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&rev_drop, c->counters + 12, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync"));

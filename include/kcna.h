@@ -148,8 +148,9 @@ typedef struct {
     float seed_recall;         /* control recall@K of the seeded pools, before the first join */
     uint64_t seed_comps;       /* distance evaluations of the initial pools */
     uint32_t bf16_rows;        /* 1: BF16 mode read an exact BF16 copy of the rows */
-    uint32_t gram_tc;          /* 1: the local join ran on tensor-core Gram tiles (integer rows,
-                                  squared norms < 2^23, d <= 128 and a multiple of 8) */
+    uint32_t gram_tc;          /* local join on tensor-core Gram tiles: 1 exact (integer rows,
+                                  squared norms < 2^23), 2 screening of rows rounded to BF16 with
+                                  FP32 recompute of the emitted pairs; d <= 128, a multiple of 8 */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;
