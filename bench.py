@@ -212,7 +212,7 @@ def roofline(st, hbm_gbs, ld, n, search_k):
         "prune": launches["prune"] * n * min(search_k, st["maxl"]) * ld * rb,
     }
     kernels = {"join": "join_tc_kernel" if st["gram_tc"] else "join_kernel", "merge": "merge_warp_kernel",
-               "prune": "prune_kernel"}
+               "prune": "prune_gram_kernel" if st.get("prune_tc") else "prune_kernel"}
     name = max(models, key=lambda k: ph.get(k, 0.0))
     ms, nl = ph[name], max(launches[name], 1)
     per_launch_bytes = models[name] / nl

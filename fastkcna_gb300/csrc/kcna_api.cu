@@ -173,25 +173,28 @@ __global__ void bf16_copy_kernel(const uint32_t *__restrict__ x, uint64_t n, uin
 }
 
 // Gram-exact check: every value an integer (BF16 exactness is checked
-// before), squared norms |x|^2 into norms[] (exact for integer rows) and the
-// largest one.  Warp per row.
+// before), squared norms |x|^2 into norms[] (exact for integer rows), the
+// largest one and whether any value is negative.  Warp per row.
 __global__ void gram_check_kernel(const float *__restrict__ X, uint32_t n, uint32_t ld, float *__restrict__ norms,
-                                  unsigned long long *nonint, unsigned *max_bits) {
+                                  unsigned long long *nonint, unsigned *max_bits, unsigned long long *negative) {
     const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
     float acc = 0.f;
-    bool bad = false;
+    bool bad = false, neg = false;
     for (uint32_t k = lane; k < ld; k += 32) {
         const float x = X[row * ld + k];
         bad |= x != rintf(x);
+        neg |= x < 0.f;
         acc = fmaf(x, x, acc);
     }
     acc = kcna_warp_sum(acc);
     bad = __any_sync(KCNA_FULL, bad);
+    neg = __any_sync(KCNA_FULL, neg);
     if (lane == 0) {
         norms[row] = acc;
         if (bad) atomicAdd(nonint, 1ull);
+        if (neg) atomicAdd(negative, 1ull);
         atomicMax(max_bits, __float_as_uint(acc));
     }
 }
@@ -233,7 +236,7 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     release_row_copies(c);
     if (!p || p->screen != KCNA_SCREEN_BF16) return KCNA_OK;
     const uint64_t n = (uint64_t)c->n_total * c->ld;
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 40, 0, 3 * 8, c->stream), "memset"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 40, 0, 4 * 8, c->stream), "memset"));
     bf16_inexact_kernel<<<std::max(1, c->num_sms) * 8, 256, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->X), n,
                                                                              c->counters + 40);
     KCNA_LAUNCHED(c);
@@ -262,15 +265,17 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     unsigned *max_bits = reinterpret_cast<unsigned *>(c->counters + 42);
     gram_check_kernel<<<kcna_div_up((uint64_t)c->n_total * 32, 256), 256, 0, c->stream>>>(c->X, c->n_total, c->ld,
                                                                                           c->norms, c->counters + 41,
-                                                                                          max_bits);
+                                                                                          max_bits, c->counters + 43);
     KCNA_LAUNCHED(c);
-    unsigned long long h[2] = {};
-    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters + 41, 16, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    unsigned long long h[3] = {};
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters + 41, 24, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "gram check"));
     float maxn = 0.f;
     const unsigned mb = (unsigned)(h[1] & 0xFFFFFFFFull);
     memcpy(&maxn, &mb, 4);
-    if (h[0] == 0 && maxn < 8388608.f) { // 2^23: |x|^2 + |y|^2 stays below 2^24
+    // every distance, partial sum and |x|^2 - 2<x,y> below 2^24: with non-negative
+    // values |x - y|^2 <= |x|^2 + |y|^2 < 2^24; with negative ones |x|, |y| < 2^11
+    if (h[0] == 0 && maxn < (h[2] ? 4194304.f : 8388608.f)) {
         c->gram_exact = true;
         if (gram) *gram = 1;
     } else {
@@ -559,6 +564,7 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
         kcna_log(c, &P, "P2K %d: recall@MAXL %.4f t %.3f", loopcount, r, kcna_now() - s0);
     }
     st->loops = (uint32_t)loopcount;
+    st->prune_tc = kcna_prune_tc_ok(c, (int)P.nsg_R, (int)std::min(P.search_K, c->cap)) ? 1u : 0u;
     st->prune_comps = prune_comps;
     st->bridge_comps = bridge_comps;
     KCNA_TRY(degree_stats(c, st));

@@ -27,9 +27,10 @@ struct kcna_ctx {
     // of data whose every value is exactly representable in BF16
     uint16_t *Xh = nullptr;
     // Gram-exact BF16 mode: the rows are integers and every squared norm is
-    // below 2^23, so |x|^2 + |y|^2 - 2<x,y> evaluated by the tensor cores in
-    // FP32 equals the canonical FMA-chain distance bit for bit; the local join
-    // then runs on tcgen05 Gram tiles.  norms[i] = |x_i|^2 (n_total floats).
+    // below 2^23 (2^22 when a value is negative), so |x|^2 + |y|^2 - 2<x,y>
+    // evaluated by the tensor cores in FP32 equals the canonical FMA-chain
+    // distance bit for bit; the local join, the P2K join and the prune then
+    // run on tcgen05 Gram tiles.  norms[i] = |x_i|^2 (n_total floats).
     bool gram_exact = false;
     float *norms = nullptr;
     // bf16_exact: Xh holds the rows' values exactly (kernels may read it in
@@ -145,7 +146,7 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
 // TMA tensor map (128 bytes, a CUtensorMap) of the BF16 rows (kcna_tmap.cu).
 kcna_status kcna_rows_tmap(kcna_ctx *c, void *out128);
 // Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
-bool kcna_prune_tc_ok(const kcna_ctx *c, int range);
+bool kcna_prune_tc_ok(const kcna_ctx *c, int range, int maxc);
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
                                  unsigned long long *comps);
 // P2K join on tcgen05 Gram tiles (kcna_p2k_tc.cu); requires c->gram_exact.

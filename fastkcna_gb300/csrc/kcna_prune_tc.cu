@@ -6,27 +6,42 @@
 // first is kept; a later candidate p is dropped when an already kept t
 // occludes it (RNG: d(t,p) < d(q,p); tau-MNG: d(t,p) < d(q,p) - 3 tau;
 // alpha-PG: d(t,p) < d(q,p) and the angle test), and the scan stops at range
-// kept.  Candidate-to-candidate distances come from Gram tiles on BF16 rows
-// ((|x|^2 + |y|^2) - 2 <x, y>, FP32 accumulation in TMEM); the kernel runs
-// only in Gram-exact mode (integer rows, squared norms below 2^23), where they
-// equal the canonical FMA-chain distances, so the kept lists are identical.
+// kept.  The kernel runs only in Gram-exact mode (integer rows, squared norms
+// below 2^23), where the tile distances (|x|^2 + |y|^2) - 2 <x, y> (BF16
+// rows, FP32 accumulation in TMEM) equal the canonical FMA-chain distances,
+// so the kept lists are identical.
 //
-// One node at a time per block (128 threads, thread = candidate row of the
-// current chunk; several blocks per SM overlap).  Per chunk of 128
-// candidates:
-//   1. TMA tile::gather4 of the chunk's BF16 rows (128-byte swizzle);
-//   2. Gram tile chunk x kept rows (kept so far, N <= 128): a candidate
-//      occluded by an earlier kept one is dead;
-//   3. Gram tile chunk x chunk: thread p builds the 128-bit mask of the
-//      earlier chunk candidates that would occlude it;
-//   4. one warp scans the chunk in order, a mask word at a time: p is kept
-//      when alive and no kept chunk candidate is in its mask; the scan stops
-//      at range;
-//   5. the newly kept rows are copied into the kept tile for the next chunk.
-// Waits are bounded; a wait that gives up sets the error word and ends the
-// block after its products have finished.
-#include <cuda.h>
-
+// Instead of testing candidates against the kept list one at a time, the
+// kernel evaluates the occlusion rule for every ordered pair t < p of the
+// node's candidates (up to 512: the lower triangle of at most 4 x 4 tiles of
+// 128) and then resolves the sequential scan on bit masks: O[t] is the set of
+// later candidates that t would occlude, and the scan keeps t, adds O[t] to
+// the dead set and jumps to the next live candidate - one step per kept
+// neighbour.
+//
+// Block layout: persistent, one block per SM, warp-specialised; the roles
+// hand work to each other through mbarriers:
+//   warp 0      metadata: node q's pool prefix by one bulk copy (requested a
+//               node ahead), the initial dead set (ids beyond the layer
+//               prefix, repeated ids), distances, and the candidates' norms by
+//               4-byte cp.async (two nodes in flight);
+//   warps 11-14 row loaders: the candidates' BF16 rows by 16-byte cp.async
+//               into a ring of five 128-row chunk slots in the 128-byte
+//               swizzled K-major layout (each warp a quarter of every chunk,
+//               the copies of consecutive chunks overlapped);
+//   warp 1      MMA issuer (one thread): tiles (J, I), J <= I, occluders of
+//               chunk J (M = 128 TMEM lanes) against candidates of chunk I
+//               (N = 128 columns), occluder-chunk major so that chunk J's slot
+//               is released after its last tile; four 128-column accumulators;
+//   warps 2-9   mask builders: warp w reads TMEM lane quarter w % 4 and
+//               column half (w - 2) / 4 of a tile, releases the accumulator,
+//               and turns 64 distances per thread into two 32-bit words of
+//               O[t] (the sign of distance minus bound, collected by funnel
+//               shifts in four independent chains);
+//   warp 10     scan: per node, the kept list by the bit-mask scan; graph row
+//               and degree written to global memory.
+// Every wait is bounded; a wait that gives up stops the block, sets the error
+// word and lets in-flight copies and products finish before TMEM is released.
 #include <algorithm>
 
 #include "kcna_internal.h"
@@ -36,19 +51,53 @@ using namespace kcna_tc;
 
 namespace {
 
-constexpr int PT = 128;                     // threads = candidate rows per chunk
-constexpr uint32_t KBB = 128;               // bytes of a row inside one 64-element K block
-constexpr uint32_t CHUNK = PT * KBB * 2;    // 32 KiB of BF16 rows (d <= 128)
-constexpr int KMAX = 128;                   // kept rows (range <= 128)
-constexpr uint32_t KEPT = KMAX * KBB * 2;   // 32 KiB
-constexpr uint32_t TCOLS = 128;             // TMEM columns: one 128-column accumulator
+constexpr int PC = 128;                           // candidates per chunk (MMA M and N)
+constexpr int MAXCH = 4;                          // chunks per node
+constexpr int MAXC = PC * MAXCH;                  // candidates per node
+constexpr int MW = MAXC / 32;                     // mask words per row
+constexpr uint32_t KBB = 128;                     // bytes of a row inside one 64-element K block
+constexpr uint32_t CHUNK_BYTES = PC * KBB * 2;    // 128 rows, two K blocks (d <= 128): 32 KiB
+constexpr int NSLOT = 5;                          // chunk slots (>= MAXCH)
+constexpr int NACC = 4;                           // 128-column TMEM accumulators
+constexpr int EPI = 8;                            // mask-building warps
+constexpr int SCAN_WARP = 2 + EPI;
+constexpr int LOAD_WARP = SCAN_WARP + 1;          // first row-loader warp
+constexpr int NLOAD = 4;                          // row-loader warps
+constexpr int PG_THREADS = (LOAD_WARP + NLOAD) * 32;
 
-struct PruneTcArgs {
-    uint32_t N, cap, W;
+// Occluder masks, word-major: word w (candidates 32w .. 32w+31) of row t is at
+// mask_base(w) + t; word w exists for rows t < 128 (w / 4 + 1) only (t < p).
+// mask_base(w) is w modulo 32, so both the mask builders (fixed w, 32
+// consecutive t) and the scan (fixed t, 16 words) are free of bank conflicts.
+__host__ __device__ constexpr int mask_base(int w) {
+    return 128 * ((w / 4) * (w / 4 + 1) / 2 * 4 + (w % 4) * (w / 4 + 1)) + w;
+}
+constexpr int MASK_WORDS = mask_base(MW);
+
+struct alignas(16) NodeMeta {
+    uint64_t key[MAXC + 2]; // pool entries from an even index (16-byte bulk copy); candidate c at koff + c
+    float pd[MAXC];         // distance to the node
+    float nrm[MAXC];        // squared norm of the row
+    uint32_t dead[MW];      // candidates that can never be kept
+    uint32_t q, nc, nch, koff;
+};
+
+struct PgShared {
+    uint64_t slot_full[NSLOT], slot_empty[NSLOT];
+    uint64_t acc_full[NACC], acc_empty[NACC];
+    uint64_t keys_full[2], ids_ready[2], meta_full[2], mask_full[2], node_empty[2];
+    uint32_t tmem;
+    int abort_flag;
+    NodeMeta meta[2];
+    uint32_t mask[2][MASK_WORDS];
+};
+
+struct PgArgs {
+    uint32_t N, cap, W, ld;
     const uint64_t *pool;
+    const uint16_t *rows; // BF16 rows, ld elements apart
     const uint32_t *pool_cnt;
     const float *norms;
-    int kind;
     float t3, thr;
     int range, maxc;
     uint32_t *g_ids;
@@ -58,262 +107,418 @@ struct PruneTcArgs {
     int *err;
 };
 
-__device__ __forceinline__ bool occl(int kind, float t3, float thr, float td, float djk, float pd) {
-    if (kind == KCNA_TAUMNG) return djk < __fsub_rn(pd, t3);
-    if (kind == KCNA_ALPHAPG) {
-        const float num = __fdiv_rn(__fsub_rn(__fadd_rn(td, djk), pd), 2.0f);
-        const float cs = __fdiv_rn(num, __fsqrt_rn(__fmul_rn(td, djk)));
-        return djk < pd && cs < thr;
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// A word whose sign bit says whether t occludes p, from the Gram entry g:
+// |t|^2 - 2g + |p|^2 is exact in Gram-exact mode, and the sign of its
+// difference to the bound is the result of the FP32 comparison.
+template <int RULE>
+__device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float td, float t3, float thr) {
+    const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
+    if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, t3))); // src/kgraph.cpp:2859
+    const uint32_t s = __float_as_uint(__fsub_rn(dd, pd));
+    if (RULE == 2 && (s >> 31)) { // alpha-PG: and the angle at t (src/kgraph.cpp:3184-3186)
+        const float num = __fdiv_rn(__fsub_rn(__fadd_rn(td, dd), pd), 2.0f);
+        const float cs = __fdiv_rn(num, __fsqrt_rn(__fmul_rn(td, dd)));
+        return cs < thr ? 0x80000000u : 0u;
     }
-    return djk < pd;
+    return s;
 }
 
-__global__ void __launch_bounds__(PT, 3) prune_tc_kernel(PruneTcArgs a, const __grid_constant__ CUtensorMap tmap,
-                                                      int ldh) {
+// RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG, 2 alpha-PG
+template <int RULE>
+__global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ uint64_t bar_rows, bar_mma;
-    __shared__ uint32_t s_tmem;
-    __shared__ uint32_t s_id[PT];
-    __shared__ float s_pd[PT], s_nrm[PT];
-    __shared__ __align__(16) uint32_t s_mask[PT][4]; // earlier chunk candidates that would occlude row p
-    __shared__ uint32_t s_alive[4];
-    __shared__ uint32_t k_id[KMAX];
-    __shared__ float k_pd[KMAX], k_nrm[KMAX];
-    __shared__ int s_nk, s_newk, s_kfrom[KMAX];
-    const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u; // swizzled tiles need 1024-byte alignment
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
-    const uint32_t tC = tiles_s, tK = tiles_s + CHUNK;
+    PgShared &S = *reinterpret_cast<PgShared *>(tiles + NSLOT * CHUNK_BYTES);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nkb = (ldh + 63) >> 6;
-    const void *tm = &tmap;
+    const int nkb = ((int)a.ld + 63) >> 6;
 
-    if (warp == 0) tmem_alloc(&s_tmem, TCOLS);
+    // K padding beyond ld is never written by the loaders and must read as zero
+    for (int i = tid; i < (int)(NSLOT * CHUNK_BYTES / 16); i += PG_THREADS)
+        reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 1) tmem_alloc(&S.tmem, NACC * PC);
     if (tid == 0) {
-        mbar_init(&bar_rows, 1);
-        mbar_init(&bar_mma, 1);
+        for (int i = 0; i < NSLOT; ++i) {
+            mbar_init(&S.slot_full[i], NLOAD * 32); // every loader lane, after its copies and a proxy fence
+            mbar_init(&S.slot_empty[i], 1);         // MMA commit after the chunk's last tile
+        }
+        for (int i = 0; i < NACC; ++i) {
+            mbar_init(&S.acc_full[i], 1);   // MMA commit
+            mbar_init(&S.acc_empty[i], EPI);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&S.keys_full[i], 1);        // metadata lane 0 (expect_tx); the bulk copy completes it
+            mbar_init(&S.ids_ready[i], 1);        // metadata lane 0 after the keys are parsed
+            mbar_init(&S.meta_full[i], 64);       // metadata lanes: stores done, norm copies landed
+            mbar_init(&S.mask_full[i], EPI);
+            mbar_init(&S.node_empty[i], 2 + NLOAD); // scan, MMA issuer, loader warps
+        }
+        S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // K padding of the kept tile beyond ldh and its unused rows read as zero
-    for (int i = tid; i < (int)((CHUNK + KEPT) / 16); i += PT) reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
     fence_proxy_async();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = s_tmem;
-    uint32_t ph_rows = 0, ph_mma = 0;
+    const uint32_t tmem = S.tmem;
+    const uint32_t slot0 = tiles_s;
     bool ok = true;
-    unsigned long long cc = 0;
 
-    for (uint32_t q = blockIdx.x; q < a.N && ok; q += gridDim.x) {
-        const uint64_t *pr = a.pool + (uint64_t)q * a.cap;
-        const int cnt = (int)a.pool_cnt[q];
-        int first = 0;
-        if (cnt > 0 && kcna_key_id(pr[0]) == q) first = 1;
-        const int lim = max(min(cnt, a.maxc), first + 1);
-        if (tid == 0) s_nk = 0;
-        int nk = 0;
-        if (first < cnt) {
-            for (int c0 = first; c0 < lim && nk < a.range && ok; c0 += PT) {
-                const int m = min(PT, lim - c0); // candidates of this chunk
-                // metadata and rows of the chunk
-                uint32_t id = 0xFFFFFFFFu;
-                float pd = 0.f;
-                if (tid < m) {
-                    const uint64_t k = pr[c0 + tid];
-                    id = kcna_key_id(k);
-                    pd = kcna_key_dist(k);
+    if (warp == 0) {
+        // ------------------------------------------------------------ metadata
+        // node kk's pool prefix (the candidates and the entry before them) by
+        // one bulk copy from an even pool index; lane 0 issues
+        uint32_t r_cnt0 = 0u, r_cnt1 = 0u, r_shift0 = 0u, r_shift1 = 0u;
+        int pending = -1; // node whose key copy is requested and not yet waited for
+        auto request = [&](int kk) {
+            const uint32_t q = blockIdx.x + (uint32_t)kk * gridDim.x;
+            if (q >= a.N) return;
+            const int b = kk & 1;
+            pending = kk;
+            const uint32_t cnt = min(a.pool_cnt[q], a.cap);
+            const uint64_t base = (uint64_t)q * a.cap;
+            const uint32_t shift = (uint32_t)(base & 1u);
+            const uint32_t ncopy = min(cnt, (uint32_t)max(a.maxc, 2));
+            const uint32_t nent = (shift + ncopy + 1u) & ~1u;
+            if (b) {
+                r_cnt1 = cnt;
+                r_shift1 = shift;
+            } else {
+                r_cnt0 = cnt;
+                r_shift0 = shift;
+            }
+            if (lane == 0) {
+                if (nent) {
+                    fence_proxy_async(); // earlier generic reads of the buffer before the async-proxy write
+                    mbar_arrive_expect_tx(&S.keys_full[b], nent * 8u);
+                    bulk_copy_g2s(smem_u32(S.meta[b].key), a.pool + (base - shift), nent * 8u, &S.keys_full[b]);
+                } else {
+                    mbar_arrive(&S.keys_full[b]);
                 }
-                const bool live = tid < m && id < a.N; // src/kgraph.cpp:1822, ids beyond the prefix are skipped
-                s_id[tid] = tid < m ? id : 0u;
-                s_pd[tid] = pd;
-                s_nrm[tid] = live ? __ldg(a.norms + id) : __uint_as_float(0x7FC00000u);
-                __syncthreads();
-                if (tid == 0) mbar_arrive_expect_tx(&bar_rows, (uint32_t)((m + 3) / 4 * 4 * nkb) * KBB);
-                __syncthreads();
-                if (tid < 32) {
-                    const int ng = (m + 3) >> 2;
-                    for (int e = lane; e < ng * nkb; e += 32) {
-                        const int g = nkb == 2 ? e >> 1 : e, kb = nkb == 2 ? e & 1 : 0;
-                        const int r = 4 * g;
-                        tma_gather4(tC + (uint32_t)kb * PT * KBB + (uint32_t)r * KBB, tm, 64 * kb, (int)s_id[r],
-                                    (int)s_id[min(r + 1, m - 1)], (int)s_id[min(r + 2, m - 1)],
-                                    (int)s_id[min(r + 3, m - 1)], &bar_rows);
+            }
+        };
+        request(0);
+        int k = 0;
+        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+            const int sl = k & 1;
+            if (!mbar_wait(&S.keys_full[sl], (k >> 1) & 1)) { ok = false; break; }
+            pending = -1;
+            if (S.abort_flag) { ok = false; break; }
+            NodeMeta &M = S.meta[sl];
+            const int cnt = (int)(sl ? r_cnt1 : r_cnt0);
+            const uint32_t shift = sl ? r_shift1 : r_shift0;
+            int first = 0;
+            if (cnt > 0 && kcna_key_id(M.key[shift]) == q) first = 1;
+            const int nc = first < cnt ? max(min(cnt, a.maxc), first + 1) - first : 0;
+            const int nch = (nc + PC - 1) / PC;
+            const uint32_t koff = shift + (uint32_t)first;
+#pragma unroll 4
+            for (int i = 0; i < MW; ++i) {
+                const int c = 32 * i + lane;
+                const bool live = c < nc;
+                uint32_t id = 0u, before = 0xFFFFFFFFu;
+                float pd = 0.f;
+                if (live) {
+                    const uint64_t key = M.key[koff + c];
+                    id = kcna_key_id(key);
+                    pd = kcna_key_dist(key);
+                    if (c > 0) before = kcna_key_id(M.key[koff + c - 1]);
+                }
+                // src/kgraph.cpp:1822: ids beyond the layer prefix are skipped; a
+                // repeated id is occluded by its twin (same row, same distance)
+                const bool dead = !live || (c > 0 && (id >= a.N || id == before));
+                const unsigned dm = __ballot_sync(KCNA_FULL, dead);
+                if (c < nch * PC) {
+                    M.pd[c] = pd;
+                    if (live && id < a.N) cp_async4(smem_u32(&M.nrm[c]), a.norms + id);
+                    else M.nrm[c] = 0.f;
+                }
+                if (lane == 0) M.dead[i] = dm;
+            }
+            if (lane == 0) {
+                M.q = q;
+                M.nc = (uint32_t)nc;
+                M.nch = (uint32_t)nch;
+                M.koff = koff;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.ids_ready[sl]);
+            mbar_arrive_cp_async(&S.meta_full[sl]); // when this lane's norm copies have landed
+            mbar_arrive(&S.meta_full[sl]);          // this lane's stores
+            // the next node's keys into the other buffer, once its node k-1 is done
+            const uint32_t qn = q + gridDim.x;
+            if (qn < a.N) {
+                if (k >= 1 && !mbar_wait(&S.node_empty[sl ^ 1], ((k - 1) >> 1) & 1)) { ok = false; break; }
+                request(k + 1);
+            }
+        }
+        cp_async_wait_0();
+        // a key copy still in flight lands before the block exits
+        if (pending >= 0) (void)mbar_wait(&S.keys_full[pending & 1], (pending >> 1) & 1, 1u << 16);
+        if (!ok) S.abort_flag = 1;
+    } else if (warp >= LOAD_WARP) {
+        // --------------------------------------------------------- row loaders
+        const int lw = warp - LOAD_WARP;
+        const int nseg = (int)(a.ld >> 3); // 16-byte segments per row
+        uint32_t gc = 0;
+        int pend = -1; // slot whose copies are in flight, not yet announced
+        int k = 0;
+        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+            const int sl = k & 1;
+            if (!mbar_wait(&S.ids_ready[sl], (k >> 1) & 1) || S.abort_flag) { ok = false; break; }
+            const NodeMeta &M = S.meta[sl];
+            const int nc = (int)M.nc, nch = (int)M.nch;
+            const uint64_t *keys = M.key + M.koff;
+            for (int i = 0; i < nch; ++i, ++gc) {
+                const int s = (int)(gc % NSLOT);
+                if (gc >= (uint32_t)NSLOT && !mbar_wait(&S.slot_empty[s], ((gc / NSLOT) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t slot = slot0 + (uint32_t)s * CHUNK_BYTES;
+                const int seg = lane & 15;
+#pragma unroll 4
+                for (int rr = 0; rr < 16; ++rr) {
+                    const int r = 32 * lw + 2 * rr + (lane >> 4); // row of the chunk
+                    const int c = PC * i + r;
+                    if (c < nc && seg < nseg) {
+                        const uint32_t id = kcna_key_id(keys[c]);
+                        cp_async16(slot + (uint32_t)(seg >> 3) * PC * KBB + sw128_off((uint32_t)r, (uint32_t)(seg & 7)),
+                                   a.rows + (uint64_t)id * a.ld + seg * 8);
                     }
                 }
-                ok = mbar_wait(&bar_rows, ph_rows) && ok;
-                ph_rows ^= 1u;
-                // 2. against the rows kept so far (columns 0..nk-1)
-                bool alive = live;
-                if (nk > 0) {
-                    if (tid == 0) {
+                cp_async_commit();
+                if (pend >= 0) { // the previous chunk's copies: landed, fenced for the tensor cores, announced
+                    cp_async_wait_1();
+                    fence_proxy_async();
+                    mbar_arrive(&S.slot_full[pend]);
+                }
+                pend = s;
+            }
+            if (pend >= 0) {
+                cp_async_wait_0();
+                fence_proxy_async();
+                mbar_arrive(&S.slot_full[pend]);
+                pend = -1;
+            }
+            if (!ok) break;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.node_empty[sl]);
+        }
+        cp_async_wait_0();
+        if (!ok) S.abort_flag = 1;
+    } else if (warp == 1) {
+        // ---------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            uint32_t gc = 0, acount = 0;
+            int k = 0;
+            const uint32_t idesc = idesc_bf16(PC, PC);
+            for (uint32_t q = blockIdx.x; q < a.N && ok; q += gridDim.x, ++k) {
+                const int sl = k & 1;
+                if (!mbar_wait(&S.ids_ready[sl], (k >> 1) & 1) || S.abort_flag) { ok = false; break; }
+                const int nch = (int)S.meta[sl].nch;
+                for (int J = 0; J < nch && ok; ++J)
+                    for (int I = J; I < nch; ++I, ++acount) {
+                        const uint32_t gI = gc + (uint32_t)I, gJ = gc + (uint32_t)J;
+                        if (J == 0 && !mbar_wait(&S.slot_full[gI % NSLOT], (gI / NSLOT) & 1)) { ok = false; break; }
+                        const int b = (int)(acount % NACC);
+                        if (acount >= (uint32_t)NACC && !mbar_wait(&S.acc_empty[b], ((acount / NACC) - 1) & 1)) {
+                            ok = false;
+                            break;
+                        }
                         fence_after();
-                        const uint32_t idesc = idesc_bf16(PT, (nk + 15) & ~15);
+                        const uint32_t aJ = slot0 + (gJ % NSLOT) * CHUNK_BYTES, bI = slot0 + (gI % NSLOT) * CHUNK_BYTES;
                         for (int kb = 0; kb < nkb; ++kb)
 #pragma unroll
                             for (int kk = 0; kk < 4; ++kk)
-                                mma_bf16(tmem, desc_sw128(tC + kb * PT * KBB + kk * 32),
-                                         desc_sw128(tK + kb * KMAX * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
-                        mma_commit(&bar_mma);
+                                mma_bf16(tmem + (uint32_t)(b * PC), desc_sw128(aJ + kb * PC * KBB + kk * 32),
+                                         desc_sw128(bI + kb * PC * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
+                        mma_commit(&S.acc_full[b]);
+                        if (I == nch - 1) mma_commit(&S.slot_empty[gJ % NSLOT]); // chunk J's last tile
                     }
-                    ok = mbar_wait(&bar_mma, ph_mma) && ok;
-                    ph_mma ^= 1u;
-                    fence_after();
-                    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-#pragma unroll 1
-                    for (int g = 0; g * 16 < nk; ++g) {
-                        uint32_t raw[16];
-                        tmem_ld16_async(trow + 16 * g, raw);
-                        tmem_wait_ld16(raw);
-#pragma unroll
-                        for (int u = 0; u < 16; ++u) {
-                            const int t = 16 * g + u;
-                            if (t < nk && alive) {
-                                const float djk =
-                                    __fsub_rn(__fadd_rn(s_nrm[tid], k_nrm[t]), 2.f * __uint_as_float(raw[u]));
-                                ++cc;
-                                if (k_id[t] == id || occl(a.kind, a.t3, a.thr, k_pd[t], djk, pd)) alive = false;
-                            }
-                        }
+                gc += (uint32_t)nch;
+                if (ok) mbar_arrive(&S.node_empty[sl]); // this node's tiles are issued
+            }
+            if (!ok) {
+                S.abort_flag = 1;
+                // products still in flight finish before TMEM is released
+                for (uint32_t b = 0; b < (uint32_t)NACC; ++b)
+                    if (acount > b) {
+                        const uint32_t last = b + (acount - 1 - b) / NACC * NACC;
+                        (void)mbar_wait(&S.acc_full[b], (last / NACC) & 1u, 1u << 16);
                     }
-                    fence_before();
-                    __syncthreads(); // TMEM read by every warp before the next product
-                    fence_after();
-                }
-                // 3. chunk x chunk: mask of earlier candidates that would occlude this one
-                if (tid == 0) {
-                    fence_after();
-                    const uint32_t idesc = idesc_bf16(PT, PT);
-                    for (int kb = 0; kb < nkb; ++kb)
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)
-                            mma_bf16(tmem, desc_sw128(tC + kb * PT * KBB + kk * 32),
-                                     desc_sw128(tC + kb * PT * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
-                    mma_commit(&bar_mma);
-                }
-                ok = mbar_wait(&bar_mma, ph_mma) && ok;
-                ph_mma ^= 1u;
-                fence_after();
-                uint32_t mk[4] = {0u, 0u, 0u, 0u};
-                {
-                    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-                    const int gmax = (32 * warp + 31) >> 4; // groups holding columns < this warp's rows
-#pragma unroll
-                    for (int g = 0; g < PT / 16; ++g) {
-                        if (g > gmax) break;
-                        uint32_t raw[16];
-                        tmem_ld16_async(trow + 16 * g, raw);
-                        tmem_wait_ld16(raw);
-#pragma unroll
-                        for (int u = 0; u < 16; ++u) {
-                            const int t = 16 * g + u;
-                            if (t < tid && alive) {
-                                const float djk =
-                                    __fsub_rn(__fadd_rn(s_nrm[tid], s_nrm[t]), 2.f * __uint_as_float(raw[u]));
-                                if (s_id[t] == id || occl(a.kind, a.t3, a.thr, s_pd[t], djk, pd))
-                                    mk[t >> 5] |= 1u << (t & 31);
-                            }
-                        }
-                    }
-                }
-#pragma unroll
-                for (int x = 0; x < 4; ++x) s_mask[tid][x] = mk[x];
-                const unsigned al = __ballot_sync(KCNA_FULL, alive);
-                if (lane == 0) s_alive[warp] = al;
-                fence_before();
-                __syncthreads();
-                fence_after();
-                // 4. the scan, in candidate order, by warp 0: 32 candidates (one word
-                // of the masks) at a time; lane p first tests the kept words of
-                // earlier blocks, then the block is resolved in order with the
-                // block's own mask word broadcast lane by lane
-                if (warp == 0) {
-                    uint32_t kw0 = 0u, kw1 = 0u, kw2 = 0u, kw3 = 0u; // kept chunk candidates
-                    int nkl = nk, newk = 0;
-                    for (int b = 0; b * 32 < m && nkl < a.range; ++b) {
-                        const int p = 32 * b + lane;
-                        const bool is_first = c0 + p == first;
-                        const bool al_p = p < m && (is_first || ((s_alive[b] >> lane) & 1u));
-                        const uint4 mk4 = *reinterpret_cast<const uint4 *>(s_mask[min(p, PT - 1)]);
-                        const bool pre = ((mk4.x & kw0) | (mk4.y & kw1) | (mk4.z & kw2) | (mk4.w & kw3)) == 0u;
-                        const uint32_t own = b == 0 ? mk4.x : b == 1 ? mk4.y : b == 2 ? mk4.z : mk4.w;
-                        const unsigned cand = __ballot_sync(KCNA_FULL, al_p && pre);
-                        uint32_t kb = 0u;
-                        int cnt = nkl;
-                        for (int i = 0; i < 32; ++i) {
-                            const uint32_t wi = __shfl_sync(KCNA_FULL, own, i);
-                            if (((cand >> i) & 1u) && !(wi & kb) && cnt < a.range) {
-                                kb |= 1u << i;
-                                ++cnt;
-                            }
-                        }
-                        if ((kb >> lane) & 1u) {
-                            const int r = __popc(kb & kcna_lanemask_lt());
-                            k_id[nkl + r] = s_id[p];
-                            k_pd[nkl + r] = s_pd[p];
-                            k_nrm[nkl + r] = s_nrm[p];
-                            s_kfrom[newk + r] = p;
-                        }
-                        if (b == 0) kw0 = kb;
-                        if (b == 1) kw1 = kb;
-                        if (b == 2) kw2 = kb;
-                        if (b == 3) kw3 = kb;
-                        nkl += __popc(kb);
-                        newk += __popc(kb);
-                    }
-                    if (lane == 0) {
-                        s_nk = nkl;
-                        s_newk = newk;
-                    }
-                }
-                __syncthreads();
-                // 5. newly kept rows into the kept tile (rows nk.., swizzled like the chunk)
-                const int newk = s_newk;
-                for (int e = tid; e < newk * 2 * 8; e += PT) {
-                    const int r = e >> 4, c16 = e & 15, kb = c16 >> 3, ch = c16 & 7;
-                    const int src = s_kfrom[r], dst = nk + r;
-                    const uint4 v = *reinterpret_cast<const uint4 *>(tiles + kb * PT * KBB + sw128_off((uint32_t)src, (uint32_t)ch));
-                    *reinterpret_cast<uint4 *>(tiles + CHUNK + kb * KMAX * KBB + sw128_off((uint32_t)dst, (uint32_t)ch)) = v;
-                }
-                nk = s_nk;
-                fence_proxy_async();
-                __syncthreads();
-                ok = __syncthreads_and(ok) != 0;
             }
         }
-        // graph row of q
-        for (int j = tid; j < (int)a.W; j += PT) {
-            a.g_ids[(uint64_t)q * a.W + j] = j < nk ? k_id[j] : KCNA_NONE;
-            a.g_dist[(uint64_t)q * a.W + j] = j < nk ? k_pd[j] : 0.f;
+        __syncwarp();
+    } else if (warp < SCAN_WARP) {
+        // -------------------------------------------------------- mask builders
+        const int qt = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column half
+        uint32_t acount = 0;
+        int k = 0;
+        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+            const int sl = k & 1;
+            bool mine = mbar_wait(&S.meta_full[sl], (k >> 1) & 1) && !S.abort_flag;
+            if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
+            const NodeMeta &M = S.meta[sl];
+            uint32_t *mask = S.mask[sl];
+            const int nch = (int)M.nch;
+            for (int J = 0; J < nch && ok; ++J) {
+                const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
+                const float n_t = M.nrm[t], td = M.pd[t];
+                for (int I = J; I < nch; ++I, ++acount) {
+                    const int b = (int)(acount % NACC);
+                    mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
+                    fence_after();
+                    const bool skip = I == J && 64 * h + 63 <= 32 * qt; // no column after any row of the warp
+                    uint32_t raw[64];
+                    if (mine && !skip) {
+                        const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC + 64 * h);
+                        tmem_ld16_async(ta, raw);
+                        tmem_ld16_async(ta + 16, raw + 16);
+                        tmem_ld16_async(ta + 32, raw + 32);
+                        tmem_ld16_async(ta + 48, raw + 48);
+                        tmem_wait_ld16(raw);
+                        tmem_wait_ld16(raw + 16);
+                        tmem_wait_ld16(raw + 32);
+                        tmem_wait_ld16(raw + 48);
+                    }
+                    // the accumulator is in registers: release it before the bit work
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.acc_empty[b]);
+                    if (!__all_sync(KCNA_FULL, mine)) {
+                        ok = false;
+                        break;
+                    }
+#pragma unroll
+                    for (int ww = 0; ww < 2; ++ww) {
+                        const int p0 = I * PC + 64 * h + 32 * ww; // first candidate of the word
+                        uint32_t word = 0;
+                        if (!skip) {
+                            const float4 *np4 = reinterpret_cast<const float4 *>(M.nrm + p0);
+                            const float4 *pd4 = reinterpret_cast<const float4 *>(M.pd + p0);
+                            // four chains of eight: candidate 8j+m ends in bit 7-m of wq[j]
+                            uint32_t wq[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+                            for (int u4 = 0; u4 < 8; ++u4) {
+                                const float4 n4 = np4[u4], d4 = pd4[u4];
+                                const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+                                for (int v = 0; v < 4; ++v) {
+                                    const uint32_t sg = occl_sign<RULE>(__uint_as_float(raw[32 * ww + 4 * u4 + v]),
+                                                                        n_t, nn[v], dv[v], td, a.t3, a.thr);
+                                    wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
+                                }
+                            }
+                            word = __brev((wq[0] << 24) | (wq[1] << 16) | (wq[2] << 8) | wq[3]);
+                            if (I == J) { // only candidates after t
+                                const int r = t - p0;
+                                word = r < 0 ? word : r >= 31 ? 0u : word & ~((2u << r) - 1u);
+                            }
+                        }
+                        mask[mask_base(4 * I + 2 * h + ww) + t] = word;
+                    }
+                }
+            }
+            if (!ok) break;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.mask_full[sl]);
         }
-        if (tid == 0) a.g_deg[q] = (uint32_t)nk;
-        __syncthreads();
+        if (!ok) S.abort_flag = 1;
+    } else {
+        // ----------------------------------------------------------------- scan
+        unsigned long long cc = 0;
+        int k = 0;
+        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+            const int sl = k & 1;
+            const bool mine = mbar_wait(&S.mask_full[sl], (k >> 1) & 1) && !S.abort_flag;
+            if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
+            const NodeMeta &M = S.meta[sl];
+            const uint32_t *mask = S.mask[sl];
+            const uint64_t *keys = M.key + M.koff;
+            const int nc = (int)M.nc;
+            uint32_t *gi = a.g_ids + (uint64_t)M.q * a.W;
+            float *gd = a.g_dist + (uint64_t)M.q * a.W;
+            int nk = 0;
+            if (nc > 0) {
+                uint32_t dead = lane < MW ? M.dead[lane] : 0xFFFFFFFFu;
+                int t = 0;
+                for (;;) {
+                    if (lane == 0) {
+                        gi[nk] = kcna_key_id(keys[t]);
+                        gd[nk] = M.pd[t];
+                        cc += (unsigned long long)nk; // a kept candidate was tested against every earlier one
+                    }
+                    ++nk;
+                    if (nk >= a.range) break;
+                    const int tw = t >> 5;
+                    uint32_t o = 0;
+                    if (lane < MW && lane >= 4 * (t >> 7)) o = mask[mask_base(lane) + t];
+                    const uint32_t above = lane > tw ? 0xFFFFFFFFu : lane < tw ? 0u : ~((2u << (t & 31)) - 1u);
+                    cc += (unsigned long long)nk * __popc(o & ~dead & above); // dropped at the nk-th kept
+                    dead |= o;
+                    const uint32_t alive = ~dead & above;
+                    const unsigned bal = __ballot_sync(KCNA_FULL, alive != 0u);
+                    if (!bal) break;
+                    const int L = __ffs(bal) - 1;
+                    t = 32 * L + __ffs(__shfl_sync(KCNA_FULL, alive, L)) - 1;
+                }
+            }
+            __syncwarp();
+            for (int j = nk + lane; j < (int)a.W; j += 32) {
+                gi[j] = KCNA_NONE;
+                gd[j] = 0.f;
+            }
+            if (lane == 0) a.g_deg[M.q] = (uint32_t)nk;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.node_empty[sl]);
+        }
+        cc = kcna_warp_sum(cc);
+        if (lane == 0 && cc) atomicAdd(a.comps, cc);
+        if (!ok) S.abort_flag = 1;
     }
-    if (!ok && tid == 0) (void)mbar_wait(&bar_mma, ph_mma, 1u << 16); // a product still in flight
-    cc = kcna_warp_sum(cc);
-    if (lane == 0 && cc) atomicAdd(a.comps, cc);
     fence_before();
     __syncthreads();
-    if (warp == 0) tmem_free(tmem, TCOLS);
-    if (!ok && tid == 0) kcna_set_err(a.err, KCNA_DERR_SPIN);
+    if (warp == 1) tmem_free(tmem, NACC * PC);
+    if (!ok) kcna_set_err(a.err, KCNA_DERR_SPIN);
+}
+
+size_t prune_gram_smem() { return 1024 + (size_t)NSLOT * CHUNK_BYTES + sizeof(PgShared); }
+
+template <int RULE>
+kcna_status launch_rule(kcna_ctx *c, const PgArgs &a, uint32_t grid) {
+    const size_t sm = prune_gram_smem();
+    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune_gram_kernel<RULE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sm),
+                             "prune_gram smem attr"));
+    prune_gram_kernel<RULE><<<grid, PG_THREADS, sm, c->stream>>>(a);
+    KCNA_LAUNCHED(c);
+    return kcna_cuda_check(c, cudaGetLastError(), "prune_gram_kernel");
 }
 
 } // namespace
 
-bool kcna_prune_tc_ok(const kcna_ctx *c, int range) {
-    return c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range <= KMAX;
+bool kcna_prune_tc_ok(const kcna_ctx *c, int range, int maxc) {
+    return c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range >= 1 && maxc >= 1 &&
+           maxc <= MAXC && prune_gram_smem() <= 227 * 1024;
 }
 
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
                                  unsigned long long *comps) {
-    if (!kcna_prune_tc_ok(c, range)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
-    PruneTcArgs a;
+    if (!kcna_prune_tc_ok(c, range, maxc)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
+    PgArgs a;
     a.N = c->n;
     a.cap = c->cap;
     a.W = c->W;
+    a.ld = c->ld;
     a.pool = c->pool;
+    a.rows = c->Xh;
     a.pool_cnt = c->pool_cnt;
     a.norms = c->norms;
-    a.kind = kind;
     a.t3 = t3;
     a.thr = thr;
     a.range = range;
@@ -323,20 +528,9 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int
     a.g_deg = c->g_deg;
     a.comps = comps;
     a.err = c->d_err;
-    const size_t sm = 1024 + CHUNK + KEPT;
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
-                             "prune_tc smem attr"));
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(prune_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                     (int)cudaSharedmemCarveoutMaxShared),
-                             "prune_tc carveout"));
-    int per_sm = 0;
-    KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prune_tc_kernel, PT, sm),
-                             "prune_tc occupancy"));
-    per_sm = std::min(std::max(per_sm, 1), (int)(512 / TCOLS));
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(c->n, (uint64_t)std::max(c->num_sms, 1) * per_sm);
-    alignas(64) CUtensorMap tmap;
-    KCNA_TRY(kcna_rows_tmap(c, &tmap));
-    prune_tc_kernel<<<grid, PT, sm, c->stream>>>(a, tmap, (int)c->ld);
-    KCNA_LAUNCHED(c);
-    return kcna_cuda_check(c, cudaGetLastError(), "prune_tc_kernel");
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(c->n, (uint64_t)std::max(c->num_sms, 1));
+    if (grid == 0) return KCNA_OK;
+    if (kind == KCNA_TAUMNG) return launch_rule<1>(c, a, grid);
+    if (kind == KCNA_ALPHAPG) return launch_rule<2>(c, a, grid);
+    return launch_rule<0>(c, a, grid);
 }

@@ -71,20 +71,23 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
 }
 
-// Bounded wait on an mbarrier phase (non-blocking tests with a short sleep,
-// about half a second in total); false when the bound ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t max_tries = (1u << 22)) {
+// Bounded wait on an mbarrier phase: mbarrier.try_wait suspends the thread
+// in hardware (up to the time hint, a microsecond, per try) instead of
+// polling, so waiting warps take no issue slots; after 64 tries each further
+// try also sleeps, so the bound holds whatever the suspension; false when
+// max_tries tries (a second or more) ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t max_tries = (1u << 20)) {
     const uint32_t a = smem_u32(mbar);
     for (uint32_t i = 0; i < max_tries; ++i) {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(1000u)
             : "memory");
         if (done) return true;
-        if (i > 64) __nanosleep(128);
+        if (i > 64) __nanosleep(256);
     }
     return false;
 }

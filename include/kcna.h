@@ -151,6 +151,7 @@ typedef struct {
     uint32_t gram_tc;          /* local join on tensor-core Gram tiles: 1 exact (integer rows,
                                   squared norms < 2^23), 2 screening of rows rounded to BF16 with
                                   FP32 recompute of the emitted pairs; d <= 128, a multiple of 8 */
+    uint32_t prune_tc;         /* 1: the occlusion prunes ran on tensor-core Gram tiles (Gram-exact rows) */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;

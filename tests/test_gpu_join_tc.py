@@ -116,6 +116,7 @@ def test_tc_join_build_matches_fp32_build(index, monkeypatch):
     assert np.array_equal(deg0, deg1)
     assert rows_equal_as_sets(g0, deg0, g1, deg1) == 0
     assert st0["loop_recall"][-1] == st1["loop_recall"][-1]
+    assert st1["prune_tc"] == 1 and st0["prune_tc"] == 0
     # the P2K join on Gram tiles evaluates the same pairs as the FP32 one
     assert st0["bridge_comps"] == st1["bridge_comps"] and st0["n_comps"] == st1["n_comps"]
 
