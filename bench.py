@@ -356,6 +356,10 @@ def run_gpu(args, ws, rank, local):
                    "seed_recall": round(st["seed_recall"], 4),
                    "plain_fp32_s": round(plain_ms / 1000.0, 4) if plain_ms else None,
                    "plain_fp32_knn_recall_at_K": round(plain_stats[-1]["loop_recall"][-1], 4) if plain_ms else None,
+                   "plain_fp32_nndescent_iterations": plain_stats[-1]["iterations"] if plain_ms else None,
+                   "plain_fp32_nndescent_recall": [round(x, 4) for x in plain_stats[-1]["iter_recall"]] if plain_ms else None,
+                   "plain_fp32_phase_ms": {k: round(v, 2) for k, v in plain_stats[-1]["phase_ms"].items() if v}
+                   if plain_ms else None,
                    "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None,
                    "search_recall_at_10": round(rec10, 4),
                    "plain_fp32_search_recall_at_10": round(plain_rec10, 4) if plain_rec10 is not None else None,

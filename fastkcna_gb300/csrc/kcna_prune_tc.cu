@@ -25,7 +25,7 @@
 //               node ahead), the initial dead set (ids beyond the layer
 //               prefix, repeated ids), distances, and the candidates' norms by
 //               4-byte cp.async (two nodes in flight);
-//   warps 11-14 row loaders: the candidates' BF16 rows by 16-byte cp.async
+//   warps 19-22 row loaders: the candidates' BF16 rows by 16-byte cp.async
 //               into a ring of five 128-row chunk slots in the 128-byte
 //               swizzled K-major layout (each warp a quarter of every chunk,
 //               the copies of consecutive chunks overlapped);
@@ -33,12 +33,12 @@
 //               chunk J (M = 128 TMEM lanes) against candidates of chunk I
 //               (N = 128 columns), occluder-chunk major so that chunk J's slot
 //               is released after its last tile; four 128-column accumulators;
-//   warps 2-9   mask builders: warp w reads TMEM lane quarter w % 4 and
-//               column half (w - 2) / 4 of a tile, releases the accumulator,
-//               and turns 64 distances per thread into two 32-bit words of
-//               O[t] (the sign of distance minus bound, collected by funnel
-//               shifts in four independent chains);
-//   warp 10     scan: per node, the kept list by the bit-mask scan; graph row
+//   warps 2-17  mask builders: warp w reads TMEM lane quarter w % 4 and
+//               column group (w - 2) / 4 (32 columns) of a tile, releases the
+//               accumulator, and turns 32 distances per thread into a 32-bit
+//               word of O[t] (the sign of distance minus bound, collected by
+//               funnel shifts in four independent chains);
+//   warp 18     scan: per node, the kept list by the bit-mask scan; graph row
 //               and degree written to global memory.
 // Every wait is bounded; a wait that gives up stops the block, sets the error
 // word and lets in-flight copies and products finish before TMEM is released.
@@ -59,7 +59,9 @@ constexpr uint32_t KBB = 128;                     // bytes of a row inside one 6
 constexpr uint32_t CHUNK_BYTES = PC * KBB * 2;    // 128 rows, two K blocks (d <= 128): 32 KiB
 constexpr int NSLOT = 5;                          // chunk slots (>= MAXCH)
 constexpr int NACC = 4;                           // 128-column TMEM accumulators
-constexpr int EPI = 8;                            // mask-building warps
+constexpr int EPI = 16;                           // mask-building warps: 4 lane quarters x 4 column groups
+constexpr int CW = PC / (EPI / 4);                // columns of a tile per mask-building warp
+constexpr int WPT = CW / 32;                      // mask words per thread and tile
 constexpr int SCAN_WARP = 2 + EPI;
 constexpr int LOAD_WARP = SCAN_WARP + 1;          // first row-loader warp
 constexpr int NLOAD = 4;                          // row-loader warps
@@ -85,7 +87,7 @@ struct alignas(16) NodeMeta {
 struct PgShared {
     uint64_t slot_full[NSLOT], slot_empty[NSLOT];
     uint64_t acc_full[NACC], acc_empty[NACC];
-    uint64_t keys_full[2], ids_ready[2], meta_full[2], mask_full[2], node_empty[2];
+    uint64_t keys_full[2], ids_ready[2], meta_full[2], bound_ready[2], mask_full[2], node_empty[2];
     uint32_t tmem;
     int abort_flag;
     NodeMeta meta[2];
@@ -113,9 +115,12 @@ __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_
 
 // A word whose sign bit says whether t occludes p, from the Gram entry g:
 // |t|^2 - 2g + |p|^2 is exact in Gram-exact mode, and the sign of its
-// difference to the bound is the result of the FP32 comparison.
+// difference to the bound is the result of the FP32 comparison.  For RNG the
+// column value is pd - |p|^2 (an exact integer difference in Gram-exact mode:
+// pool distances are canonical distances of integer rows), one add fewer.
 template <int RULE>
 __device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float td, float t3, float thr) {
+    if (RULE == 0) return __float_as_uint(__fsub_rn(__fmaf_rn(-2.f, g, nt), pd)); // pd holds pd - |p|^2
     const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
     if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, t3))); // src/kgraph.cpp:2859
     const uint32_t s = __float_as_uint(__fsub_rn(dd, pd));
@@ -154,6 +159,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             mbar_init(&S.keys_full[i], 1);        // metadata lane 0 (expect_tx); the bulk copy completes it
             mbar_init(&S.ids_ready[i], 1);        // metadata lane 0 after the keys are parsed
             mbar_init(&S.meta_full[i], 64);       // metadata lanes: stores done, norm copies landed
+            mbar_init(&S.bound_ready[i], EPI);    // mask builders' shares of the RNG column values
             mbar_init(&S.mask_full[i], EPI);
             mbar_init(&S.node_empty[i], 2 + NLOAD); // scan, MMA issuer, loader warps
         }
@@ -356,16 +362,24 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         __syncwarp();
     } else if (warp < SCAN_WARP) {
         // -------------------------------------------------------- mask builders
-        const int qt = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column half
+        const int qt = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column group
         uint32_t acount = 0;
         int k = 0;
         for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
             const int sl = k & 1;
             bool mine = mbar_wait(&S.meta_full[sl], (k >> 1) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
-            const NodeMeta &M = S.meta[sl];
+            NodeMeta &M = S.meta[sl];
             uint32_t *mask = S.mask[sl];
             const int nch = (int)M.nch;
+            if (RULE == 0) { // column values pd - |p|^2 in place of pd (the scan reads distances from the keys)
+                for (int c = (warp - 2) * 32 + lane; c < nch * PC; c += EPI * 32)
+                    M.pd[c] = __fsub_rn(M.pd[c], M.nrm[c]);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.bound_ready[sl]);
+                mine = mbar_wait(&S.bound_ready[sl], (k >> 1) & 1);
+                if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
+            }
             for (int J = 0; J < nch && ok; ++J) {
                 const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
                 const float n_t = M.nrm[t], td = M.pd[t];
@@ -373,18 +387,14 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                     const int b = (int)(acount % NACC);
                     mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
                     fence_after();
-                    const bool skip = I == J && 64 * h + 63 <= 32 * qt; // no column after any row of the warp
-                    uint32_t raw[64];
+                    const bool skip = I == J && CW * h + CW - 1 <= 32 * qt; // no column after any row of the warp
+                    uint32_t raw[CW];
                     if (mine && !skip) {
-                        const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC + 64 * h);
-                        tmem_ld16_async(ta, raw);
-                        tmem_ld16_async(ta + 16, raw + 16);
-                        tmem_ld16_async(ta + 32, raw + 32);
-                        tmem_ld16_async(ta + 48, raw + 48);
-                        tmem_wait_ld16(raw);
-                        tmem_wait_ld16(raw + 16);
-                        tmem_wait_ld16(raw + 32);
-                        tmem_wait_ld16(raw + 48);
+                        const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC + CW * h);
+#pragma unroll
+                        for (int x = 0; x < CW / 16; ++x) tmem_ld16_async(ta + 16 * x, raw + 16 * x);
+#pragma unroll
+                        for (int x = 0; x < CW / 16; ++x) tmem_wait_ld16(raw + 16 * x);
                     }
                     // the accumulator is in registers: release it before the bit work
                     fence_before();
@@ -395,8 +405,8 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                         break;
                     }
 #pragma unroll
-                    for (int ww = 0; ww < 2; ++ww) {
-                        const int p0 = I * PC + 64 * h + 32 * ww; // first candidate of the word
+                    for (int ww = 0; ww < WPT; ++ww) {
+                        const int p0 = I * PC + CW * h + 32 * ww; // first candidate of the word
                         uint32_t word = 0;
                         if (!skip) {
                             const float4 *np4 = reinterpret_cast<const float4 *>(M.nrm + p0);
@@ -420,7 +430,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                                 word = r < 0 ? word : r >= 31 ? 0u : word & ~((2u << r) - 1u);
                             }
                         }
-                        mask[mask_base(4 * I + 2 * h + ww) + t] = word;
+                        mask[mask_base(4 * I + CW / 32 * h + ww) + t] = word;
                     }
                 }
             }
@@ -450,7 +460,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                 for (;;) {
                     if (lane == 0) {
                         gi[nk] = kcna_key_id(keys[t]);
-                        gd[nk] = M.pd[t];
+                        gd[nk] = kcna_key_dist(keys[t]);
                         cc += (unsigned long long)nk; // a kept candidate was tested against every earlier one
                     }
                     ++nk;
