@@ -111,7 +111,10 @@ struct PgArgs {
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// wait_group covers committed groups only: commit whatever is outstanding first
+__device__ __forceinline__ void cp_async_wait_0() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
 // A word whose sign bit says whether t occludes p, from the Gram entry g:
 // |t|^2 - 2g + |p|^2 is exact in Gram-exact mode, and the sign of its
