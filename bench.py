@@ -353,6 +353,7 @@ def run_gpu(args, ws, rank, local):
                    "iter_cand_M": [round(x / 1e6, 1) for x in st["iter_cand"]],
                    "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]],
                    "bf16_rows": st["bf16_rows"], "seed_ms": round(st["seed_total_ms"], 1),
+                   "seed_train_ms": round(st["seed_train_ms"], 1),
                    "seed_recall": round(st["seed_recall"], 4),
                    "plain_fp32_s": round(plain_ms / 1000.0, 4) if plain_ms else None,
                    "plain_fp32_knn_recall_at_K": round(plain_stats[-1]["loop_recall"][-1], 4) if plain_ms else None,

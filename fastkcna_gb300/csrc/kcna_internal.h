@@ -143,8 +143,6 @@ kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);  // iter 0: init lists
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr);
-// TMA tensor map (128 bytes, a CUtensorMap) of the BF16 rows (kcna_tmap.cu).
-kcna_status kcna_rows_tmap(kcna_ctx *c, void *out128);
 // Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
 bool kcna_prune_tc_ok(const kcna_ctx *c, int range, int maxc);
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,

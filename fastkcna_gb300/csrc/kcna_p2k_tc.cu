@@ -21,16 +21,16 @@
 // join (kcna_join_tc.cu):
 //   warp 0      producer: walks the block's range of nodes, packs tiles, copies
 //               pusher / neighbour ids into the tile stage with cp.async, then
-//               gathers their BF16 rows with TMA (tile::gather4) and radius /
-//               norm with cp.async; a tile with no rows ends the stream.
+//               radius, norm and isnew flags; a tile with no rows ends the
+//               stream.
+//   warps 10-13 row loaders: the pushers' and neighbours' BF16 rows by 16-byte
+//               cp.async in the 128-byte swizzled K-major layout.
 //   warp 1      MMA issuer: M = 128, N = columns used rounded up to 16.
 //   warps 2-9   epilogue: warp w reads TMEM lanes 32*(w%4).. (pushers) and
 //               every second 16-column group of the span its lanes' nodes
 //               cover; per thread a count pass, one atomicAdd on the pusher's
 //               candidate count, and a write pass reading TMEM again.
 #include <algorithm>
-
-#include <cuda.h>
 
 #include "kcna_internal.h"
 #include "kcna_tc.cuh"
@@ -39,7 +39,9 @@ using namespace kcna_tc;
 
 namespace {
 
-constexpr int PW_WARPS = 10;
+constexpr int LOAD_WARP = 10; // first row-loader warp
+constexpr int NLOAD = 4;      // row-loader warps
+constexpr int PW_WARPS = LOAD_WARP + NLOAD;
 constexpr int PW_THREADS = PW_WARPS * 32;
 constexpr int PM = 128;                      // pusher rows per tile (MMA M)
 constexpr int PN = 256;                      // neighbour columns per tile (MMA N at most)
@@ -62,7 +64,7 @@ struct StageMeta {
 };
 
 struct PwShared {
-    uint64_t tile_full[TS], tile_empty[TS], acc_full[NACC], acc_empty[NACC];
+    uint64_t ids_ready[TS], meta_full[TS], tile_full[TS], tile_empty[TS], acc_full[NACC], acc_empty[NACC];
     uint32_t tmem;
     volatile int abort_flag;
     StageMeta meta[TS];
@@ -84,38 +86,22 @@ struct P2kArgs {
     int *err;
 };
 
-// rows of `count` ids (masked to 31 bits) -> a region whose K blocks are
-// `rrows` rows apart, by TMA gather4 (four rows of one K block per
-// instruction; the last group repeats its last row); lane-strided.  Returns
-// the transaction bytes.
-__device__ __forceinline__ uint32_t tma_rows(uint32_t region, uint32_t rrows, const uint32_t *ids, int count,
-                                             const void *tmap, int nkb, uint64_t *bar, int lane) {
-    const int ng = (count + 3) >> 2;
-    for (int e = lane; e < ng * nkb; e += 32) {
-        const int g = nkb == 2 ? e >> 1 : e, kb = nkb == 2 ? e & 1 : 0;
-        const int r = 4 * g, last = count - 1;
-        tma_gather4(region + (uint32_t)kb * rrows * KBB + (uint32_t)r * KBB, tmap, 64 * kb,
-                    (int)(ids[r] & 0x7FFFFFFFu), (int)(ids[min(r + 1, last)] & 0x7FFFFFFFu),
-                    (int)(ids[min(r + 2, last)] & 0x7FFFFFFFu), (int)(ids[min(r + 3, last)] & 0x7FFFFFFFu), bar);
-    }
-    return (uint32_t)(ng * 4 * nkb) * KBB;
-}
-
-__global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const __grid_constant__ CUtensorMap tmap) {
+__global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t tiles_s = (smem_u32(smem_raw) + 1023u) & ~1023u;
     unsigned char *tiles = smem_raw + (tiles_s - smem_u32(smem_raw));
     PwShared &S = *reinterpret_cast<PwShared *>(tiles + TS * STAGE);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nkb = (a.ldh + 63) >> 6;
-    const void *tm = &tmap;
 
     for (int i = tid; i < (int)(TS * STAGE / 16); i += PW_THREADS)
         reinterpret_cast<uint4 *>(tiles)[i] = make_uint4(0, 0, 0, 0);
     if (warp == 1) tmem_alloc(&S.tmem, NACC * PN);
     if (tid == 0) {
         for (int i = 0; i < TS; ++i) {
-            mbar_init(&S.tile_full[i], 33); // producer lanes' copies + the producer's expect_tx (metadata, rows)
+            mbar_init(&S.ids_ready[i], 1);          // producer lane 0 once the ids have landed
+            mbar_init(&S.meta_full[i], 64);         // producer lanes: stores done, radius / norm copies landed
+            mbar_init(&S.tile_full[i], NLOAD * 32); // every loader lane, after its copies and a proxy fence
             mbar_init(&S.tile_empty[i], 9); // MMA commit + epilogue warps
         }
         for (int i = 0; i < NACC; ++i) {
@@ -148,10 +134,15 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const 
             return true;
         };
         auto close_tile = [&]() {
-            // ids landed: gather rows, radius and norms, then publish
+            // ids landed: announce them to the loaders, then radius, norms and flags
             asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
             __syncwarp();
-            const uint32_t base = tiles_s + st * STAGE;
+            if (lane == 0) {
+                M->rows = rows;
+                M->cols = cols;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.ids_ready[st]);
             for (uint32_t i = lane; i < rows; i += 32) {
                 const uint32_t u = M->row_id[i] & 0x7FFFFFFFu;
                 cp_async4(smem_u32(&M->row_rad[i]), a.radius + u);
@@ -167,20 +158,8 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const 
 #pragma unroll
             for (int k2 = 0; k2 < PN / 32; ++k2)
                 if (lane + 32 * k2 < cols) M->col_new[lane + 32 * k2] = fl[k2];
-            if (lane == 0) {
-                M->rows = rows;
-                M->cols = cols;
-            }
-            mbar_arrive_cp_async(&S.tile_full[st]);
-            __syncwarp();
-            if (lane == 0)
-                mbar_arrive_expect_tx(&S.tile_full[st],
-                                      rows ? (uint32_t)(((rows + 3) / 4 + (cols + 3) / 4) * 4 * nkb) * KBB : 0u);
-            __syncwarp();
-            if (rows) {
-                tma_rows(base, PM, M->row_id, (int)rows, tm, nkb, &S.tile_full[st], lane);
-                tma_rows(base + ROWS_A, PN, M->col_id, (int)cols, tm, nkb, &S.tile_full[st], lane);
-            }
+            mbar_arrive_cp_async(&S.meta_full[st]); // when this lane's copies have landed
+            mbar_arrive(&S.meta_full[st]);          // this lane's stores
             ++tcount;
         };
         ok = open_tile();
@@ -229,6 +208,40 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const 
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
         if (!ok) S.abort_flag = 1;
+    } else if (warp >= LOAD_WARP) {
+        // --------------------------------------------------------- row loaders
+        // pushers' and neighbours' BF16 rows by 16-byte cp.async into the
+        // stage's 128-byte swizzled K-major regions
+        const int lw = warp - LOAD_WARP;
+        const int nseg = a.ldh >> 3, seg = lane & 15;
+        for (uint32_t t = 0;; ++t) {
+            const int st = (int)(t % TS);
+            if (!mbar_wait(&S.ids_ready[st], (t / TS) & 1) || S.abort_flag) { ok = false; break; }
+            const StageMeta &M = S.meta[st];
+            const int rows = (int)M.rows, cols = (int)M.cols;
+            const uint32_t base = tiles_s + (uint32_t)st * STAGE;
+            if (seg < nseg) {
+                for (int k = 0; k < PM / (2 * NLOAD); ++k) {
+                    const int r = PM / NLOAD * lw + 2 * k + (lane >> 4);
+                    if (r < rows)
+                        cp_async16(base + (uint32_t)(seg >> 3) * PM * KBB + sw128_off((uint32_t)r, (uint32_t)(seg & 7)),
+                                   a.Xh + (uint64_t)(M.row_id[r] & 0x7FFFFFFFu) * a.ldh + seg * 8);
+                }
+                for (int k = 0; k < PN / (2 * NLOAD); ++k) {
+                    const int cc = PN / NLOAD * lw + 2 * k + (lane >> 4);
+                    if (cc < cols)
+                        cp_async16(base + ROWS_A + (uint32_t)(seg >> 3) * PN * KBB +
+                                       sw128_off((uint32_t)cc, (uint32_t)(seg & 7)),
+                                   a.Xh + (uint64_t)M.col_id[cc] * a.ldh + seg * 8);
+                }
+            }
+            asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+            fence_proxy_async(); // the copies, for the tensor cores' reads
+            mbar_arrive(&S.tile_full[st]);
+            if (rows == 0) break;
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (!ok) S.abort_flag = 1;
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA issuer
         if (lane == 0) {
@@ -260,7 +273,7 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a, const 
         unsigned long long cc = 0;
         for (uint32_t t = 0;; ++t) {
             const int st = (int)(t % TS), b = (int)(t % NACC);
-            bool mine = mbar_wait(&S.tile_full[st], (t / TS) & 1) && !S.abort_flag;
+            bool mine = mbar_wait(&S.meta_full[st], (t / TS) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
             const StageMeta &M = S.meta[st];
             const uint32_t rows = M.rows;
@@ -370,9 +383,7 @@ kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t 
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(p2k_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                              "p2k_tc smem attr"));
     const uint32_t grid = (uint32_t)std::max(c->num_sms, 1);
-    alignas(64) CUtensorMap tmap;
-    KCNA_TRY(kcna_rows_tmap(c, &tmap));
-    p2k_tc_kernel<<<grid, PW_THREADS, sm, c->stream>>>(a, tmap);
+    p2k_tc_kernel<<<grid, PW_THREADS, sm, c->stream>>>(a);
     KCNA_LAUNCHED(c);
     return kcna_cuda_check(c, cudaGetLastError(), "p2k_tc_kernel");
 }
