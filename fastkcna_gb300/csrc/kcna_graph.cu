@@ -213,9 +213,13 @@ __global__ void rev_count_kernel(const uint32_t *__restrict__ g_ids, const uint3
     uint32_t des = g_ids[t];
     if (des < N) atomicAdd(indeg + des, 1u);
 }
-__global__ void rev_fill_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg, uint32_t N,
-                                uint32_t W, const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
-                                uint32_t *__restrict__ rev) {
+// Reverse edge n -> des as (n << 32 | distance bits): the distance of the
+// kept edge is the canonical d(n, des), equal bit for bit to d(des, n), so
+// InterInsert needs no distance evaluation.
+__global__ void rev_fill_kernel(const uint32_t *__restrict__ g_ids, const float *__restrict__ g_dist,
+                                const uint32_t *__restrict__ g_deg, uint32_t N, uint32_t W,
+                                const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                                uint64_t *__restrict__ rev) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (uint64_t)N * W) return;
     uint32_t n = (uint32_t)(t / W), j = (uint32_t)(t % W);
@@ -223,7 +227,7 @@ __global__ void rev_fill_kernel(const uint32_t *__restrict__ g_ids, const uint32
     uint32_t des = g_ids[t];
     if (des >= N) return;
     uint32_t p = atomicAdd(cursor + des, 1u);
-    rev[off[des] + p] = n;
+    rev[off[des] + p] = ((uint64_t)n << 32) | __float_as_uint(g_dist[t]);
 }
 
 // exclusive scan of u32 counts into u64 offsets (3 phases)
@@ -288,9 +292,9 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
                                                        uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
                                                        uint32_t *__restrict__ g_deg, uint32_t W,
                                                        const uint64_t *__restrict__ off,
-                                                       const uint32_t *__restrict__ rev,
+                                                       const uint64_t *__restrict__ rev,
                                                        unsigned long long *comps, int *err) {
-    __shared__ uint64_t s_key[LCAP];   // sorting keys (rev ids; later (dist, position))
+    __shared__ uint64_t s_key[LCAP];   // sorting keys (rev (id, dist); later (dist, position))
     __shared__ uint32_t s_id[LCAP];
     __shared__ float s_d[LCAP];
     __shared__ uint32_t s_kid[128];
@@ -308,9 +312,9 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
         s_id[j] = g_ids[(uint64_t)q * W + j];
         s_d[j] = g_dist[(uint64_t)q * W + j];
     }
-    // reverse sources sorted by id
+    // reverse sources sorted by id (each with its distance in the low word)
     const int np2 = kcna_pow2_ceil_d(max(nin, 1));
-    for (int j = threadIdx.x; j < np2; j += LT) s_key[j] = j < nin ? (uint64_t)rev[r0 + j] : KCNA_EMPTY_KEY;
+    for (int j = threadIdx.x; j < np2; j += LT) s_key[j] = j < nin ? rev[r0 + j] : KCNA_EMPTY_KEY;
     kcna_cta_bitonic(s_key, np2);
     // keep sources not in the pruned list (InterInsert dup check, :2064-2071)
     int keep_local = 0;
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
     const int b = threadIdx.x * per;
     uint32_t flags = 0;
     for (int e = 0; e < per && b + e < nin; ++e) {
-        uint32_t src = (uint32_t)s_key[b + e];
+        uint32_t src = (uint32_t)(s_key[b + e] >> 32);
         bool dup = false;
         for (int j = 0; j < deg; ++j)
             if (s_id[j] == src) {
@@ -353,9 +357,8 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
     int pos = deg + (int)s_warp[w] + incl - keep_local;
     for (int e = 0; e < per && b + e < nin; ++e)
         if (flags & (1u << e)) {
-            uint32_t src = (uint32_t)s_key[b + e];
-            s_id[pos] = src;
-            s_d[pos] = rows_l2(rows, src, q); // oracle(n, des)
+            s_id[pos] = (uint32_t)(s_key[b + e] >> 32);
+            s_d[pos] = __uint_as_float((uint32_t)s_key[b + e]); // oracle(n, des), from the reverse edge
             ++pos;
         }
     const int total = deg + s_nk;
@@ -1023,7 +1026,8 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     const uint64_t N = c->n;
     const uint32_t W = c->W;
     // reverse-edge CSR: in-degree count, scan, fill
-    uint32_t *indeg = nullptr, *cursor = nullptr, *rev = nullptr;
+    uint32_t *indeg = nullptr, *cursor = nullptr;
+    uint64_t *rev = nullptr;
     uint64_t *off = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
@@ -1043,8 +1047,8 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     uint64_t E = 0;
     if ((s = exclusive_scan(c, indeg, N, off, &E)) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &rev, std::max<uint64_t>(E, 1), "reverse edges")) != KCNA_OK) return cleanup(), s;
-    rev_fill_kernel<<<kcna_div_up(N * W, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, (uint32_t)N, W, off, cursor,
-                                                                     rev);
+    rev_fill_kernel<<<kcna_div_up(N * W, 256), 256, 0, c->stream>>>(c->g_ids, c->g_dist, c->g_deg, (uint32_t)N, W,
+                                                                     off, cursor, rev);
     KCNA_LAUNCHED(c);
     PruneRule rule = make_rule(p, kind);
     cudaMemsetAsync(c->counters + 17, 0, 8, c->stream);
