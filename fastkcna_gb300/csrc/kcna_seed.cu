@@ -193,17 +193,23 @@ __global__ void bucket_scatter_kernel(const uint32_t *__restrict__ bucket, int64
     rank[tab * rows + r] = (uint32_t)pos;
 }
 
-// Initial pool of node i: sorted union of its +-SEED_WIN neighbours in every table order
-__global__ void __launch_bounds__(128) seed_pools_kernel(const float *__restrict__ X, int ld, uint32_t N,
-                                                         const uint32_t *__restrict__ order,
+// Initial pool of node i: sorted union of its +-SEED_WIN neighbours in every
+// table order, with canonical distances (the node's row staged in shared
+// memory; candidate rows read through R, the BF16 copy when it is exact).
+template <class R>
+__global__ void __launch_bounds__(128) seed_pools_kernel(R rows, uint32_t N, const uint32_t *__restrict__ order,
                                                          const uint32_t *__restrict__ rank, uint32_t cap,
                                                          uint32_t limit, uint64_t *__restrict__ pool,
                                                          uint32_t *__restrict__ pool_cnt,
                                                          unsigned long long *comps) {
     __shared__ uint64_t s_k[4][SEED_CAND];
+    extern __shared__ __align__(16) float s_row[]; // 4 warps x ld
     const int w = threadIdx.x >> 5, lane = kcna_lane();
     const uint32_t i = blockIdx.x * 4 + w;
     if (i >= N) return;
+    const int nv = rows.ld >> 2;
+    float4 *own = reinterpret_cast<float4 *>(s_row) + (size_t)w * nv;
+    for (int k = lane; k < nv; k += 32) own[k] = rows.ld4(i, k);
     uint64_t *sk = s_k[w];
     for (int e = lane; e < SEED_CAND; e += 32) {
         const int tab = e / (2 * SEED_WIN), off = e % (2 * SEED_WIN);
@@ -225,8 +231,16 @@ __global__ void __launch_bounds__(128) seed_pools_kernel(const float *__restrict
         if (ok) {
             ++cc;
             const uint32_t id = (uint32_t)v;
-            keys[h] = kcna_key(kcna_l2_ldg(X + (uint64_t)id * ld, X + (uint64_t)i * ld, ld), id,
-                               (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+            float acc = 0.f;
+            for (int k0 = 0; k0 < nv; k0 += 8) { // eight loads in flight
+                float4 y[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) y[u] = k0 + u < nv ? rows.ld4(id, k0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (k0 + u < nv) acc = kcna_acc4(acc, y[u], own[k0 + u]);
+            }
+            keys[h] = kcna_key(acc, id, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
         }
     }
     __syncwarp();
@@ -481,8 +495,13 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     // --- 4. initial pools
     const uint32_t limit = std::min(p->L, c->cap);
     cudaMemsetAsync(c->counters + 30, 0, 8, s);
-    seed_pools_kernel<<<kcna_div_up(N, 4), 128, 0, s>>>(c->X, (int)ld, N, order, rank, c->cap, limit, c->pool,
-                                                        c->pool_cnt, c->counters + 30);
+    const size_t srow = (size_t)4 * ld * 4;
+    if (c->bf16_exact)
+        seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsB16{c->Xh, (int)ld}, N, order, rank, c->cap, limit,
+                                                               c->pool, c->pool_cnt, c->counters + 30);
+    else
+        seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsF32{c->X, (int)ld}, N, order, rank, c->cap, limit,
+                                                               c->pool, c->pool_cnt, c->counters + 30);
     KCNA_TRY(launch_ok(c, "seed pools"));
     unsigned long long h = 0;
     cudaMemcpyAsync(&h, c->counters + 30, 8, cudaMemcpyDeviceToHost, s);
