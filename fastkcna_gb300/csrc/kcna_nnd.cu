@@ -327,7 +327,8 @@ struct MergeArgs {
 // few survivors are sorted, deduplicated and merged, and only the pool entries
 // they displace are written.  A node with more than MW_SURV survivors is
 // queued for the block merge (merge_kernel).  Same result as merging all
-// candidates.
+// candidates.  Persistent: each warp takes nodes grid-stride, so a block
+// meets its barrier once at the end instead of waiting for its slowest node.
 constexpr int MW_WARPS = 8, MW_SURV = 512;
 
 __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, uint32_t N, uint32_t *big_list,
@@ -342,8 +343,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
     if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t node = blockIdx.x * MW_WARPS + w;
-    if (node < N) {
+    for (uint32_t node = blockIdx.x * MW_WARPS + w; node < N; node += gridDim.x * MW_WARPS) {
         const uint32_t raw = a.cand_cnt[node];
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
@@ -434,6 +434,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 a.radius[node] = newcnt >= a.limit ? kcna_key_dist(*s_last) : __uint_as_float(0x7F800000u);
             }
         }
+        __syncwarp(); // the next node reuses this warp's shared memory
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1000,8 +1001,13 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->big_cnt, 0, 4, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
-    merge_warp_kernel<<<kcna_div_up(c->n, MW_WARPS), MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list,
-                                                                                      c->big_cnt);
+    int mw_per_sm = 0;
+    KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mw_per_sm, merge_warp_kernel,
+                                                                             MW_WARPS * 32, smw),
+                             "merge occupancy"));
+    const uint32_t mw_grid = (uint32_t)std::min<uint64_t>(kcna_div_up(c->n, MW_WARPS),
+                                                          (uint64_t)std::max(c->num_sms, 1) * std::max(mw_per_sm, 1));
+    merge_warp_kernel<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
     merge_kernel<<<std::max(1, c->num_sms) * 4, MT, sm, c->stream>>>(a, c->big_list, c->big_cnt);
     c->launches += 2;
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
