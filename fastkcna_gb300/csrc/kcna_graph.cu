@@ -293,7 +293,8 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
                                                        uint32_t *__restrict__ g_deg, uint32_t W,
                                                        const uint64_t *__restrict__ off,
                                                        const uint64_t *__restrict__ rev,
-                                                       unsigned long long *comps, int *err) {
+                                                       unsigned long long *comps, int *err,
+                                                       const uint32_t *__restrict__ nodes) {
     __shared__ uint64_t s_key[LCAP];   // sorting keys (rev (id, dist); later (dist, position))
     __shared__ uint32_t s_id[LCAP];
     __shared__ float s_d[LCAP];
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
     __shared__ float s_kd[128];
     __shared__ uint32_t s_warp[LT / 32];
     __shared__ int s_nk;
-    const uint32_t q = blockIdx.x;
+    const uint32_t q = nodes ? nodes[blockIdx.x] : blockIdx.x;
     const int deg = (int)g_deg[q];
     const uint64_t r0 = off[q], r1 = off[q + 1];
     const uint64_t room = (uint64_t)(LCAP - deg);
@@ -395,6 +396,101 @@ __global__ void __launch_bounds__(LT) link_merge_kernel(R rows, uint32_t N, Prun
             g_dist[(uint64_t)q * W + j] = j < nk ? s_kd[j] : 0.f;
         }
         if (lane == 0) g_deg[q] = nk;
+    }
+}
+
+// Warp per node, persistent: the same InterInsert merge and reversed prune as
+// link_merge_kernel for the common node whose pruned list and reverse
+// sources fit LW_CAP entries; larger nodes are queued for the block kernel.
+constexpr int LW_WARPS = 4, LW_CAP = 256;
+
+template <class R>
+__global__ void __launch_bounds__(LW_WARPS * 32) link_warp_kernel(R rows, uint32_t N, PruneRule rule, int range,
+                                                                 uint32_t *__restrict__ g_ids,
+                                                                 float *__restrict__ g_dist,
+                                                                 uint32_t *__restrict__ g_deg, uint32_t W,
+                                                                 const uint64_t *__restrict__ off,
+                                                                 const uint64_t *__restrict__ rev,
+                                                                 unsigned long long *comps, uint32_t *big_list,
+                                                                 uint32_t *big_cnt) {
+    __shared__ uint64_t s_key[LW_WARPS][LW_CAP];
+    __shared__ uint32_t s_id[LW_WARPS][LW_CAP];
+    __shared__ float s_d[LW_WARPS][LW_CAP];
+    __shared__ uint32_t s_kid[LW_WARPS][128];
+    __shared__ float s_kd[LW_WARPS][128];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    uint64_t *key = s_key[w];
+    uint32_t *ids = s_id[w];
+    float *ds = s_d[w];
+    for (uint32_t q = blockIdx.x * LW_WARPS + w; q < N; q += gridDim.x * LW_WARPS) {
+        const int deg = (int)min(g_deg[q], W);
+        const uint64_t r0 = off[q], r1 = off[q + 1];
+        const int nin = (int)(r1 - r0);
+        if (deg + nin > LW_CAP) {
+            if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = q;
+            continue;
+        }
+        for (int j = lane; j < deg; j += 32) {
+            ids[j] = g_ids[(uint64_t)q * W + j];
+            ds[j] = g_dist[(uint64_t)q * W + j];
+        }
+        // reverse sources (id << 32 | distance) sorted by id
+        const int np2 = kcna_pow2_ceil_d(max(nin, 1));
+        for (int j = lane; j < np2; j += 32) key[j] = j < nin ? rev[r0 + j] : KCNA_EMPTY_KEY;
+        kcna_warp_bitonic(key, np2);
+        // sources not in the pruned list, appended in id order (InterInsert, :2064-2071)
+        int total = deg;
+        for (int b0 = 0; b0 < nin; b0 += 32) {
+            const int j = b0 + lane;
+            bool keep = false;
+            uint64_t k = 0;
+            if (j < nin) {
+                k = key[j];
+                const uint32_t src = (uint32_t)(k >> 32);
+                keep = true;
+                for (int t = 0; t < deg; ++t)
+                    if (ids[t] == src) {
+                        keep = false;
+                        break;
+                    }
+            }
+            const unsigned m = __ballot_sync(KCNA_FULL, keep);
+            if (keep) {
+                const int pos = total + __popc(m & kcna_lanemask_lt());
+                ids[pos] = (uint32_t)(k >> 32);
+                ds[pos] = __uint_as_float((uint32_t)k); // oracle(n, des), from the reverse edge
+            }
+            total += __popc(m);
+        }
+        __syncwarp();
+        uint32_t *gi = g_ids + (uint64_t)q * W;
+        float *gd = g_dist + (uint64_t)q * W;
+        if (total <= range) {
+            for (int j = lane; j < (int)W; j += 32) {
+                gi[j] = j < total ? ids[j] : KCNA_NONE;
+                gd[j] = j < total ? ds[j] : 0.f;
+            }
+            if (lane == 0) g_deg[q] = (uint32_t)total;
+            continue;
+        }
+        // reversed prune: stable sort by distance, then the occlusion scan without the search_K cap
+        const int tp = kcna_pow2_ceil_d(total);
+        for (int j = lane; j < tp; j += 32)
+            key[j] = j < total ? (((uint64_t)__float_as_uint(ds[j]) << 32) | (uint32_t)j) : KCNA_EMPTY_KEY;
+        kcna_warp_bitonic(key, tp);
+        auto get = [&](int i, uint32_t &id, float &dd) {
+            const uint32_t p = (uint32_t)key[i];
+            id = ids[p];
+            dd = ds[p];
+        };
+        const int first = ids[(uint32_t)key[0]] == q ? 1 : 0;
+        const int nk = warp_prune(rows, 0xFFFFFFFFu, rule, first, total, range, get, s_kid[w], s_kd[w], comps);
+        for (int j = lane; j < (int)W; j += 32) {
+            gi[j] = j < nk ? s_kid[w][j] : KCNA_NONE;
+            gd[j] = j < nk ? s_kd[w][j] : 0.f;
+        }
+        if (lane == 0) g_deg[q] = (uint32_t)nk;
+        __syncwarp();
     }
 }
 
@@ -1052,16 +1148,37 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     KCNA_LAUNCHED(c);
     PruneRule rule = make_rule(p, kind);
     cudaMemsetAsync(c->counters + 17, 0, 8, c->stream);
+    // warp per node for the common node, the block kernel for the few larger ones
+    uint32_t *blist = nullptr, *bcnt = nullptr;
+    if ((s = kcna_alloc(c, &blist, N + 1, "link big list")) != KCNA_OK) return cleanup(), s;
+    bcnt = blist + N;
+    cudaMemsetAsync(bcnt, 0, 4, c->stream);
+    auto launch_link = [&](auto rows) -> kcna_status {
+        int per_sm = 0;
+        KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, link_warp_kernel<decltype(rows)>,
+                                                                                 LW_WARPS * 32, 0),
+                                 "link occupancy"));
+        const uint32_t grid = (uint32_t)std::min<uint64_t>(kcna_div_up(N, LW_WARPS),
+                                                           (uint64_t)std::max(c->num_sms, 1) * std::max(per_sm, 1));
+        link_warp_kernel<<<grid, LW_WARPS * 32, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids,
+                                                                c->g_dist, c->g_deg, W, off, rev, c->counters + 17,
+                                                                blist, bcnt);
+        KCNA_LAUNCHED(c);
+        uint32_t hb = 0;
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb, bcnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync"));
+        if (hb > 0) {
+            link_merge_kernel<<<hb, LT, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids, c->g_dist,
+                                                        c->g_deg, W, off, rev, c->counters + 17, c->d_err, blist);
+            KCNA_LAUNCHED(c);
+        }
+        return kcna_cuda_check(c, cudaGetLastError(), "link kernels");
+    };
     if (c->bf16_exact)
-        link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(RowsB16{c->Xh, (int)c->ld}, (uint32_t)N, rule,
-                                                             (int)p->nsg_R, c->g_ids, c->g_dist, c->g_deg, W, off, rev,
-                                                             c->counters + 17, c->d_err);
+        s = launch_link(RowsB16{c->Xh, (int)c->ld});
     else
-        link_merge_kernel<<<(uint32_t)N, LT, 0, c->stream>>>(RowsF32{c->X, (int)c->ld}, (uint32_t)N, rule,
-                                                             (int)p->nsg_R, c->g_ids, c->g_dist, c->g_deg, W, off, rev,
-                                                             c->counters + 17, c->d_err);
-    KCNA_LAUNCHED(c);
-    s = kcna_cuda_check(c, cudaGetLastError(), "link kernels");
+        s = launch_link(RowsF32{c->X, (int)c->ld});
+    cudaFree(blist);
     unsigned long long h = 0;
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 17, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
