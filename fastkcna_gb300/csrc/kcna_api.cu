@@ -564,7 +564,8 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
         kcna_log(c, &P, "P2K %d: recall@MAXL %.4f t %.3f", loopcount, r, kcna_now() - s0);
     }
     st->loops = (uint32_t)loopcount;
-    st->prune_tc = kcna_prune_tc_ok(c, (int)P.nsg_R, (int)std::min(P.search_K, c->cap)) ? 1u : 0u;
+    st->prune_tc = kcna_prune_tc_ok(c, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, (int)P.nsg_R,
+                                    (int)std::min(P.search_K, c->cap)) ? 1u : 0u;
     st->prune_comps = prune_comps;
     st->bridge_comps = bridge_comps;
     KCNA_TRY(degree_stats(c, st));

@@ -1093,7 +1093,7 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     const size_t sm = (size_t)PW * 2 * range * 4;
     const int maxc = (int)std::min(p->search_K, c->cap);
     KCNA_TRY(kcna_phase_begin(c));
-    if (kcna_prune_tc_ok(c, (int)range, maxc)) { // Gram-exact rows: occlusion masks from tensor-core tiles
+    if (kcna_prune_tc_ok(c, kind, (int)range, maxc)) { // Gram-exact rows: occlusion masks from tensor-core tiles
         KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, rule.thr, (int)range, maxc, c->counters + 16));
     } else {
         if (c->bf16_exact)

@@ -144,7 +144,7 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr);
 // Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
-bool kcna_prune_tc_ok(const kcna_ctx *c, int range, int maxc);
+bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc);
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
                                  unsigned long long *comps);
 // P2K join on tcgen05 Gram tiles (kcna_p2k_tc.cu); requires c->gram_exact.

@@ -1,12 +1,11 @@
 // kcna_prune_tc.cu - occlusion prune on tcgen05 Gram tiles.
 //
 // Same result as prune_kernel (kcna_graph.cu; reference nsg_sync_prune
-// src/kgraph.cpp:1809-1851, taumg_sync_prune :2833-2876, alphapg_sync_prune
-// :3157-3203): the candidates of node q are pool[first .. lim) in order; the
+// src/kgraph.cpp:1809-1851, taumg_sync_prune :2833-2876) for the RNG and
+// tau-MNG rules: the candidates of node q are pool[first .. lim) in order; the
 // first is kept; a later candidate p is dropped when an already kept t
-// occludes it (RNG: d(t,p) < d(q,p); tau-MNG: d(t,p) < d(q,p) - 3 tau;
-// alpha-PG: d(t,p) < d(q,p) and the angle test), and the scan stops at range
-// kept.  The kernel runs only in Gram-exact mode (integer rows, squared norms
+// occludes it (RNG: d(t,p) < d(q,p); tau-MNG: d(t,p) < d(q,p) - 3 tau), and
+// the scan stops at range kept.  The kernel runs only in Gram-exact mode (integer rows, squared norms
 // below 2^23), where the tile distances (|x|^2 + |y|^2) - 2 <x, y> (BF16
 // rows, FP32 accumulation in TMEM) equal the canonical FMA-chain distances,
 // so the kept lists are identical.
@@ -126,16 +125,13 @@ __device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float
     if (RULE == 0) return __float_as_uint(__fsub_rn(__fmaf_rn(-2.f, g, nt), pd)); // pd holds pd - |p|^2
     const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
     if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, t3))); // src/kgraph.cpp:2859
-    const uint32_t s = __float_as_uint(__fsub_rn(dd, pd));
-    if (RULE == 2 && (s >> 31)) { // alpha-PG: and the angle at t (src/kgraph.cpp:3184-3186)
-        const float num = __fdiv_rn(__fsub_rn(__fadd_rn(td, dd), pd), 2.0f);
-        const float cs = __fdiv_rn(num, __fsqrt_rn(__fmul_rn(td, dd)));
-        return cs < thr ? 0x80000000u : 0u;
-    }
-    return s;
+    return __float_as_uint(__fsub_rn(dd, pd));
 }
 
-// RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG, 2 alpha-PG
+// RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG.  alpha-PG is left to the FP32
+// prune: its angle test (two IEEE divisions and a square root) on every near
+// pair of the triangle made the tile version ten times slower than RNG (3.9 s
+// vs 0.37 s per 2M-row build, against 1.15 s for the sequential FP32 prune).
 template <int RULE>
 __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -515,14 +511,14 @@ kcna_status launch_rule(kcna_ctx *c, const PgArgs &a, uint32_t grid) {
 
 } // namespace
 
-bool kcna_prune_tc_ok(const kcna_ctx *c, int range, int maxc) {
-    return c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range >= 1 && maxc >= 1 &&
+bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc) {
+    return kind != KCNA_ALPHAPG && c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range >= 1 && maxc >= 1 &&
            maxc <= MAXC && prune_gram_smem() <= 227 * 1024;
 }
 
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
                                  unsigned long long *comps) {
-    if (!kcna_prune_tc_ok(c, range, maxc)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
+    if (!kcna_prune_tc_ok(c, kind, range, maxc)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
     PgArgs a;
     a.N = c->n;
     a.cap = c->cap;
@@ -544,6 +540,5 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int
     const uint32_t grid = (uint32_t)std::min<uint64_t>(c->n, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
     if (kind == KCNA_TAUMNG) return launch_rule<1>(c, a, grid);
-    if (kind == KCNA_ALPHAPG) return launch_rule<2>(c, a, grid);
     return launch_rule<0>(c, a, grid);
 }
