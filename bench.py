@@ -238,15 +238,22 @@ def traffic_from_profile(name):
 def search_recall10(ix, Q, truth, n, L=100):
     """Index search recall@10 of the context's graph: beam of L from the entry
     point plus L-1 seeded random nodes (the same start for every query and
-    build), against the exact 10-NN."""
+    build), against the exact 10-NN; and the queries per second of that batched
+    GPU beam search through the C ABI (host query and result buffers, median of
+    3 timed calls after one untimed)."""
     _, _, ep = ix.graph()
     rng = np.random.default_rng(7)
     extra = rng.choice(n, size=L, replace=False)
     start = np.concatenate([[ep], extra[extra != ep][: L - 1]]).astype(np.uint32)
     init = np.broadcast_to(start, (Q.shape[0], L)).copy()
     found, _ = ix.search(Q, L, 10, init_ids=init)
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ix.search(Q, L, 10, init_ids=init)
+        times.append(time.perf_counter() - t0)
     hit = sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth))
-    return hit / (10.0 * Q.shape[0])
+    return hit / (10.0 * Q.shape[0]), Q.shape[0] / statistics.median(times)
 
 
 def run_gpu(args, ws, rank, local):
@@ -278,7 +285,7 @@ def run_gpu(args, ws, rank, local):
         plain_ms = e0.elapsed_time(e1) / args.steps
         Q = synth.queries("c2", 10000)
         truth, _ = ix.knn_queries(Q, 10)
-        plain_rec10 = search_recall10(ix, Q, truth, n)
+        plain_rec10, plain_qps = search_recall10(ix, Q, truth, n)
         ix.build("nsg", p)
     # timed region: device-resident rows, one build per step
     clock = ClockSampler(local)
@@ -327,7 +334,7 @@ def run_gpu(args, ws, rank, local):
         Q = synth.queries("c2", 10000)
         truth, _ = ix.knn_queries(Q, 10)
         plain_rec10 = None
-    rec10 = search_recall10(ix, Q, truth, n)  # the graph of the last (end-to-end) build
+    rec10, qps = search_recall10(ix, Q, truth, n)  # the graph of the last (end-to-end) build
     hbm, bf16, src = peaks()
     kname, roof = roofline(st, hbm, (X.shape[1] + 3) // 4 * 4, n, FLAGS["search_K"])
     roof["peak_source"] = f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
@@ -364,6 +371,8 @@ def run_gpu(args, ws, rank, local):
                    "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None,
                    "search_recall_at_10": round(rec10, 4),
                    "plain_fp32_search_recall_at_10": round(plain_rec10, 4) if plain_rec10 is not None else None,
+                   "search_qps": round(qps),
+                   "plain_fp32_search_qps": round(plain_qps) if plain_ms else None,
                    "search": "10,000 queries, beam 100 from the entry point + 99 seeded random nodes, exact 10-NN"},
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
