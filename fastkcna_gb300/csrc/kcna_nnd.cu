@@ -349,25 +349,42 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
         const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+#pragma unroll 4
         for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
+        // candidates in groups of 128 (four per lane), the next group's loads in
+        // flight while this group is searched
+        constexpr int CG = 4;
+        uint64_t nxt[CG];
+#pragma unroll
+        for (int u = 0; u < CG; ++u) {
+            const uint32_t j = 32 * u + lane;
+            nxt[u] = j < nc ? gc[j] : KCNA_EMPTY_KEY;
+        }
         __syncwarp();
         // survivors: not in the pool, landing below limit
         uint32_t ns = 0;
-        for (uint32_t b0 = 0; b0 < nc; b0 += 32) {
-            const uint32_t j = b0 + lane;
-            bool surv = false;
-            uint64_t k = 0;
-            if (j < nc) {
-                k = kcna_key_noflags(gc[j]);
-                if (k != KCNA_EMPTY_KEY_NOFLAGS) {
+        for (uint32_t b0 = 0; b0 < nc; b0 += 32 * CG) {
+            uint64_t cur[CG];
+#pragma unroll
+            for (int u = 0; u < CG; ++u) {
+                cur[u] = nxt[u];
+                const uint32_t j = b0 + 32 * CG + 32 * u + lane;
+                nxt[u] = j < nc ? gc[j] : KCNA_EMPTY_KEY;
+            }
+#pragma unroll
+            for (int u = 0; u < CG; ++u) {
+                const uint32_t j = b0 + 32 * u + lane;
+                bool surv = false;
+                const uint64_t k = kcna_key_noflags(cur[u]);
+                if (j < nc && k != KCNA_EMPTY_KEY_NOFLAGS) {
                     const int b = kcna_lower_bound(s_pool, (int)np, k);
                     surv = (uint32_t)b < a.limit && !(b < (int)np && (s_pool[b] >> 2) == (k >> 2));
                 }
+                const unsigned m = __ballot_sync(KCNA_FULL, surv);
+                const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
+                if (surv && pos < (uint32_t)MW_SURV) s_sv[pos] = k;
+                ns += __popc(m);
             }
-            const unsigned m = __ballot_sync(KCNA_FULL, surv);
-            const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
-            if (surv && pos < (uint32_t)MW_SURV) s_sv[pos] = k;
-            ns += __popc(m);
         }
         if (ns > (uint32_t)MW_SURV) {
             if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = node;
