@@ -26,7 +26,7 @@
 namespace {
 
 constexpr int H1 = 256, H2 = 64;
-constexpr int SEED_TABLES = 16, SEED_BITS = 16, SEED_WIN = 8; // 16 tables x (2 x 8) = 256 candidates per node
+constexpr int SEED_TABLES = 16, SEED_BITS = 16, SEED_WIN = 16; // 16 tables x (2 x 16) = 512 candidates per node
 constexpr int SEED_CAND = SEED_TABLES * 2 * SEED_WIN;
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
@@ -193,8 +193,9 @@ __global__ void bucket_scatter_kernel(const uint32_t *__restrict__ bucket, int64
     rank[tab * rows + r] = (uint32_t)pos;
 }
 
-// Initial pool of node i: sorted union of its +-SEED_WIN neighbours in every
-// table order, with canonical distances (the node's row staged in shared
+// Initial pool of node i, for rows too wide for the banded kernels below:
+// sorted union of its +-SEED_WIN neighbours in every table order, with
+// canonical distances (the node's row staged in shared
 // memory; candidate rows read through R, the BF16 copy when it is exact).
 template <class R>
 __global__ void __launch_bounds__(128) seed_pools_kernel(R rows, uint32_t N, const uint32_t *__restrict__ order,
@@ -257,6 +258,88 @@ __global__ void __launch_bounds__(128) seed_pools_kernel(R rows, uint32_t N, con
         pool_cnt[i] = cnt;
         if (cc) atomicAdd(comps, cc);
     }
+}
+
+// Initial pools, step 1: in the order of table tab, every position p meets
+// positions p+1 .. p+SEED_WIN; each pair's canonical distance goes to both
+// nodes' fixed candidate slots (node a's slot tab*2W + W + delta-1 holds the
+// delta-th node after it, slot tab*2W + delta-1 the delta-th node before it).
+// A warp stages the rows of its 32 positions and the SEED_WIN after them in
+// shared memory (row pitch ld + 4 floats: the 16-byte reads of 8 lanes fall in
+// distinct banks), so each row is read from memory about 1.5 times per table
+// instead of once per candidate.
+constexpr int BAND_WARPS = 4, BAND_ROWS = 32 + SEED_WIN;
+
+template <class R>
+__global__ void __launch_bounds__(BAND_WARPS * 32) seed_band_kernel(R rows, uint32_t N, const uint32_t *__restrict__ ord,
+                                                                    int tab, uint64_t *__restrict__ slots,
+                                                                    uint32_t stride, unsigned long long *comps) {
+    extern __shared__ __align__(16) float s_rows[]; // BAND_WARPS x BAND_ROWS x pitch
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    const int nv = rows.ld >> 2, pitch4 = nv + 1;
+    float4 *sr = reinterpret_cast<float4 *>(s_rows) + (size_t)w * BAND_ROWS * pitch4;
+    const uint64_t p0 = ((uint64_t)blockIdx.x * BAND_WARPS + w) * 32;
+    if (p0 >= N) return;
+    const int nr = (int)min((uint64_t)BAND_ROWS, N - p0);
+    for (int e = lane; e < nr * nv; e += 32) {
+        const int r = e / nv, k = e - r * nv;
+        sr[r * pitch4 + k] = rows.ld4(ord[p0 + r], k);
+    }
+    __syncwarp();
+    const uint64_t p = p0 + lane;
+    unsigned long long cc = 0;
+    if (p < N) {
+        const uint32_t a = ord[p];
+        const float4 *ra = sr + lane * pitch4;
+        for (int dlt = 1; dlt <= SEED_WIN; ++dlt) {
+            if (lane + dlt >= nr) break;
+            ++cc;
+            const uint32_t b = ord[p + dlt];
+            const float4 *rb = sr + (lane + dlt) * pitch4;
+            float acc = 0.f;
+            for (int k = 0; k < nv; ++k) acc = kcna_acc4(acc, ra[k], rb[k]);
+            const uint32_t fl = (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
+            slots[(uint64_t)a * stride + tab * 2 * SEED_WIN + SEED_WIN + dlt - 1] = kcna_key(acc, b, fl);
+            slots[(uint64_t)b * stride + tab * 2 * SEED_WIN + dlt - 1] = kcna_key(acc, a, fl);
+        }
+    }
+    cc = kcna_warp_sum(cc);
+    if (lane == 0 && cc) atomicAdd(comps, cc);
+}
+
+// Initial pools, step 2: node i's slots sorted by (distance, id); the same id
+// from several tables gives the same key, so repeats are adjacent and dropped;
+// the nearest `limit` distinct entries become the pool.
+__global__ void __launch_bounds__(128) seed_collect_kernel(const uint64_t *__restrict__ slots, uint32_t stride,
+                                                           uint32_t N, uint32_t cap, uint32_t limit,
+                                                           uint64_t *__restrict__ pool,
+                                                           uint32_t *__restrict__ pool_cnt) {
+    __shared__ uint64_t s_k[4][SEED_CAND];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    const uint32_t i = blockIdx.x * 4 + w;
+    if (i >= N) return;
+    uint64_t *sk = s_k[w];
+    for (int e = lane; e < SEED_CAND; e += 32) sk[e] = slots[(uint64_t)i * stride + e];
+    kcna_warp_bitonic(sk, SEED_CAND);
+    // compaction moves entries down, so the previous key comes from registers
+    uint32_t cnt = 0;
+    uint64_t carry = KCNA_EMPTY_KEY;
+    for (int e0 = 0; e0 < SEED_CAND; e0 += 32) {
+        const uint64_t v = sk[e0 + lane];
+        uint64_t prev = __shfl_up_sync(KCNA_FULL, v, 1);
+        if (lane == 0) prev = carry;
+        carry = __shfl_sync(KCNA_FULL, v, 31);
+        const bool ok = v != KCNA_EMPTY_KEY && (e0 + lane == 0 || (prev >> 2) != (v >> 2));
+        const unsigned m = __ballot_sync(KCNA_FULL, ok);
+        __syncwarp();
+        if (ok) sk[cnt + __popc(m & kcna_lanemask_lt())] = v;
+        cnt += __popc(m);
+        __syncwarp();
+    }
+    const uint32_t keep = min(cnt, limit);
+    uint64_t *pr = pool + (uint64_t)i * cap;
+    for (uint32_t e = lane; e < cap; e += 32) pr[e] = e < keep ? sk[e] : KCNA_EMPTY_KEY;
+    if (lane == 0) pool_cnt[i] = keep;
 }
 
 __global__ void fill_u32_kernel(uint32_t *p, uint32_t v, uint64_t n) {
@@ -495,13 +578,40 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     // --- 4. initial pools
     const uint32_t limit = std::min(p->L, c->cap);
     cudaMemsetAsync(c->counters + 30, 0, 8, s);
-    const size_t srow = (size_t)4 * ld * 4;
-    if (c->bf16_exact)
-        seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsB16{c->Xh, (int)ld}, N, order, rank, c->cap, limit,
-                                                               c->pool, c->pool_cnt, c->counters + 30);
-    else
-        seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsF32{c->X, (int)ld}, N, order, rank, c->cap, limit,
-                                                               c->pool, c->pool_cnt, c->counters + 30);
+    const size_t band_smem = (size_t)BAND_WARPS * BAND_ROWS * (ld + 4) * 4;
+    if (band_smem <= 200 * 1024) { // banded: each pair once, rows read in table order
+        uint64_t *slots = c->cand;
+        uint32_t stride = c->CB;
+        if (c->CB < (uint32_t)SEED_CAND) {
+            KCNA_TRY(dev.get(&slots, (size_t)N * SEED_CAND, "seed slots"));
+            stride = SEED_CAND;
+        }
+        KCNA_TRY(kcna_cuda_check(c, cudaMemset2DAsync(slots, (size_t)stride * 8, 0xFF, (size_t)SEED_CAND * 8, N, s),
+                                 "memset"));
+        auto band = [&](auto rows) -> kcna_status {
+            KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(seed_band_kernel<decltype(rows)>,
+                                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                             (int)band_smem),
+                                     "seed band smem attr"));
+            for (int tab = 0; tab < SEED_TABLES; ++tab)
+                seed_band_kernel<<<kcna_div_up(N, 32 * BAND_WARPS), BAND_WARPS * 32, band_smem, s>>>(
+                    rows, N, order + (size_t)tab * N, tab, slots, stride, c->counters + 30);
+            return launch_ok(c, "seed band", SEED_TABLES);
+        };
+        if (c->bf16_exact)
+            KCNA_TRY(band(RowsB16{c->Xh, (int)ld}));
+        else
+            KCNA_TRY(band(RowsF32{c->X, (int)ld}));
+        seed_collect_kernel<<<kcna_div_up(N, 4), 128, 0, s>>>(slots, stride, N, c->cap, limit, c->pool, c->pool_cnt);
+    } else {
+        const size_t srow = (size_t)4 * ld * 4;
+        if (c->bf16_exact)
+            seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsB16{c->Xh, (int)ld}, N, order, rank, c->cap,
+                                                                   limit, c->pool, c->pool_cnt, c->counters + 30);
+        else
+            seed_pools_kernel<<<kcna_div_up(N, 4), 128, srow, s>>>(RowsF32{c->X, (int)ld}, N, order, rank, c->cap,
+                                                                   limit, c->pool, c->pool_cnt, c->counters + 30);
+    }
     KCNA_TRY(launch_ok(c, "seed pools"));
     unsigned long long h = 0;
     cudaMemcpyAsync(&h, c->counters + 30, 8, cudaMemcpyDeviceToHost, s);
