@@ -26,7 +26,7 @@
 namespace {
 
 constexpr int H1 = 256, H2 = 64;
-constexpr int SEED_TABLES = 16, SEED_BITS = 16, SEED_WIN = 16; // 16 tables x (2 x 16) = 512 candidates per node
+constexpr int SEED_TABLES = 16, SEED_BITS = 16, SEED_WIN = 32; // 16 tables x (2 x 32) = 1024 candidates per node
 constexpr int SEED_CAND = SEED_TABLES * 2 * SEED_WIN;
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
