@@ -101,20 +101,32 @@ __global__ void gelu_bwd_kernel(const float *__restrict__ Z, float *__restrict__
     if (t < n) dG[t] *= gelu_grad(Z[t]);
 }
 
-// column sums of an (rows x cols) matrix: one block per column group of 32, rows strided
-__global__ void colsum_kernel(const float *__restrict__ M, int64_t rows, int cols, float *__restrict__ out) {
+// column sums of an (rows x cols) matrix in two deterministic passes: block
+// (column group of 32, chunk of CS_ROWS rows) -> partial[chunk][col], then the
+// chunks summed in order
+constexpr int CS_ROWS = 256;
+__global__ void colsum_partial_kernel(const float *__restrict__ M, int64_t rows, int cols,
+                                      float *__restrict__ partial) {
     __shared__ float s[8][33];
     const int c = blockIdx.x * 32 + (threadIdx.x & 31), ry = threadIdx.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.y * CS_ROWS, r1 = min(rows, r0 + CS_ROWS);
     float acc = 0.f;
     if (c < cols)
-        for (int64_t r = ry; r < rows; r += 8) acc += M[r * cols + c];
+        for (int64_t r = r0 + ry; r < r1; r += 8) acc += M[r * cols + c];
     s[ry][threadIdx.x & 31] = acc;
     __syncthreads();
     if (ry == 0 && c < cols) {
         float t = 0.f;
         for (int i = 0; i < 8; ++i) t += s[i][threadIdx.x];
-        out[c] = t;
+        partial[(int64_t)blockIdx.y * cols + c] = t;
     }
+}
+__global__ void colsum_final_kernel(const float *__restrict__ partial, int nchunk, int cols, float *__restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float t = 0.f;
+    for (int k = 0; k < nchunk; ++k) t += partial[(int64_t)k * cols + c];
+    out[c] = t;
 }
 
 __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
@@ -265,42 +277,74 @@ __global__ void __launch_bounds__(128) seed_pools_kernel(R rows, uint32_t N, con
 // nodes' fixed candidate slots (node a's slot tab*2W + W + delta-1 holds the
 // delta-th node after it, slot tab*2W + delta-1 the delta-th node before it).
 // A warp stages the rows of its 32 positions and the SEED_WIN after them in
-// shared memory (row pitch ld + 4 floats: the 16-byte reads of 8 lanes fall in
-// distinct banks), so each row is read from memory about 1.5 times per table
-// instead of once per candidate.
+// shared memory as they are stored (BF16 or FP32; row pitch padded by 8 or 16
+// bytes so that the lanes' reads fall in distinct banks), so each row is read
+// from memory about twice per table instead of once per candidate; each lane
+// keeps SEED_WIN running sums and reads its own row once per 4 dimensions.
 constexpr int BAND_WARPS = 4, BAND_ROWS = 32 + SEED_WIN;
+
+template <class R> struct BandStage;
+template <> struct BandStage<RowsF32> {
+    static constexpr int ELT = 4;
+    __device__ static float4 get(const unsigned char *row, int k) {
+        return reinterpret_cast<const float4 *>(row)[k];
+    }
+    __device__ static void put(unsigned char *row, int k, const float *src) {
+        reinterpret_cast<float4 *>(row)[k] = __ldg(reinterpret_cast<const float4 *>(src) + k);
+    }
+};
+template <> struct BandStage<RowsB16> {
+    static constexpr int ELT = 2;
+    __device__ static float4 get(const unsigned char *row, int k) {
+        const uint2 u = reinterpret_cast<const uint2 *>(row)[k];
+        return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u), __uint_as_float(u.y << 16),
+                           __uint_as_float(u.y & 0xFFFF0000u));
+    }
+    __device__ static void put(unsigned char *row, int k, const uint16_t *src) {
+        reinterpret_cast<uint2 *>(row)[k] = __ldg(reinterpret_cast<const uint2 *>(src) + k);
+    }
+};
+__host__ __device__ constexpr int band_pitch(int ld, int elt) { return ld * elt + 4 * elt; } // bytes
 
 template <class R>
 __global__ void __launch_bounds__(BAND_WARPS * 32) seed_band_kernel(R rows, uint32_t N, const uint32_t *__restrict__ ord,
                                                                     int tab, uint64_t *__restrict__ slots,
                                                                     uint32_t stride, unsigned long long *comps) {
-    extern __shared__ __align__(16) float s_rows[]; // BAND_WARPS x BAND_ROWS x pitch
+    using B = BandStage<R>;
+    extern __shared__ __align__(16) unsigned char s_band[]; // BAND_WARPS x BAND_ROWS x pitch
     const int w = threadIdx.x >> 5, lane = kcna_lane();
-    const int nv = rows.ld >> 2, pitch4 = nv + 1;
-    float4 *sr = reinterpret_cast<float4 *>(s_rows) + (size_t)w * BAND_ROWS * pitch4;
+    const int nv = rows.ld >> 2, pitch = band_pitch(rows.ld, B::ELT);
+    unsigned char *sr = s_band + (size_t)w * BAND_ROWS * pitch;
     const uint64_t p0 = ((uint64_t)blockIdx.x * BAND_WARPS + w) * 32;
     if (p0 >= N) return;
     const int nr = (int)min((uint64_t)BAND_ROWS, N - p0);
     for (int e = lane; e < nr * nv; e += 32) {
         const int r = e / nv, k = e - r * nv;
-        sr[r * pitch4 + k] = rows.ld4(ord[p0 + r], k);
+        B::put(sr + (size_t)r * pitch, k, rows.p + (uint64_t)ord[p0 + r] * rows.ld);
     }
     __syncwarp();
     const uint64_t p = p0 + lane;
     unsigned long long cc = 0;
     if (p < N) {
+        const unsigned char *ra = sr + (size_t)lane * pitch;
+        float acc[SEED_WIN];
+#pragma unroll
+        for (int d = 0; d < SEED_WIN; ++d) acc[d] = 0.f;
+        for (int k = 0; k < nv; ++k) { // the canonical chain of every pair, dimension by dimension
+            const float4 x = B::get(ra, k);
+#pragma unroll
+            for (int d = 0; d < SEED_WIN; ++d)
+                if (lane + d + 1 < nr) acc[d] = kcna_acc4(acc[d], x, B::get(ra + (size_t)(d + 1) * pitch, k));
+        }
         const uint32_t a = ord[p];
-        const float4 *ra = sr + lane * pitch4;
-        for (int dlt = 1; dlt <= SEED_WIN; ++dlt) {
-            if (lane + dlt >= nr) break;
+        const uint32_t fl = (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
+#pragma unroll
+        for (int d = 0; d < SEED_WIN; ++d) {
+            if (lane + d + 1 >= nr) break;
             ++cc;
-            const uint32_t b = ord[p + dlt];
-            const float4 *rb = sr + (lane + dlt) * pitch4;
-            float acc = 0.f;
-            for (int k = 0; k < nv; ++k) acc = kcna_acc4(acc, ra[k], rb[k]);
-            const uint32_t fl = (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
-            slots[(uint64_t)a * stride + tab * 2 * SEED_WIN + SEED_WIN + dlt - 1] = kcna_key(acc, b, fl);
-            slots[(uint64_t)b * stride + tab * 2 * SEED_WIN + dlt - 1] = kcna_key(acc, a, fl);
+            const uint32_t b = ord[p + d + 1];
+            slots[(uint64_t)a * stride + tab * 2 * SEED_WIN + SEED_WIN + d] = kcna_key(acc[d], b, fl);
+            slots[(uint64_t)b * stride + tab * 2 * SEED_WIN + d] = kcna_key(acc[d], a, fl);
         }
     }
     cc = kcna_warp_sum(cc);
@@ -373,7 +417,14 @@ kcna_status launch_ok(kcna_ctx *c, const char *what, int n = 1) {
 // row pitch ld): loss, gradients.  Work buffers in `ws` (see below).
 struct EncoderWork {
     float *Z1, *G, *H2, *Y, *nrm, *dY, *dG, *loss;
+    float *part; // column-sum partials: ceil(rows / CS_ROWS) x H1
 };
+inline size_t colsum_parts(int64_t rows) { return (size_t)((rows + CS_ROWS - 1) / CS_ROWS) * H1; }
+static void colsum(cudaStream_t s, const float *M, int64_t rows, int cols, float *part, float *out) {
+    const int nchunk = (int)((rows + CS_ROWS - 1) / CS_ROWS);
+    colsum_partial_kernel<<<dim3(kcna_div_up(cols, 32), nchunk), 256, 0, s>>>(M, rows, cols, part);
+    colsum_final_kernel<<<kcna_div_up(cols, 256), 256, 0, s>>>(part, nchunk, cols, out);
+}
 
 static kcna_status encoder_fwd_bwd(kcna_ctx *c, const float *Xb, int ld, int B, const float *W1, const float *b1,
                                    const float *W2, const float *b2, float margin, EncoderWork &w, float *dW1,
@@ -390,13 +441,13 @@ static kcna_status encoder_fwd_bwd(kcna_ctx *c, const float *Xb, int ld, int B, 
     triplet_kernel<<<kcna_div_up((int64_t)B * 32, 256), 256, 0, s>>>(w.Y, B, margin, w.dY, w.loss);
     norm_bwd_kernel<<<kcna_div_up(R * 32, 256), 256, 0, s>>>(w.Y, w.nrm, w.dY, R);
     KCNA_TRY(launch_ok(c, "triplet", 2));
-    colsum_kernel<<<kcna_div_up(H2, 32), 256, 0, s>>>(w.dY, R, H2, db2);
+    colsum(s, w.dY, R, H2, w.part, db2);
     // dW2 = dZ2^T G ; dG = dZ2 W2
     KCNA_TRY(kcna_tc_gemm(s, w.dY, H2, 1, 1, w.G, H1, 1, 1, dW2, H1, H2, H1, (int)R, 0.f, c->d_err));
     KCNA_TRY(kcna_tc_gemm(s, w.dY, H2, 1, 0, W2, H1, 1, 1, w.dG, H1, (int)R, H1, H2, 0.f, c->d_err));
     gelu_bwd_kernel<<<kcna_div_up(R * H1, 256), 256, 0, s>>>(w.Z1, w.dG, R * H1);
-    colsum_kernel<<<kcna_div_up(H1, 32), 256, 0, s>>>(w.dG, R, H1, db1);
-    KCNA_TRY(launch_ok(c, "gelu_bwd", 4));
+    colsum(s, w.dG, R, H1, w.part, db1);
+    KCNA_TRY(launch_ok(c, "gelu_bwd", 6));
     // dW1 = dZ1^T Xb
     KCNA_TRY(kcna_tc_gemm(s, w.dG, H1, 1, 1, Xb, ld, 1, 1, dW1, ld, H1, ld, (int)R, 0.f, c->d_err));
     c->launches += 1;
@@ -510,6 +561,7 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     KCNA_TRY(dev.get(&w.dY, (size_t)R * H2, "dY"));
     KCNA_TRY(dev.get(&w.dG, (size_t)R * H1, "dG"));
     KCNA_TRY(dev.get(&w.loss, 1, "loss"));
+    KCNA_TRY(dev.get(&w.part, colsum_parts(R), "column sums"));
     float first_loss = -1.f, last_loss = 0.f;
     for (int it = 0; it < steps; ++it) {
         make_triplets_kernel<<<kcna_div_up(B, 256), 256, 0, s>>>(sc->pool, sc->pool_cnt, sc->cap, ns, kp, B,
@@ -578,7 +630,7 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     // --- 4. initial pools
     const uint32_t limit = std::min(p->L, c->cap);
     cudaMemsetAsync(c->counters + 30, 0, 8, s);
-    const size_t band_smem = (size_t)BAND_WARPS * BAND_ROWS * (ld + 4) * 4;
+    const size_t band_smem = (size_t)BAND_WARPS * BAND_ROWS * band_pitch((int)ld, c->bf16_exact ? 2 : 4);
     if (band_smem <= 200 * 1024) { // banded: each pair once, rows read in table order
         uint64_t *slots = c->cand;
         uint32_t stride = c->CB;
@@ -663,6 +715,7 @@ extern "C" kcna_status kcna_encoder_grads(kcna_ctx *c, const float *rows, uint32
     KCNA_TRY(dev.get(&w.dY, (size_t)R * H2, "dY"));
     KCNA_TRY(dev.get(&w.dG, (size_t)R * H1, "dG"));
     KCNA_TRY(dev.get(&w.loss, 1, "loss"));
+    KCNA_TRY(dev.get(&w.part, colsum_parts(R), "column sums"));
     cudaMemsetAsync(Xb, 0, (size_t)R * ld * 4, s);
     cudaMemsetAsync(pW1, 0, (size_t)H1 * ld * 4, s);
     cudaMemcpy2DAsync(Xb, (size_t)ld * 4, rows, (size_t)d * 4, (size_t)d * 4, R, cudaMemcpyHostToDevice, s);
