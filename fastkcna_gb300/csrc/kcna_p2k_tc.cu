@@ -23,11 +23,11 @@
 //               pusher / neighbour ids into the tile stage with cp.async, then
 //               radius, norm and isnew flags; a tile with no rows ends the
 //               stream.
-//   warps 10-13 row loaders: the pushers' and neighbours' BF16 rows by 16-byte
+//   warps 18-21 row loaders: the pushers' and neighbours' BF16 rows by 16-byte
 //               cp.async in the 128-byte swizzled K-major layout.
 //   warp 1      MMA issuer: M = 128, N = columns used rounded up to 16.
-//   warps 2-9   epilogue: warp w reads TMEM lanes 32*(w%4).. (pushers) and
-//               every second 16-column group of the span its lanes' nodes
+//   warps 2-17  epilogue: warp w reads TMEM lanes 32*(w%4).. (pushers) and
+//               every fourth 16-column group of the span its lanes' nodes
 //               cover; per thread a count pass, one atomicAdd on the pusher's
 //               candidate count, and a write pass reading TMEM again.
 #include <algorithm>
@@ -39,7 +39,8 @@ using namespace kcna_tc;
 
 namespace {
 
-constexpr int LOAD_WARP = 10; // first row-loader warp
+constexpr int EPI = 16;       // epilogue warps: 4 lane quarters x 4 column phases
+constexpr int LOAD_WARP = 2 + EPI; // first row-loader warp
 constexpr int NLOAD = 4;      // row-loader warps
 constexpr int PW_WARPS = LOAD_WARP + NLOAD;
 constexpr int PW_THREADS = PW_WARPS * 32;
@@ -102,11 +103,11 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             mbar_init(&S.ids_ready[i], 1);          // producer lane 0 once the ids have landed
             mbar_init(&S.meta_full[i], 64);         // producer lanes: stores done, radius / norm copies landed
             mbar_init(&S.tile_full[i], NLOAD * 32); // every loader lane, after its copies and a proxy fence
-            mbar_init(&S.tile_empty[i], 9); // MMA commit + epilogue warps
+            mbar_init(&S.tile_empty[i], 1 + EPI); // MMA commit + epilogue warps
         }
         for (int i = 0; i < NACC; ++i) {
             mbar_init(&S.acc_full[i], 1);
-            mbar_init(&S.acc_empty[i], 8);
+            mbar_init(&S.acc_empty[i], EPI);
         }
         S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -297,7 +298,7 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             }
             const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * PN);
             uint32_t cnt = 0;
-            for (int g = gl + h; g <= gh; g += 2) { // count pass
+            for (int g = gl + h; g <= gh; g += 4) { // count pass
                 uint32_t raw[16];
                 tmem_ld16_async(trow + 16 * g, raw);
                 tmem_wait_ld16(raw);
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             uint32_t p = cnt ? atomicAdd(a.cand_cnt + u, cnt) : 0u;
             if (__any_sync(KCNA_FULL, cnt != 0u)) { // write pass
                 uint64_t *dst = a.cand + (uint64_t)u * a.CB;
-                for (int g = gl + h; g <= gh; g += 2) {
+                for (int g = gl + h; g <= gh; g += 4) {
                     uint32_t raw[16];
                     tmem_ld16_async(trow + 16 * g, raw);
                     tmem_wait_ld16(raw);
