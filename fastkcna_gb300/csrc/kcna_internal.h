@@ -58,6 +58,7 @@ struct kcna_ctx {
     uint64_t *cand = nullptr;
     uint32_t *cand_cnt = nullptr;
     uint32_t *big_list = nullptr, *big_cnt = nullptr; // merge queue of nodes with many candidates
+    uint32_t merge_big_last = 0;                      // nodes the previous merge queued
     unsigned long long *counters = nullptr; // device scratch counters (64 slots)
 
     // graph: n x W ids / dists / isnew flags, degrees; previous-loop ids

@@ -325,21 +325,28 @@ struct MergeArgs {
 // pool entry, or one that would land at rank >= limit, is dropped.  In a
 // converging NN-descent almost every candidate is such a repeat, so only the
 // few survivors are sorted, deduplicated and merged, and only the pool entries
-// they displace are written.  A node with more than MW_SURV survivors is
+// they displace are written.  A node with more than SURV survivors is
 // queued for the block merge (merge_kernel).  Same result as merging all
 // candidates.  Persistent: each warp takes nodes grid-stride, so a block
 // meets its barrier once at the end instead of waiting for its slowest node.
-constexpr int MW_WARPS = 8, MW_SURV = 512;
+// SURV is 512, or 1024 while the previous merge queued many nodes (the first
+// iterations, when the pools are filling): twice the shared memory per warp
+// and fewer warps per SM, but fewer nodes left to the block merge.
+constexpr int MW_WARPS = 8;
+__host__ __device__ constexpr size_t merge_warp_bytes(uint32_t cap, int surv) {
+    return ((size_t)cap * 8 + (size_t)surv * 8 + 16 + 15) & ~(size_t)15;
+}
 
+template <int SURV>
 __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, uint32_t N, uint32_t *big_list,
                                                                   uint32_t *big_cnt) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
-    const size_t per_warp = ((size_t)a.cap * 8 + (size_t)MW_SURV * 8 + 16 + 15) & ~(size_t)15;
+    const size_t per_warp = merge_warp_bytes(a.cap, SURV);
     unsigned char *base = smem + w * per_warp;
     uint64_t *s_pool = reinterpret_cast<uint64_t *>(base);
     uint64_t *s_sv = s_pool + a.cap;         // survivors (keys without flags)
-    uint64_t *s_last = s_sv + MW_SURV;       // key landing at rank limit-1
+    uint64_t *s_last = s_sv + SURV;          // key landing at rank limit-1
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
     if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
     __syncthreads();
@@ -382,11 +389,11 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 }
                 const unsigned m = __ballot_sync(KCNA_FULL, surv);
                 const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
-                if (surv && pos < (uint32_t)MW_SURV) s_sv[pos] = k;
+                if (surv && pos < (uint32_t)SURV) s_sv[pos] = k;
                 ns += __popc(m);
             }
         }
-        if (ns > (uint32_t)MW_SURV) {
+        if (ns > (uint32_t)SURV) {
             if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = node;
         } else {
             uint32_t nu = 0; // distinct survivors
@@ -1011,27 +1018,38 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "merge smem attr"));
-    const size_t smw = (((size_t)c->cap * 8 + (size_t)MW_SURV * 8 + 16 + 15) & ~(size_t)15) * MW_WARPS;
-    KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)std::max<size_t>(smw, 48 * 1024)),
-                             "merge smem attr"));
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
-    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->big_cnt, 0, 4, c->stream), "memset"));
-    KCNA_TRY(kcna_phase_begin(c));
-    int mw_per_sm = 0;
-    KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mw_per_sm, merge_warp_kernel,
-                                                                             MW_WARPS * 32, smw),
-                             "merge occupancy"));
-    const uint32_t mw_grid = (uint32_t)std::min<uint64_t>(kcna_div_up(c->n, MW_WARPS),
-                                                          (uint64_t)std::max(c->num_sms, 1) * std::max(mw_per_sm, 1));
-    merge_warp_kernel<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
+    const bool wide = c->merge_big_last > c->n / 64; // many nodes overflowed the survivor buffer last time
+    const int surv = wide ? 1024 : 512;
+    const size_t smw = merge_warp_bytes(c->cap, surv) * MW_WARPS;
+    auto launch_warp = [&](auto kern) -> kcna_status {
+        KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)std::max<size_t>(smw, 48 * 1024)),
+                                 "merge smem attr"));
+        int mw_per_sm = 0;
+        KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mw_per_sm, kern, MW_WARPS * 32, smw),
+                                 "merge occupancy"));
+        const uint32_t mw_grid = (uint32_t)std::min<uint64_t>(
+            kcna_div_up(c->n, MW_WARPS), (uint64_t)std::max(c->num_sms, 1) * std::max(mw_per_sm, 1));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->big_cnt, 0, 4, c->stream), "memset"));
+        KCNA_TRY(kcna_phase_begin(c));
+        kern<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
+        return KCNA_OK;
+    };
+    if (wide)
+        KCNA_TRY(launch_warp(merge_warp_kernel<1024>));
+    else
+        KCNA_TRY(launch_warp(merge_warp_kernel<512>));
     merge_kernel<<<std::max(1, c->num_sms) * 4, MT, sm, c->stream>>>(a, c->big_list, c->big_cnt);
     c->launches += 2;
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_MERGE));
     unsigned long long h[10] = {};
+    uint32_t hb = 0;
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(h, c->counters, 10 * 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb, c->big_cnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "merge sync"));
+    c->merge_big_last = hb;
     c->cand_merged += h[7];
     c->pool_entries_merged += h[9];
     if (merged) *merged = h[7];
@@ -1151,6 +1169,7 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
     const uint32_t maxl = std::max(std::max(P.L, P.K), std::max(P.search_L, P.search_K));
     if (maxl > 1024) return kcna_fail(c, KCNA_E_ARG, "max(L, K, search_L, search_K) must be <= 1024");
     st->maxl = maxl;
+    c->merge_big_last = c->n; // the first merges fill the pools: wide survivor buffers
     KCNA_TRY(kcna_nnd_alloc(c, &P, maxl));
     KCNA_TRY(kcna_controls_setup(c, &P, maxl));
     // join iterations count from 1 when the first lists come from an update step
