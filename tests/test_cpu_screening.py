@@ -77,3 +77,36 @@ def test_fp8_e4m3_screening_error_c4(capsys):
         infl = ((np.sqrt(nn) + 2 * np.median(E)) ** 2 / nn).mean()
         print(f"C4 FP8 bound inflates a 50-NN radius by {100 * (infl - 1):.0f} % on average")
     assert np.median(rel) < 0.1
+
+
+def _gram_d2(A, B):
+    return np.maximum((A * A).sum(1)[:, None] + (B * B).sum(1)[None, :] - 2.0 * A @ B.T, 0.0)
+
+
+def test_screen_pass_ratio_c4(capsys):
+    """How many pairs each screen lets through at a converged pool radius on
+    C4: the radius is each row's 4th-NN distance among 8,000 rows (the scale
+    of a 500-NN radius among 1M rows); a pair passes the exact test when
+    d <= r, a screen when the encoded distance is within its bound.  The
+    distances of C4 concentrate (a random pair sits ~9 % beyond the 500-NN
+    radius), so the FP8 bound, ~14 % wider, passes several times the exact
+    pairs and every one of them would need an FP32 recompute."""
+    X = synth.base("c4", 8000).astype(np.float64)
+    Xq, _ = _fp8_rows(X)
+    Xb = _bf16(X)
+    E8 = np.sqrt(((Xq - X) ** 2).sum(1))
+    Eb = np.sqrt(((Xb - X) ** 2).sum(1))
+    nq = (Xq * Xq).sum(1)
+    i = np.arange(200)
+    d = _gram_d2(X[i], X)
+    r = np.sort(d, axis=1)[:, 4][:, None]
+    exact = int((d <= r).sum())
+    b8 = (np.sqrt(r) + E8[i, None] + E8[None, :]) ** 2 + 2.0**-8 * (nq[i, None] + nq[None, :])
+    p8 = int((_gram_d2(Xq[i], Xq) <= b8).sum())
+    bb = (np.sqrt(r) + Eb[i, None] + Eb[None, :]) ** 2
+    pb = int((_gram_d2(Xb[i], Xb) <= bb).sum())
+    with capsys.disabled():
+        print(f"\nC4 pairs passing at a 500-NN-scale radius: exact {exact}, FP8 E4M3 screen {p8} "
+              f"({p8 / exact:.1f}x), BF16 screen {pb} ({pb / exact:.2f}x)")
+    assert p8 >= pb >= exact  # every screen is a superset of the exact test
+    assert p8 > 2 * exact and pb < 1.6 * exact
