@@ -80,8 +80,9 @@ TOOLS = {"fastnsg": 1, "fasttaumng": 2, "fastalphapg": 3, "fasthnsw": 4, "fastns
 
 
 def build_host(verbose: bool = False) -> None:
-    """The C++ kgraph::KGraph facade (libkgraph_gb300.so) and the five command
-    lines (bin/fast*), linked against libkcna.so."""
+    """The C++ kgraph::KGraph facade (libkgraph_gb300.so), the five command
+    lines (bin/fast*, linked against libkcna.so) and the fvecs converter
+    (bin/fvec2lshkit, host code only)."""
     cxx = os.environ.get("CXX", "g++")
     inc = ["-I", os.path.join(ROOT, "include")]
     common = [cxx, "-O2", "-std=c++17", "-Wall", "-Wno-unused-result", *inc]
@@ -102,6 +103,10 @@ def build_host(verbose: bool = False) -> None:
             raise RuntimeError("g++ failed on kgraph_facade.cpp")
     os.makedirs(BIN, exist_ok=True)
     jobs = []
+    conv_src = os.path.join(HOST, "fvec2lshkit.cpp")
+    conv = os.path.join(BIN, "fvec2lshkit")
+    if stale(conv, [conv_src]):
+        jobs.append(("fvec2lshkit", common + [conv_src, "-o", conv]))
     for tool, k in TOOLS.items():
         out = os.path.join(BIN, tool)
         if stale(out, [cli_src, FACADE, *headers]):
