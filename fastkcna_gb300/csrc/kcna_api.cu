@@ -657,7 +657,10 @@ kcna_status kcna_prune(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
     uint64_t comps = 0;
     uint32_t used = 0;
     KCNA_TRY(prepare_rows(c, p, &used));
-    KCNA_TRY(kcna_prune_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
+    if (kind == KCNA_CAGRA)
+        KCNA_TRY(kcna_cagra_prune(c, p));
+    else
+        KCNA_TRY(kcna_prune_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
     return kcna_check_device_err(c, "prune");
 }
 
@@ -666,6 +669,7 @@ kcna_status kcna_link(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
     KCNA_TRY(bind(c));
     uint64_t comps = 0;
     uint32_t used = 0;
+    if (kind == KCNA_CAGRA) return kcna_fail(c, KCNA_E_ARG, "link: the CAGRA rank prune has no link step");
     KCNA_TRY(prepare_rows(c, p, &used));
     KCNA_TRY(kcna_link_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
     return kcna_check_device_err(c, "link");

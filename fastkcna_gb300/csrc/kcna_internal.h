@@ -164,6 +164,8 @@ kcna_status kcna_seed_finish(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_exclusive_scan_u32(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t *out, uint64_t *total_h);
 kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W);
 kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
+// CAGRA-style rank prune of the pools into the graph (kcna_cagra.cu).
+kcna_status kcna_cagra_prune(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
 kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed);
 kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed);

@@ -16,8 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libkcna.so")
 
-NSG, HNSW_LAYER, TAUMNG, ALPHAPG = 1, 2, 3, 4
-KINDS = {"nsg": NSG, "hnsw": HNSW_LAYER, "taumng": TAUMNG, "alphapg": ALPHAPG}
+NSG, HNSW_LAYER, TAUMNG, ALPHAPG, CAGRA = 1, 2, 3, 4, 5
+KINDS = {"nsg": NSG, "hnsw": HNSW_LAYER, "taumng": TAUMNG, "alphapg": ALPHAPG, "cagra": CAGRA}
 SCREEN_FP32, SCREEN_BF16 = 0, 1
 MAX_ITERS, MAX_LOOPS, NUM_PHASES = 64, 16, 12
 PHASES = ["join", "merge", "sample", "prune", "link", "p2k", "ep", "tree", "controls", "init", "other", "spare"]

@@ -39,7 +39,8 @@ typedef enum {
     KCNA_NSG = 1,
     KCNA_HNSW_LAYER = 2, /* NSG-style layer without tree_grow (buildHNSWLayer, :2326-2337) */
     KCNA_TAUMNG = 3,
-    KCNA_ALPHAPG = 4
+    KCNA_ALPHAPG = 4,
+    KCNA_CAGRA = 5 /* kcna_prune only: CAGRA-style rank prune (BuildCagra, :2818-2829) */
 } kcna_kind;
 
 /* Distance screening forms for the local join and the P2K join. */
@@ -208,7 +209,10 @@ kcna_status kcna_set_pools(kcna_ctx *ctx, const kcna_params *params, const uint3
 
 /* Occlusion prune of every pool into the graph (kind NSG/HNSW_LAYER: RNG,
  * TAUMNG: tau, ALPHAPG: angle).  Replaces nsg_sync_prune (src/kgraph.cpp:1809-1851),
- * taumg_sync_prune (:2833-2876) and alphapg_sync_prune (:3157-3203). */
+ * taumg_sync_prune (:2833-2876) and alphapg_sync_prune (:3157-3203).
+ * Kind CAGRA: the rank prune of BuildCagra (src/kgraph.cpp:2665-2829) over the
+ * first K pool entries, about K / 2 edges per node (width >= K / 2 + 1);
+ * 2 <= K <= min(pool capacity, 1024). */
 kcna_status kcna_prune(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind);
 /* Prune + reverse-edge insert + re-prune of over-full nodes.  Replaces
  * nsg_Link / taumg_Link / alphapg_Link (src/kgraph.cpp:2087-2143, 3085-3141, 3424-3480). */

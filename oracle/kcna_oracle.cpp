@@ -1,7 +1,8 @@
 // kcna_oracle.cpp - TEST INFRASTRUCTURE, not product code.
 //
 // CPU restatement of FastKCNA's graph-construction path (NN-descent, occlusion
-// prune + link, entry point, tree_grow, UpdateNhoods, P2K "BridgeView") written
+// prune + link, entry point, tree_grow, UpdateNhoods, P2K "BridgeView", the
+// CAGRA-style rank prune) written
 // from the reference's behaviour, function by function, each citing the
 // reference file:line it follows (paths relative to the reference project).
 // It is the checker for the CUDA library: the tests, the smoke check and the
@@ -831,6 +832,68 @@ struct Builder {
             if (nh[i].nn_nsg.size() > width) width = (unsigned)nh[i].nn_nsg.size();
     }
 
+    // CAGRA-style rank prune, src/kgraph.cpp:2818-2829 (BuildCagra; none of the
+    // reference's build functions calls it).  With Ki = min(K, pool count):
+    //  * route[j] counts the detours i -> pool[k] -> pool[j]: k < j, and
+    //    pool[j] at rank l < j in pool[k]'s own list (CagraComputeRoute
+    //    :2665-2757, the live loop :2707-2725);
+    //  * the prune_K = K / 2 entries with the fewest detours are kept, equal
+    //    counts in rank order (sort_indexes :62-76);
+    //  * every kept edge i -> w gives w a reverse entry (i, its rank in i's kept
+    //    list), taken by increasing rank, equal ranks by increasing source id
+    //    (CagraReverse :2759-2788 sorts by rank only, so the order of equal
+    //    ranks is unspecified there);
+    //  * the graph alternates kept and reverse entries until prune_K are
+    //    placed, one more when the last step places both (CagraMerge
+    //    :2790-2816); reverse entries carry d(i, source).
+    // Entries past a pool's count are absent (the reference reads them as is).
+    void build_cagra() {
+        const unsigned n = D.n, K = P.K, PK = K / 2;
+        std::vector<std::vector<unsigned>> keep(n);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < (int)n; ++i) {
+            const auto &pool = nh[i].pool;
+            const unsigned Ki = std::min(K, nh[i].L);
+            std::vector<unsigned> route(Ki, 0);
+            for (unsigned k = 0; k < Ki; ++k) {
+                const unsigned one = pool[k].id;
+                const unsigned Kl = std::min(K, nh[one].L);
+                for (unsigned l = 0; l < Kl; ++l) {
+                    const unsigned two = nh[one].pool[l].id;
+                    for (unsigned j = std::max(k, l) + 1; j < Ki; ++j)
+                        if (two == pool[j].id) {
+                            ++route[j];
+                            break;
+                        }
+                }
+            }
+            std::vector<unsigned> idx(Ki);
+            for (unsigned j = 0; j < Ki; ++j) idx[j] = j;
+            std::stable_sort(idx.begin(), idx.end(), [&](unsigned a, unsigned b) { return route[a] < route[b]; });
+            idx.resize(std::min(PK, Ki));
+            keep[i] = idx;
+        }
+        std::vector<std::vector<std::pair<unsigned, unsigned>>> rev(n); // (rank, source)
+        for (unsigned i = 0; i < n; ++i)
+            for (unsigned r = 0; r < keep[i].size(); ++r) rev[nh[i].pool[keep[i][r]].id].push_back({r, i});
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int w = 0; w < (int)n; ++w) std::sort(rev[w].begin(), rev[w].end());
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < (int)n; ++i) {
+            auto &h = nh[i];
+            h.nn_nsg.clear();
+            size_t k = 0, j = 0;
+            while (h.nn_nsg.size() < PK && (k < keep[i].size() || j < rev[i].size())) {
+                if (k < keep[i].size()) h.nn_nsg.push_back(h.pool[keep[i][k++]]);
+                if (j < rev[i].size()) {
+                    const unsigned s = rev[i][j++].second;
+                    h.nn_nsg.push_back(Nb(s, D(i, s), true));
+                }
+            }
+        }
+        update_nhoods();
+    }
+
     // src/kgraph.cpp:3537-3584 (UpdateNhoods)
     void update_nhoods() {
 #pragma omp parallel for schedule(dynamic, 100)
@@ -1127,7 +1190,8 @@ static void store_graph(Builder &B, uint32_t *out_ids, float *out_d, uint32_t *o
     }
 }
 
-// Prune every pool (sync_prune of the given kind) into out (n x width).
+// Prune every pool (sync_prune of the given kind, or the CAGRA rank prune) into
+// out (n x width).
 int kcnao_prune(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p,
                 const uint32_t *pid, const float *pd, const uint32_t *pcnt, uint32_t cap, uint32_t *out_ids,
                 float *out_d, uint32_t *out_deg, uint32_t width, int nthreads) {
@@ -1137,8 +1201,12 @@ int kcnao_prune(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t 
     Builder B(Data{X, stride, n, d}, *p, kind, &st);
     B.MAXL = std::max(cap, std::max(std::max(p->L, p->K), std::max(p->search_L, p->search_K)));
     load_pools(B, pid, pd, pcnt, cap);
+    if (kind == KCNA_CAGRA) {
+        B.build_cagra();
+    } else {
 #pragma omp parallel for schedule(dynamic, 64)
-    for (int q = 0; q < (int)n; ++q) B.sync_prune(q);
+        for (int q = 0; q < (int)n; ++q) B.sync_prune(q);
+    }
     store_graph(B, out_ids, out_d, out_deg, width);
     return 0;
 }

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libkcna_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libkcna_ref.so")
 
-KCNA_NSG, KCNA_HNSW_LAYER, KCNA_TAUMNG, KCNA_ALPHAPG = 1, 2, 3, 4
+KCNA_NSG, KCNA_HNSW_LAYER, KCNA_TAUMNG, KCNA_ALPHAPG, KCNA_CAGRA = 1, 2, 3, 4, 5
 MAX_ITERS, MAX_LOOPS = 64, 16
 
 

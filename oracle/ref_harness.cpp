@@ -180,7 +180,23 @@ int kref_prune(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d
     fill(M, X, stride, n, d);
     RefOracle O(M);
     KGraphConstructor *con = empty_constructor(O, p, pid, pd, pcnt, cap);
-    for (unsigned q = 0; q < n; ++q) {
+    if (kind == KCNA_CAGRA) {
+        // BuildCagra (src/kgraph.cpp:2818-2829) step by step, with one addition:
+        // CagraReverse sorts each reverse list by rank only (std::sort), which
+        // leaves the order of equal ranks unspecified; they are put in
+        // increasing source id before CagraMerge, the order the oracle states.
+        std::vector<std::vector<unsigned>> indexes(n);
+        std::vector<std::vector<RankNeighbor>> regra(n);
+        con->CagraComputeRoute(indexes, con->params.K / 2);
+        con->CagraReverse(indexes, regra);
+        for (auto &r : regra)
+            std::stable_sort(r.begin(), r.end(), [](const RankNeighbor &a, const RankNeighbor &b) {
+                return a.rank != b.rank ? a.rank < b.rank : a.id < b.id;
+            });
+        con->CagraMerge(indexes, regra);
+        con->UpdateNhoods();
+    }
+    for (unsigned q = 0; q < n && kind != KCNA_CAGRA; ++q) {
         if (kind == KCNA_TAUMNG)
             con->taumg_sync_prune(q);
         else if (kind == KCNA_ALPHAPG)

@@ -10,7 +10,10 @@ stores its outputs:
   * Link (prune + InterInsert + reversed prune) of the three kinds, one thread
     (src/kgraph.cpp:2087-2143, 3085-3141, 3424-3480);
   * beam search (get_neighbors, src/kgraph.cpp:1560-1623) of 20 queries over
-    the NSG link graph from fixed seed ids.
+    the NSG link graph from fixed seed ids;
+  * into ref_cagra_*.npz, the CAGRA-style rank prune (BuildCagra,
+    src/kgraph.cpp:2665-2829) of the stored pools with K = 48 and K = 46, the
+    order of equal-rank reverse entries fixed as oracle/ref_harness.cpp states.
 The datasets are stored with the outputs (C2-like rows as uint8).
 
 Usage: python tests/golden/make_golden.py   (needs oracle/_ref built here)
@@ -57,9 +60,24 @@ def make(name, X, tau):
     np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
 
 
+def make_cagra(name):
+    """CAGRA rank prune of the pools already stored in ref_<name>.npz."""
+    ref = oracle_py.Reference()
+    z = dict(np.load(os.path.join(HERE, f"ref_{name}.npz")))
+    X = z["X"].astype(np.float32)
+    out = {}
+    for k in (48, 46):
+        p = oracle_py.params(**dict(PARAMS, K=k), tau=float(z["tau"]))
+        gi, gd, deg = ref.prune(oracle_py.KCNA_CAGRA, X, p, z["pool_ids"], z["pool_d"], z["pool_cnt"], k // 2 + 1)
+        out[f"k{k}_ids"], out[f"k{k}_d"], out[f"k{k}_deg"] = gi, gd, deg
+    np.savez_compressed(os.path.join(HERE, f"ref_cagra_{name}.npz"), **out)
+
+
 if __name__ == "__main__":
     if not oracle_py.Reference.available():
         sys.exit("oracle/_ref/libkcna_ref.so is missing: run oracle/build_ref.sh")
     make("c1", synth.base("c1", N), 0.05)
     make("c2", synth.base("c2", N), 10.0)
+    make_cagra("c1")
+    make_cagra("c2")
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

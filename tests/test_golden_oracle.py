@@ -70,3 +70,20 @@ def test_pools_are_valid_knn_pools():
             row = z["pool_ids"][i, :c]
             assert len(set(row.tolist())) == c and i not in row
             assert np.all(np.diff(z["pool_d"][i, :c]) >= 0)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("k", [48, 46])
+def test_cagra_prune(oracle, name, k):
+    """CAGRA rank prune (BuildCagra) of the reference's pools, K = 48 (even
+    prune_K) and K = 46 (odd prune_K: rows of prune_K + 1)."""
+    z = load(name)
+    c = dict(np.load(os.path.join(HERE, f"ref_cagra_{name}.npz")))
+    p = oracle_py.params(**dict(P, K=k), tau=float(z["tau"]))
+    gi, gd, deg = oracle.prune(oracle_py.KCNA_CAGRA, z["X"], p, z["pool_ids"], z["pool_d"], z["pool_cnt"], k // 2 + 1)
+    assert np.array_equal(deg, c[f"k{k}_deg"])
+    assert np.array_equal(gi, c[f"k{k}_ids"])
+    if name == "c2":
+        assert np.array_equal(gd, c[f"k{k}_d"])
+    else:
+        np.testing.assert_allclose(gd, c[f"k{k}_d"], rtol=2e-6)
