@@ -556,7 +556,10 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
         if (iter == iters) break;
         double s0 = kcna_now();
         uint64_t bc = 0;
-        KCNA_TRY(kcna_bridge_view(c, &P, maxl, loopcount, &bc));
+        if (P.refine == KCNA_REFINE_POOL_SEARCH)
+            KCNA_TRY(kcna_pool_search_run(c, &P, maxl, loopcount, &bc));
+        else
+            KCNA_TRY(kcna_bridge_view(c, &P, maxl, loopcount, &bc));
         bridge_comps += bc;
         KCNA_TRY(kcna_control_recall(c, maxl, &r));
         if (loopcount - 1 < KCNA_MAX_LOOPS) st->search_time[loopcount - 1] = kcna_now() - s0;
@@ -673,6 +676,15 @@ kcna_status kcna_link(kcna_ctx *c, const kcna_params *p, kcna_kind kind) {
     KCNA_TRY(prepare_rows(c, p, &used));
     KCNA_TRY(kcna_link_all(c, p, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, &comps));
     return kcna_check_device_err(c, "link");
+}
+
+kcna_status kcna_pool_search(kcna_ctx *c, const kcna_params *p, uint32_t loopcount, uint64_t *comps) {
+    if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "pool search: null argument");
+    KCNA_TRY(bind(c));
+    uint64_t cc = 0;
+    KCNA_TRY(kcna_pool_search_run(c, p, c->cap, (int)loopcount, &cc));
+    if (comps) *comps = cc;
+    return kcna_check_device_err(c, "pool search");
 }
 
 kcna_status kcna_set_graph(kcna_ctx *c, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep) {

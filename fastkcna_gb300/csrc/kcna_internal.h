@@ -171,5 +171,7 @@ kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed);
 kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed);
 kcna_status kcna_update_nhoods(kcna_ctx *c, int loopcount);
 kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, int loopcount, uint64_t *comps);
+// Per-node pool search over the graph (inSearch; kcna_pool_search.cu).
+kcna_status kcna_pool_search_run(kcna_ctx *c, const kcna_params *p, uint32_t maxl, int loopcount, uint64_t *comps);
 kcna_status kcna_search_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint32_t *d_init, uint32_t L,
                                uint32_t k, uint32_t *d_out_ids, float *d_out_d);

@@ -44,7 +44,7 @@ class Params(C.Structure):
         ("delta", C.c_float), ("recall", C.c_float)] + [
         (n, C.c_uint32) for n in ("nsg_R", "search_L", "search_K", "step", "massq_S", "loop_i")] + [
         ("tau", C.c_float), ("angle", C.c_float), ("screen", C.c_uint32), ("learned_seed", C.c_uint32),
-        ("verbosity", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+        ("verbosity", C.c_uint32), ("refine", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class Stats(C.Structure):
@@ -273,6 +273,14 @@ class Index:
         cnt = np.empty(self.n, np.uint32)
         self._check(self.lib.kcna_get_pools(self.h, _ptr(ids), _ptr(d), _ptr(cnt), c))
         return ids, d, cnt
+
+    def pool_search(self, loopcount: int, p: Params | None = None, **kw) -> int:
+        """Per-node pool search of loop `loopcount` (inSearch) over the current
+        graph; returns the distance evaluations."""
+        p = p or params(**kw)
+        cc = C.c_uint64(0)
+        self._check(self.lib.kcna_pool_search(self.h, C.byref(p), C.c_uint32(loopcount), C.byref(cc)))
+        return int(cc.value)
 
     def set_pools(self, ids, dists, counts, p: Params | None = None, **kw):
         p = p or params(**kw)

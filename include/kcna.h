@@ -43,6 +43,12 @@ typedef enum {
     KCNA_CAGRA = 5 /* kcna_prune only: CAGRA-style rank prune (BuildCagra, :2818-2829) */
 } kcna_kind;
 
+/* Refinement of the pools between prune loops (kcna_params.refine). */
+typedef enum {
+    KCNA_REFINE_BRIDGE_VIEW = 0, /* P2K BridgeView (src/kgraph.cpp:2478-2663), the reference's builds */
+    KCNA_REFINE_POOL_SEARCH = 1  /* per-node pool search, inSearch (:2340-2414, :3667-3688) */
+} kcna_refine;
+
 /* Distance screening forms for the local join and the P2K join. */
 typedef enum {
     KCNA_SCREEN_FP32 = 0, /* plain FP32, the drop-in */
@@ -74,7 +80,8 @@ typedef struct {
     uint32_t screen;     /* kcna_screen */
     uint32_t learned_seed; /* 1: seed NN-descent from learned codes (kcna_seed_learned) */
     uint32_t verbosity;  /* 0 silent, 1 per-phase lines on stderr */
-    uint32_t reserved[5];
+    uint32_t refine;     /* kcna_refine: the refinement between prune loops */
+    uint32_t reserved[4];
 } kcna_params;
 
 /* Fills p with the reference defaults (src/kgraph.h:12-40). */
@@ -217,6 +224,13 @@ kcna_status kcna_prune(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind)
 /* Prune + reverse-edge insert + re-prune of over-full nodes.  Replaces
  * nsg_Link / taumg_Link / alphapg_Link (src/kgraph.cpp:2087-2143, 3085-3141, 3424-3480). */
 kcna_status kcna_link(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind);
+/* Per-node pool search of loop `loopcount` (>= 1): every node's pool is the
+ * beam of a greedy search over the context graph, expanding the entries at
+ * positions < min(search_L + (loopcount - 1) * step, MAXL).  Replaces inSearch /
+ * poolSearch (src/kgraph.cpp:3667-3688, 2340-2414); kcna_build runs it between
+ * prune loops when params->refine is KCNA_REFINE_POOL_SEARCH.  comps (may be
+ * NULL) receives the distance evaluations. */
+kcna_status kcna_pool_search(kcna_ctx *ctx, const kcna_params *params, uint32_t loopcount, uint64_t *comps);
 /* Installs a caller graph (ids n*width padded with 0xFFFFFFFF, degrees n). */
 kcna_status kcna_set_graph(kcna_ctx *ctx, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep);
 

@@ -1024,6 +1024,79 @@ struct Builder {
     }
 
     // buildFastNSG / TauMNG / AlphaPG / HNSW layer: src/kgraph.cpp:3720-3966
+    // Per-node pool search, src/kgraph.cpp:2340-2414 (poolSearch) driven by
+    // inSearch (:3667-3688); the reference's builds call BridgeView in its
+    // place (the inSearch calls at :3761, :3835, :3893, :3950 are commented
+    // out).  Node q's pool is its beam: the entries at positions < cur_L are
+    // expanded in pool order, each expansion inserting the unvisited graph
+    // neighbours of the expanded node into the pool (InsertIntoPool), and the
+    // scan restarts at the lowest position an insert landed at.  Only q's own
+    // pool changes, so the result does not depend on thread timing.  Two
+    // stated choices where the reference reads undefined state: the initial
+    // radius is pool.back().dist (:2347), the overflow slot, which admits
+    // exactly the inserts that reach pool[0, L) when it is taken as
+    // pool[L - 1].dist for a full pool and +inf otherwise; positions at or
+    // past the pool count are empty and not expanded.  Returns the distance
+    // evaluations.
+    uint64_t pool_search(unsigned q, std::vector<uint32_t> &mark, uint32_t stamp) {
+        auto &h = nh[q];
+        h.pool.resize(MAXL + 1);
+        float radius = h.L >= MAXL ? h.pool[h.L - 1].dist : std::numeric_limits<float>::max();
+        const unsigned cur_loop = loopcount - 1;
+        const unsigned cur_L = std::min(P.search_L + cur_loop * P.step, MAXL);
+        const unsigned pre_L = cur_loop == 0 ? 0 : std::min(P.search_L + (cur_loop - 1) * P.step, MAXL);
+        for (unsigned t = 0; t < h.L; ++t) { // :2353-2384
+            mark[h.pool[t].id] = stamp;
+            h.pool[t].isnew = cur_loop > 0 && t >= pre_L && t < cur_L ? h.pool[t].flag : false;
+            h.pool[t].flag = true;
+        }
+        uint64_t cc = 0;
+        unsigned k = 0;
+        while (k < cur_L) { // :2386-2410
+            unsigned nk = cur_L;
+            if (k < h.L && h.pool[k].flag) {
+                h.pool[k].flag = false;
+                const unsigned n = h.pool[k].id;
+                for (const auto &e : nh[n].nn_nsg) {
+                    const unsigned id = e.id;
+                    if (mark[id] == stamp || id == q) continue;
+                    mark[id] = stamp;
+                    ++cc;
+                    const float dist = D(q, id);
+                    unsigned r = (unsigned)h.pool.size();
+                    if (dist <= radius) { // parallel_InsertIntoPool, :1539-1559
+                        Nb nn(id, dist, true);
+                        nn.isnew = true;
+                        r = (unsigned)insert_into_pool(&h.pool[0], h.L, nn);
+                        if (r <= h.L) {
+                            if (h.L + 1 < h.pool.size())
+                                ++h.L;
+                            else
+                                radius = h.pool[h.L - 1].dist;
+                        }
+                    }
+                    if (r < nk) nk = r;
+                }
+            }
+            k = nk <= k ? nk : k + 1;
+        }
+        return cc;
+    }
+
+    // src/kgraph.cpp:3667-3688 (inSearch)
+    uint64_t in_search() {
+        uint64_t cc = 0;
+#pragma omp parallel reduction(+ : cc)
+        {
+            std::vector<uint32_t> mark(D.n, 0);
+            uint32_t stamp = 0;
+#pragma omp for schedule(dynamic, 100)
+            for (int i = 0; i < (int)D.n; ++i) cc += pool_search((unsigned)i, mark, ++stamp);
+        }
+        bridge_comps += cc;
+        return cc;
+    }
+
     void build() {
         nndescent();
         std::mt19937 rng(P.seed);
@@ -1050,7 +1123,10 @@ struct Builder {
             loopcount++;
             if (iter == iters) break;
             double s = now();
-            bridge_view();
+            if (P.refine == KCNA_REFINE_POOL_SEARCH)
+                in_search();
+            else
+                bridge_view();
             if (loopcount - 1 < KCNA_MAX_LOOPS) st->search_time[loopcount - 1] = now() - s;
             if (loopcount <= KCNA_MAX_LOOPS) st->loop_recall[loopcount] = evaluate();
         }
@@ -1208,6 +1284,36 @@ int kcnao_prune(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t 
         for (int q = 0; q < (int)n; ++q) B.sync_prune(q);
     }
     store_graph(B, out_ids, out_d, out_deg, width);
+    return 0;
+}
+
+// Per-node pool search (inSearch of loop `loopcount`) of the given pools over
+// the given graph; pools out (n x cap) and the distance evaluations.
+int kcnao_pool_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p,
+                      const uint32_t *pid, const float *pd, const uint32_t *pcnt, uint32_t cap,
+                      const uint32_t *g_ids, const uint32_t *g_deg, uint32_t width, uint32_t loopcount,
+                      uint32_t *out_ids, float *out_d, uint32_t *out_cnt, uint64_t *comps, int nthreads) {
+    set_threads(nthreads);
+    kcna_stats st;
+    memset(&st, 0, sizeof st);
+    Builder B(Data{X, stride, n, d}, *p, KCNA_NSG, &st);
+    B.MAXL = cap;
+    load_pools(B, pid, pd, pcnt, cap);
+    for (unsigned i = 0; i < n; ++i) {
+        B.nh[i].nn_nsg.clear();
+        for (uint32_t j = 0; j < std::min(g_deg[i], width); ++j)
+            B.nh[i].nn_nsg.push_back(Nb(g_ids[(uint64_t)i * width + j], 0.f, false));
+    }
+    B.loopcount = loopcount;
+    *comps = B.in_search();
+    for (unsigned i = 0; i < n; ++i) {
+        const auto &h = B.nh[i];
+        out_cnt[i] = h.L;
+        for (uint32_t j = 0; j < cap; ++j) {
+            out_ids[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].id : 0xFFFFFFFFu;
+            out_d[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].dist : INFINITY;
+        }
+    }
     return 0;
 }
 

@@ -29,7 +29,7 @@ class Params(C.Structure):
         (n, C.c_uint32) for n in ("nsg_R", "search_L", "search_K", "step", "massq_S", "loop_i")
     ] + [("tau", C.c_float), ("angle", C.c_float)] + [
         ("screen", C.c_uint32), ("learned_seed", C.c_uint32), ("verbosity", C.c_uint32),
-        ("reserved", C.c_uint32 * 5),
+        ("refine", C.c_uint32), ("reserved", C.c_uint32 * 4),
     ]
 
 
@@ -64,7 +64,7 @@ def params(**kw) -> Params:
     p = Params()
     d = dict(K=25, L=100, S=10, R=100, iterations=30, controls=100, seed=2024, nthreads=40, delta=0.002,
              recall=0.95, nsg_R=50, search_L=40, search_K=500, step=10, massq_S=10, loop_i=2, tau=0.0,
-             angle=60.0, screen=0, learned_seed=0, verbosity=0)
+             angle=60.0, screen=0, learned_seed=0, verbosity=0, refine=0)
     d.update(kw)
     for k, v in d.items():
         setattr(p, k, v)
@@ -174,6 +174,23 @@ class Oracle(_Lib):
     def link(self, kind, X, p, pid, pd, pcnt, width, nthreads=0):
         return self._graph_call("link", kind, X, p, pid, pd, pcnt, width, nthreads)
 
+    def pool_search(self, X, p, pid, pd, pcnt, g_ids, g_deg, loopcount, nthreads=0):
+        """inSearch of loop `loopcount` on the given pools over the given graph:
+        (pool ids, dists, counts, distance evaluations)."""
+        X, pid, pd, pcnt, g_ids, g_deg = _f32(X), _u32(pid), _f32(pd), _u32(pcnt), _u32(g_ids), _u32(g_deg)
+        n, d = X.shape
+        cap = pid.shape[1]
+        oi = np.empty((n, cap), np.uint32)
+        od = np.empty((n, cap), np.float32)
+        oc = np.empty(n, np.uint32)
+        cc = C.c_uint64(0)
+        rc = self.fn("pool_search")(_ptr(X), C.c_uint64(d), C.c_uint32(n), C.c_uint32(d), C.byref(p), _ptr(pid),
+                                    _ptr(pd), _ptr(pcnt), C.c_uint32(cap), _ptr(g_ids), _ptr(g_deg),
+                                    C.c_uint32(g_ids.shape[1]), C.c_uint32(loopcount), _ptr(oi), _ptr(od), _ptr(oc),
+                                    C.byref(cc), C.c_int(nthreads))
+        assert rc == 0, rc
+        return oi, od, oc, cc.value
+
     def beam_search(self, X, g_ids, g_deg, Q, init_ids, L, k, nthreads=0):
         X, g_ids, g_deg, Q, init_ids = _f32(X), _u32(g_ids), _u32(g_deg), _f32(Q), _u32(init_ids)
         n, d = X.shape
@@ -270,6 +287,19 @@ class Reference(_Lib):
 
     def link(self, kind, X, p, pid, pd, pcnt, width):
         return self._graph_call("link", kind, X, p, pid, pd, pcnt, width)
+
+    def pool_search(self, X, p, pid, pd, pcnt, g_ids, g_deg, loopcount, nthreads=8):
+        X, pid, pd, pcnt, g_ids, g_deg = _f32(X), _u32(pid), _f32(pd), _u32(pcnt), _u32(g_ids), _u32(g_deg)
+        n, d = X.shape
+        cap = pid.shape[1]
+        oi = np.empty((n, cap), np.uint32)
+        od = np.empty((n, cap), np.float32)
+        oc = np.empty(n, np.uint32)
+        scan = C.c_float(0)
+        self.fn("pool_search")(_ptr(X), C.c_uint64(d), C.c_uint32(n), C.c_uint32(d), C.byref(p), _ptr(pid), _ptr(pd),
+                               _ptr(pcnt), C.c_uint32(cap), _ptr(g_ids), _ptr(g_deg), C.c_uint32(g_ids.shape[1]),
+                               C.c_uint32(loopcount), C.c_int(nthreads), _ptr(oi), _ptr(od), _ptr(oc), C.byref(scan))
+        return oi, od, oc, scan.value
 
     def beam_search(self, X, g_ids, g_deg, Q, init_ids, L, k):
         X, g_ids, g_deg, Q, init_ids = _f32(X), _u32(g_ids), _u32(g_deg), _f32(Q), _u32(init_ids)

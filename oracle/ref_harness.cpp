@@ -231,6 +231,38 @@ int kref_link(int kind, const float *X, uint64_t stride, uint32_t n, uint32_t d,
     return 0;
 }
 
+// inSearch (src/kgraph.cpp:3667-3688) of loop `loopcount` on the given pools
+// over the given graph; pools out (n x cap) and the scan rate it returns.
+int kref_pool_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p,
+                     const uint32_t *pid, const float *pd, const uint32_t *pcnt, uint32_t cap, const uint32_t *g_ids,
+                     const uint32_t *g_deg, uint32_t width, uint32_t loopcount, int nthreads, uint32_t *out_ids,
+                     float *out_d, uint32_t *out_cnt, float *scan) {
+    Quiet quiet;
+    omp_set_num_threads(nthreads);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraphConstructor *con = empty_constructor(O, p, pid, pd, pcnt, cap);
+    for (unsigned i = 0; i < n; ++i) {
+        con->nhoods[i].nn_nsg.clear();
+        for (unsigned j = 0; j < std::min(g_deg[i], width); ++j)
+            con->nhoods[i].nn_nsg.push_back(Neighbor(g_ids[(uint64_t)i * width + j], 0.f, false));
+    }
+    con->loopcount = loopcount;
+    con->inSearch();
+    *scan = con->search_cc.empty() ? 0.f : con->search_cc.back();
+    for (unsigned i = 0; i < n; ++i) {
+        auto &h = con->nhoods[i];
+        out_cnt[i] = std::min<uint32_t>(h.L, cap);
+        for (unsigned j = 0; j < cap; ++j) {
+            out_ids[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].id : 0xFFFFFFFFu;
+            out_d[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].dist : INFINITY;
+        }
+    }
+    delete con;
+    return 0;
+}
+
 int kref_beam_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, const uint32_t *g_ids,
                      const uint32_t *g_deg, uint32_t width, const float *Q, uint64_t qstride, uint32_t m,
                      const uint32_t *init_ids, uint32_t L, uint32_t k, uint32_t *out_ids, float *out_d) {

@@ -13,7 +13,10 @@ stores its outputs:
     the NSG link graph from fixed seed ids;
   * into ref_cagra_*.npz, the CAGRA-style rank prune (BuildCagra,
     src/kgraph.cpp:2665-2829) of the stored pools with K = 48 and K = 46, the
-    order of equal-rank reverse entries fixed as oracle/ref_harness.cpp states.
+    order of equal-rank reverse entries fixed as oracle/ref_harness.cpp states;
+  * into ref_pool_search_*.npz, the per-node pool search (inSearch,
+    src/kgraph.cpp:2340-2414, 3667-3688) of the stored pools over the stored
+    NSG link graph, loops 1 and 2.
 The datasets are stored with the outputs (C2-like rows as uint8).
 
 Usage: python tests/golden/make_golden.py   (needs oracle/_ref built here)
@@ -73,6 +76,21 @@ def make_cagra(name):
     np.savez_compressed(os.path.join(HERE, f"ref_cagra_{name}.npz"), **out)
 
 
+def make_pool_search(name):
+    """inSearch of loops 1 and 2 on the pools and NSG link graph of ref_<name>.npz."""
+    ref = oracle_py.Reference()
+    z = dict(np.load(os.path.join(HERE, f"ref_{name}.npz")))
+    X = z["X"].astype(np.float32)
+    p = oracle_py.params(**PARAMS, tau=float(z["tau"]))
+    out = {}
+    for loop in (1, 2):
+        oi, od, oc, scan = ref.pool_search(X, p, z["pool_ids"], z["pool_d"], z["pool_cnt"], z["link_nsg_ids"],
+                                           z["link_nsg_deg"], loop, nthreads=1)
+        out[f"loop{loop}_ids"], out[f"loop{loop}_d"], out[f"loop{loop}_cnt"] = oi, od, oc
+        out[f"loop{loop}_scan"] = np.float32(scan)
+    np.savez_compressed(os.path.join(HERE, f"ref_pool_search_{name}.npz"), **out)
+
+
 if __name__ == "__main__":
     if not oracle_py.Reference.available():
         sys.exit("oracle/_ref/libkcna_ref.so is missing: run oracle/build_ref.sh")
@@ -80,4 +98,6 @@ if __name__ == "__main__":
     make("c2", synth.base("c2", N), 10.0)
     make_cagra("c1")
     make_cagra("c2")
+    make_pool_search("c1")
+    make_pool_search("c2")
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

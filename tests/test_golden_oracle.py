@@ -87,3 +87,21 @@ def test_cagra_prune(oracle, name, k):
         assert np.array_equal(gd, c[f"k{k}_d"])
     else:
         np.testing.assert_allclose(gd, c[f"k{k}_d"], rtol=2e-6)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("loop", [1, 2])
+def test_pool_search(oracle, name, loop):
+    """Per-node pool search (inSearch) of the reference's pools over its NSG
+    link graph: pools identical, and the same distance evaluations."""
+    z = load(name)
+    g = dict(np.load(os.path.join(HERE, f"ref_pool_search_{name}.npz")))
+    p = oracle_py.params(**P, tau=float(z["tau"]))
+    oi, od, oc, cc = oracle.pool_search(z["X"], p, z["pool_ids"], z["pool_d"], z["pool_cnt"], z["link_nsg_ids"],
+                                        z["link_nsg_deg"], loop)
+    assert np.array_equal(oc, g[f"loop{loop}_cnt"])
+    assert np.array_equal(oi, g[f"loop{loop}_ids"])
+    if name == "c2":
+        assert np.array_equal(od, g[f"loop{loop}_d"])
+    n = z["X"].shape[0]
+    assert cc / (n * (n - 1) / 2) == pytest.approx(float(g[f"loop{loop}_scan"]), rel=1e-5)
