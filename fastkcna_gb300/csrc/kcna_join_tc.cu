@@ -12,8 +12,9 @@
 // FMA-chain distance bit for bit and the join emits exactly the candidates of
 // the FP32 kernel.  Screen mode (rows not exact in BF16): the rows are
 // rounded to BF16 and a pair is emitted when its Gram distance is below a
-// bound on the rounding error; every emitted pair is recomputed in FP32
-// afterwards (rescore_kernel in kcna_nnd.cu).
+// bound on the rounding error; every emitted pair whose id is not already in
+// the target's pool is recomputed in FP32 afterwards (rescore_kernel in
+// kcna_nnd.cu; a repeat would be dropped by the merge anyway).
 //
 // A node's set (A then B) is ~20-60 rows and A ~10-30 columns, so one node
 // per 128-row tile would leave most TMEM lanes idle.  Tiles are packed: the

@@ -804,29 +804,68 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) select_reverse_kernel(uint32_t
 }
 
 // BF16 screen mode: every candidate the screening join emitted is recomputed
-// with the canonical FP32 chain from the FP32 rows; a candidate beyond the
-// target's radius becomes an empty key (the merges skip those).  Warp per
-// target, the target's row in shared memory, lane per candidate.
+// with the canonical FP32 chain from the FP32 rows, unless its id is already
+// in the target's pool: such a repeat carries the pool entry's own distance
+// (the chain is symmetric), so the merge would drop it as equal to that entry,
+// and it becomes an empty key without a recompute.  A recomputed candidate
+// beyond the target's radius becomes an empty key too (the merges skip those).
+// Warp per target: the target's row in shared memory and its first np pool
+// ids (np = min(count, limit), the entries the merge compares against) in an
+// open-addressing table of ht slots; lane per candidate.  ht = 0 skips the
+// repeat test.  (Adding the candidate ids to the table as well, to skip
+// repeats within the buffer, was measured slower: the larger table costs
+// occupancy and the inserts cost atomics.)
 __global__ void __launch_bounds__(256) rescore_kernel(const float *__restrict__ X, int ld, uint32_t N,
                                                       uint64_t *__restrict__ cand, const uint32_t *__restrict__ cand_cnt,
                                                       uint32_t CB, const float *__restrict__ radius,
-                                                      unsigned long long *rescored) {
-    extern __shared__ __align__(16) float s_rows[]; // 8 warps x ld
+                                                      const uint64_t *__restrict__ pool,
+                                                      const uint32_t *__restrict__ pool_cnt, uint32_t cap,
+                                                      uint32_t limit, uint32_t ht, unsigned long long *rescored,
+                                                      unsigned long long *repeats) {
+    extern __shared__ __align__(16) float s_rows[]; // 8 warps x ld, then 8 warps x ht table slots
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t t = blockIdx.x * 8 + w;
     if (t >= N) return;
     float *xt = s_rows + (size_t)w * ld;
+    uint32_t *tab = reinterpret_cast<uint32_t *>(s_rows + (size_t)8 * ld) + (size_t)w * ht;
     for (int k = lane; k < ld; k += 32) xt[k] = X[(uint64_t)t * ld + k];
+    if (ht) {
+        for (uint32_t h = lane; h < ht; h += 32) tab[h] = KCNA_NONE;
+        __syncwarp();
+        const uint32_t np = min(pool_cnt[t], min(limit, cap));
+        for (uint32_t i = lane; i < np; i += 32) {
+            const uint32_t id = kcna_key_id(pool[(uint64_t)t * cap + i]);
+            uint32_t h = (id * 0x9E3779B1u) & (ht - 1);
+            for (uint32_t probe = 0; probe < ht; ++probe, h = (h + 1) & (ht - 1)) {
+                const uint32_t old = atomicCAS(&tab[h], KCNA_NONE, id);
+                if (old == KCNA_NONE || old == id) break;
+            }
+        }
+    }
     __syncwarp();
     const uint32_t nc = min(cand_cnt[t], CB);
     const float rad = radius[t];
     uint64_t *buf = cand + (uint64_t)t * CB;
     const float4 *x4 = reinterpret_cast<const float4 *>(xt);
-    unsigned long long n = 0;
+    unsigned long long n = 0, rep = 0;
     for (uint32_t j = lane; j < nc; j += 32) {
         const uint64_t k = buf[j];
         if (kcna_key_noflags(k) == KCNA_EMPTY_KEY_NOFLAGS) continue;
         const uint32_t id = kcna_key_id(k);
+        bool in_pool = false;
+        if (ht) {
+            uint32_t h = (id * 0x9E3779B1u) & (ht - 1);
+            for (uint32_t probe = 0; probe < ht; ++probe, h = (h + 1) & (ht - 1)) {
+                const uint32_t e = tab[h];
+                if (e == id) in_pool = true;
+                if (e == id || e == KCNA_NONE) break;
+            }
+        }
+        if (in_pool) {
+            buf[j] = KCNA_EMPTY_KEY;
+            ++rep;
+            continue;
+        }
         const float4 *xc = reinterpret_cast<const float4 *>(X + (uint64_t)id * ld);
         float d = 0.f;
         for (int q = 0; q < (ld >> 2); ++q) d = kcna_acc4(d, x4[q], __ldg(xc + q));
@@ -834,7 +873,9 @@ __global__ void __launch_bounds__(256) rescore_kernel(const float *__restrict__ 
         ++n;
     }
     n = kcna_warp_sum(n);
+    rep = kcna_warp_sum(rep);
     if (lane == 0 && n) atomicAdd(rescored, n);
+    if (lane == 0 && rep) atomicAdd(repeats, rep);
 }
 
 // control recall: |pool[0..min(cnt,K)) ∩ exact[0..K)| per control
@@ -978,8 +1019,20 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     if ((c->gram_exact || c->bf16_screen) && kcna_join_tc_fits(a)) {
         KCNA_TRY(kcna_join_tc_launch(c, a));
         if (c->bf16_screen) {
-            rescore_kernel<<<kcna_div_up(c->n, 8), 256, (size_t)8 * c->ld * 4, c->stream>>>(
-                c->X, (int)c->ld, c->n, c->cand, c->cand_cnt, c->CB, c->radius, c->counters + 13);
+            const uint32_t limit = std::min(p->L, c->cap);
+            uint32_t ht = 64; // the pool ids at half load at most
+            while (ht < 2 * limit) ht <<= 1;
+            size_t rs = (size_t)8 * c->ld * 4 + (size_t)8 * ht * 4;
+            if (rs > 160 * 1024) { // very long pools: recompute every candidate
+                ht = 0;
+                rs = (size_t)8 * c->ld * 4;
+            }
+            KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                             (int)std::max<size_t>(rs, 48 * 1024)),
+                                     "rescore smem attr"));
+            rescore_kernel<<<kcna_div_up(c->n, 8), 256, rs, c->stream>>>(
+                c->X, (int)c->ld, c->n, c->cand, c->cand_cnt, c->CB, c->radius, c->pool, c->pool_cnt, c->cap, limit,
+                ht, c->counters + 13, c->counters + 14);
             KCNA_LAUNCHED(c);
             KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "rescore_kernel"));
         }
