@@ -285,6 +285,21 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     return KCNA_OK;
 }
 
+kcna_status kcna_rows_reset(kcna_ctx *c, uint32_t n, uint32_t d) {
+    if (n < 2 || d == 0 || n > KCNA_MAX_ID) return kcna_fail(c, KCNA_E_ARG, "upload: need n >= 2, d >= 1, n < 2^30");
+    KCNA_TRY(bind(c));
+    free_state(c);
+    if (c->X) cudaFree(c->X);
+    c->X = nullptr;
+    release_row_copies(c);
+    c->d = d;
+    c->ld = (d + 3) & ~3u;
+    c->n_total = c->n = n;
+    KCNA_TRY(kcna_alloc(c, &c->X, (size_t)n * c->ld, "rows"));
+    if (c->ld != d) KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->X, 0, (size_t)n * c->ld * 4, c->stream), "memset"));
+    return KCNA_OK;
+}
+
 extern "C" {
 
 void kcna_params_default(kcna_params *p) {
@@ -340,6 +355,7 @@ kcna_status kcna_create(kcna_ctx **out, int device) {
 
 void kcna_destroy(kcna_ctx *c) {
     if (!c) return;
+    if (c->writer.joinable()) c->writer.join();
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_state(c);
@@ -363,18 +379,9 @@ void *kcna_stream(const kcna_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 static kcna_status upload(kcna_ctx *c, const float *rows, uint32_t n, uint32_t d, uint64_t stride, cudaMemcpyKind kind) {
     if (!c) return KCNA_E_ARG;
-    if (!rows || n < 2 || d == 0 || stride < (uint64_t)d * 4 || n > KCNA_MAX_ID)
+    if (!rows || stride < (uint64_t)d * 4)
         return kcna_fail(c, KCNA_E_ARG, "upload: need rows, n >= 2, d >= 1, stride >= 4*d, n < 2^30");
-    KCNA_TRY(bind(c));
-    free_state(c);
-    if (c->X) cudaFree(c->X);
-    c->X = nullptr;
-    release_row_copies(c);
-    c->d = d;
-    c->ld = (d + 3) & ~3u;
-    c->n_total = c->n = n;
-    KCNA_TRY(kcna_alloc(c, &c->X, (size_t)n * c->ld, "rows"));
-    if (c->ld != d) KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->X, 0, (size_t)n * c->ld * 4, c->stream), "memset"));
+    KCNA_TRY(kcna_rows_reset(c, n, d));
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpy2DAsync(c->X, (size_t)c->ld * 4, rows, stride, (size_t)d * 4, n, kind, c->stream),
                              "upload copy"));
     return kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "upload sync");
@@ -757,25 +764,6 @@ kcna_status kcna_search(kcna_ctx *c, const float *queries, uint32_t m, uint64_t 
     cudaFree(oid);
     cudaFree(od);
     return s == KCNA_OK ? kcna_check_device_err(c, "search") : s;
-}
-
-kcna_status kcna_write_nsg(kcna_ctx *c, const char *path) {
-    if (!c || !c->has_graph) return kcna_fail(c, KCNA_E_STATE, "write_nsg: no graph");
-    if (!path) return kcna_fail(c, KCNA_E_ARG, "write_nsg: null path");
-    std::vector<uint32_t> ids((size_t)c->n * c->W), deg(c->n);
-    uint32_t ep = 0, W = 0;
-    KCNA_TRY(kcna_get_graph(c, ids.data(), deg.data(), &ep, &W));
-    uint32_t width = 0;
-    for (uint32_t d : deg) width = std::max(width, d);
-    FILE *f = fopen(path, "wb");
-    if (!f) return kcna_fail(c, KCNA_E_IO, std::string("write_nsg: cannot open ") + path);
-    bool ok = fwrite(&width, 4, 1, f) == 1 && fwrite(&ep, 4, 1, f) == 1;
-    for (uint32_t i = 0; ok && i < c->n; ++i) {
-        uint32_t gk = std::min(deg[i], W);
-        ok = fwrite(&gk, 4, 1, f) == 1 && (gk == 0 || fwrite(ids.data() + (size_t)i * W, 4, gk, f) == gk);
-    }
-    ok = (fclose(f) == 0) && ok;
-    return ok ? KCNA_OK : kcna_fail(c, KCNA_E_IO, std::string("write_nsg: write failed for ") + path);
 }
 
 } // extern "C"

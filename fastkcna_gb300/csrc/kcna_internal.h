@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kcna.h"
@@ -17,6 +18,11 @@ struct kcna_ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     std::string err;
+    // background file writer (kcna_write_nsg_async): one write in flight; its
+    // outcome is read after join
+    std::thread writer;
+    kcna_status writer_status = KCNA_OK;
+    std::string writer_err;
     uint64_t launches = 0;
     int *d_err = nullptr; // device error word (kcna_common.cuh KCNA_DERR_*)
 
@@ -163,6 +169,8 @@ kcna_status kcna_seed_finish(kcna_ctx *c, const kcna_params *p);
 // kcna_graph.cu: prune / link / entry point / connectivity / P2K / search
 kcna_status kcna_exclusive_scan_u32(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t *out, uint64_t *total_h);
 kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W);
+// Drops every state and allocates (zero-padded) device rows for n x d floats.
+kcna_status kcna_rows_reset(kcna_ctx *c, uint32_t n, uint32_t d);
 kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t *comps);
 // CAGRA-style rank prune of the pools into the graph (kcna_cagra.cu).
 kcna_status kcna_cagra_prune(kcna_ctx *c, const kcna_params *p);

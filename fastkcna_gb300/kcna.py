@@ -131,6 +131,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "kcna_kernel_launches": ([P], U64),
         "kcna_stream": ([P], C.c_void_p),
         "kcna_write_nsg": ([P, C.c_char_p], C.c_int),
+        "kcna_write_nsg_async": ([P, C.c_char_p], C.c_int),
+        "kcna_wait_writes": ([P], C.c_int),
+        "kcna_upload_lshkit": ([P, C.c_char_p], C.c_int),
+        "kcna_pool_search": ([P, C.POINTER(Params), U32, C.POINTER(U64)], C.c_int),
     }
     for name, (argt, rest) in sig.items():
         f = getattr(lib, name)
@@ -311,6 +315,21 @@ class Index:
 
     def write_nsg(self, path: str):
         self._check(self.lib.kcna_write_nsg(self.h, path.encode()))
+
+    def write_nsg_async(self, path: str):
+        """Snapshot the graph and write the NSG file on a host thread."""
+        self._check(self.lib.kcna_write_nsg_async(self.h, path.encode()))
+
+    def wait_writes(self):
+        self._check(self.lib.kcna_wait_writes(self.h))
+
+    def upload_lshkit(self, path: str):
+        """Rows straight from an lshkit file (mapped, streamed through pinned buffers)."""
+        self._check(self.lib.kcna_upload_lshkit(self.h, path.encode()))
+        import struct
+        with open(path, "rb") as f:
+            _, _, d = struct.unpack("<III", f.read(12))
+        self.n, self.d = (os.path.getsize(path) - 12) // (4 * d), d
 
 
 def version() -> str:

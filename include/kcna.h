@@ -176,6 +176,11 @@ const char *kcna_version(void); /* replaces KGraph::version (src/kgraph.cpp:3973
 kcna_status kcna_upload(kcna_ctx *ctx, const float *rows, uint32_t n, uint32_t d, uint64_t stride_bytes);
 /* Same, from DEVICE memory of the context's device (no host copy). */
 kcna_status kcna_upload_device(kcna_ctx *ctx, const float *dev_rows, uint32_t n, uint32_t d, uint64_t stride_bytes);
+/* Loads an lshkit float file (u32 header {4, rows, cols}, then the rows; the
+ * row count follows from the file size) straight into the context: the file
+ * is mapped and streamed through two pinned 64 MiB staging buffers.  Replaces
+ * Matrix::load_lshkit + MatrixOracle (src/kgraph-data.h:161-177, 262-274). */
+kcna_status kcna_upload_lshkit(kcna_ctx *ctx, const char *path);
 /* Restricts every following call to the first n_prefix rows.
  * Replaces IndexOracle::set_size (src/kgraph.h:80, src/kgraph-data.h:372-382). */
 kcna_status kcna_set_size(kcna_ctx *ctx, uint32_t n_prefix);
@@ -296,6 +301,12 @@ kcna_status kcna_encoder_grads(kcna_ctx *ctx, const float *rows, uint32_t n_rows
 /* Writes the graph in the NSG/efanna format written by SaveNsg
  * (src/kgraph.cpp:1704-1724): u32 width, u32 ep, per node u32 GK + GK u32 ids. */
 kcna_status kcna_write_nsg(kcna_ctx *ctx, const char *path);
+/* Same file, written on a host thread after one device-to-host snapshot of the
+ * graph, so the caller can go on; one write in flight per context.
+ * kcna_wait_writes joins it and returns its outcome (KCNA_E_IO on failure);
+ * kcna_destroy joins it too. */
+kcna_status kcna_write_nsg_async(kcna_ctx *ctx, const char *path);
+kcna_status kcna_wait_writes(kcna_ctx *ctx);
 
 #ifdef __cplusplus
 }
