@@ -353,36 +353,87 @@ __global__ void __launch_bounds__(BAND_WARPS * 32) seed_band_kernel(R rows, uint
 
 // Initial pools, step 2: node i's slots sorted by (distance, id); the same id
 // from several tables gives the same key, so repeats are adjacent and dropped;
-// the nearest `limit` distinct entries become the pool.
+// the nearest `limit` distinct entries become the pool.  Warp per node, the
+// 1024 slots held in registers (32 per lane, slot 32 r + lane in k[r]) and
+// sorted by a bitonic network: strides below 32 exchange across lanes by
+// shuffles, larger strides between a lane's own registers.
+static_assert(SEED_CAND == 1024, "the collect sort holds 32 keys per lane");
+
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
+    const uint32_t lo = __shfl_xor_sync(KCNA_FULL, (uint32_t)v, m);
+    const uint32_t hi = __shfl_xor_sync(KCNA_FULL, (uint32_t)(v >> 32), m);
+    return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ uint64_t shfl_idx64(uint64_t v, int src) {
+    const uint32_t lo = __shfl_sync(KCNA_FULL, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(KCNA_FULL, (uint32_t)(v >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ uint64_t shfl_up64(uint64_t v, int d) {
+    const uint32_t lo = __shfl_up_sync(KCNA_FULL, (uint32_t)v, d);
+    const uint32_t hi = __shfl_up_sync(KCNA_FULL, (uint32_t)(v >> 32), d);
+    return ((uint64_t)hi << 32) | lo;
+}
+
+// Ascending bitonic sort of the 1024 keys k[r] (key index 32 r + lane).
+__device__ __forceinline__ void warp_sort1024(uint64_t (&k)[32], int lane) {
+#pragma unroll
+    for (int size = 2; size <= 1024; size <<= 1) {
+#pragma unroll
+        for (int j = size >> 1; j > 0; j >>= 1) {
+            if (j >= 32) { // partner in this lane's register r ^ (j / 32)
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < 32; ++r) {
+                    if (r & jr) continue;
+                    const bool asc = ((r * 32) & size) == 0;
+                    const uint64_t x = k[r], y = k[r | jr];
+                    const bool sw = asc ? x > y : x < y;
+                    k[r] = sw ? y : x;
+                    k[r | jr] = sw ? x : y;
+                }
+            } else { // partner in lane ^ j, same register
+#pragma unroll
+                for (int r = 0; r < 32; ++r) {
+                    const bool asc = (((r * 32) | lane) & size) == 0;
+                    const uint64_t x = k[r], y = shfl_xor64(x, j);
+                    const bool keep_min = ((lane & j) == 0) == asc;
+                    k[r] = keep_min ? (y < x ? y : x) : (y > x ? y : x);
+                }
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) seed_collect_kernel(const uint64_t *__restrict__ slots, uint32_t stride,
                                                            uint32_t N, uint32_t cap, uint32_t limit,
                                                            uint64_t *__restrict__ pool,
                                                            uint32_t *__restrict__ pool_cnt) {
-    __shared__ uint64_t s_k[4][SEED_CAND];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
     const uint32_t i = blockIdx.x * 4 + w;
     if (i >= N) return;
-    uint64_t *sk = s_k[w];
-    for (int e = lane; e < SEED_CAND; e += 32) sk[e] = slots[(uint64_t)i * stride + e];
-    kcna_warp_bitonic(sk, SEED_CAND);
-    // compaction moves entries down, so the previous key comes from registers
+    const uint64_t *src = slots + (uint64_t)i * stride;
+    uint64_t k[32];
+#pragma unroll
+    for (int r = 0; r < 32; ++r) k[r] = src[32 * r + lane];
+    warp_sort1024(k, lane);
+    uint64_t *pr = pool + (uint64_t)i * cap;
     uint32_t cnt = 0;
     uint64_t carry = KCNA_EMPTY_KEY;
-    for (int e0 = 0; e0 < SEED_CAND; e0 += 32) {
-        const uint64_t v = sk[e0 + lane];
-        uint64_t prev = __shfl_up_sync(KCNA_FULL, v, 1);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        const uint64_t v = k[r];
+        uint64_t prev = shfl_up64(v, 1);
         if (lane == 0) prev = carry;
-        carry = __shfl_sync(KCNA_FULL, v, 31);
-        const bool ok = v != KCNA_EMPTY_KEY && (e0 + lane == 0 || (prev >> 2) != (v >> 2));
+        carry = shfl_idx64(v, 31);
+        const bool ok = v != KCNA_EMPTY_KEY && (r + lane == 0 || (prev >> 2) != (v >> 2));
         const unsigned m = __ballot_sync(KCNA_FULL, ok);
-        __syncwarp();
-        if (ok) sk[cnt + __popc(m & kcna_lanemask_lt())] = v;
+        const uint32_t pos = cnt + __popc(m & kcna_lanemask_lt());
+        if (ok && pos < limit) pr[pos] = v;
         cnt += __popc(m);
-        __syncwarp();
     }
     const uint32_t keep = min(cnt, limit);
-    uint64_t *pr = pool + (uint64_t)i * cap;
-    for (uint32_t e = lane; e < cap; e += 32) pr[e] = e < keep ? sk[e] : KCNA_EMPTY_KEY;
+    for (uint32_t e = keep + lane; e < cap; e += 32) pr[e] = KCNA_EMPTY_KEY;
     if (lane == 0) pool_cnt[i] = keep;
 }
 
