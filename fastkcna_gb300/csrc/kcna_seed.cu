@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(128) seed_pools_kernel(R rows, uint32_t N, con
     }
 }
 
-// Initial pools, step 1: in the order of table tab, every position p meets
+// Initial pools, step 1 (one launch, grid row tab for table tab): in the order
+// of table tab, every position p meets
 // positions p+1 .. p+SEED_WIN; each pair's canonical distance goes to both
 // nodes' fixed candidate slots (node a's slot tab*2W + W + delta-1 holds the
 // delta-th node after it, slot tab*2W + delta-1 the delta-th node before it).
@@ -307,10 +308,13 @@ template <> struct BandStage<RowsB16> {
 __host__ __device__ constexpr int band_pitch(int ld, int elt) { return ld * elt + 4 * elt; } // bytes
 
 template <class R>
-__global__ void __launch_bounds__(BAND_WARPS * 32) seed_band_kernel(R rows, uint32_t N, const uint32_t *__restrict__ ord,
-                                                                    int tab, uint64_t *__restrict__ slots,
-                                                                    uint32_t stride, unsigned long long *comps) {
+__global__ void __launch_bounds__(BAND_WARPS * 32) seed_band_kernel(R rows, uint32_t N,
+                                                                    const uint32_t *__restrict__ orders,
+                                                                    uint64_t *__restrict__ slots, uint32_t stride,
+                                                                    unsigned long long *comps) {
     using B = BandStage<R>;
+    const int tab = (int)blockIdx.y; // one grid row per table
+    const uint32_t *__restrict__ ord = orders + (size_t)tab * N;
     extern __shared__ __align__(16) unsigned char s_band[]; // BAND_WARPS x BAND_ROWS x pitch
     const int w = threadIdx.x >> 5, lane = kcna_lane();
     const int nv = rows.ld >> 2, pitch = band_pitch(rows.ld, B::ELT);
@@ -696,10 +700,9 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
                                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                              (int)band_smem),
                                      "seed band smem attr"));
-            for (int tab = 0; tab < SEED_TABLES; ++tab)
-                seed_band_kernel<<<kcna_div_up(N, 32 * BAND_WARPS), BAND_WARPS * 32, band_smem, s>>>(
-                    rows, N, order + (size_t)tab * N, tab, slots, stride, c->counters + 30);
-            return launch_ok(c, "seed band", SEED_TABLES);
+            seed_band_kernel<<<dim3(kcna_div_up(N, 32 * BAND_WARPS), SEED_TABLES), BAND_WARPS * 32, band_smem, s>>>(
+                rows, N, order, slots, stride, c->counters + 30);
+            return launch_ok(c, "seed band");
         };
         if (c->bf16_exact)
             KCNA_TRY(band(RowsB16{c->Xh, (int)ld}));
