@@ -171,3 +171,51 @@ def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
     name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
     assert name == "prune" and r["kernel"] == "prune_kernel"
     assert r["achieved"] == pytest.approx((3 * 1000 * 500 * 128 * 4 / 3) / (0.4 / 3) / 1e9, abs=0.06)
+
+
+C_CALLER = r"""
+/* A plain C caller of the drop-in boundary: what a cgo/FFI stub would declare. */
+#include <stdio.h>
+#include "kcna.h"
+
+int build_index(const char *lshkit_path, const char *nsg_path) {
+    kcna_ctx *ctx = NULL;
+    kcna_params p;
+    kcna_stats st;
+    uint64_t comps = 0;
+    if (kcna_create(&ctx, 0) != KCNA_OK) return 1;
+    kcna_params_default(&p);
+    p.K = 500; p.L = 500; p.S = 12; p.R = 100; p.iterations = 6;
+    p.search_L = 80; p.nsg_R = 50; p.search_K = 500;
+    p.learned_seed = 1; p.screen = KCNA_SCREEN_BF16; p.refine = KCNA_REFINE_BRIDGE_VIEW;
+    if (kcna_upload_lshkit(ctx, lshkit_path) != KCNA_OK || kcna_build(ctx, &p, KCNA_NSG, &st) != KCNA_OK) {
+        fprintf(stderr, "%s\n", kcna_last_error(ctx));
+        kcna_destroy(ctx);
+        return 2;
+    }
+    kcna_write_nsg_async(ctx, nsg_path);
+    kcna_pool_search(ctx, &p, 1, &comps);
+    kcna_prune(ctx, &p, KCNA_CAGRA);
+    int rc = kcna_wait_writes(ctx) == KCNA_OK ? 0 : 3;
+    kcna_destroy(ctx);
+    return rc;
+}
+"""
+
+
+def test_c_caller_compiles_and_links(tmp_path):
+    """include/kcna.h is plain C: a C99 caller compiles and links against the
+    library (not run: no GPU here)."""
+    import shutil
+
+    from fastkcna_gb300 import build as kbuild
+
+    if not shutil.which("gcc") or not os.path.exists(kbuild.LIB):
+        pytest.skip("gcc or the built library is missing")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER + "\nint main(int argc, char **argv) { return argc > 2 ? build_index(argv[1], argv[2]) : 0; }\n")
+    cuda_lib = "/usr/local/cuda/lib64"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(kbuild.ROOT, "include"), str(src),
+                        "-o", str(tmp_path / "caller"), "-L", kbuild.HERE, "-lkcna", "-L", cuda_lib, "-lcudart",
+                        f"-Wl,-rpath,{kbuild.HERE}"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
