@@ -329,9 +329,9 @@ struct MergeArgs {
 // queued for the block merge (merge_kernel).  Same result as merging all
 // candidates.  Persistent: each warp takes nodes grid-stride, so a block
 // meets its barrier once at the end instead of waiting for its slowest node.
-// SURV is 512, or 1024 while the previous merge queued many nodes (the first
-// iterations, when the pools are filling): twice the shared memory per warp
-// and fewer warps per SM, but fewer nodes left to the block merge.
+// SURV is 512, or 1024 while the previous merge queued more than n/32 nodes
+// (the first iterations, when the pools are filling): twice the shared memory
+// per warp and fewer warps per SM, but fewer nodes left to the block merge.
 constexpr int MW_WARPS = 8;
 __host__ __device__ constexpr size_t merge_warp_bytes(uint32_t cap, int surv) {
     return ((size_t)cap * 8 + (size_t)surv * 8 + 16 + 15) & ~(size_t)15;
@@ -1071,8 +1071,11 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "merge smem attr"));
-    const bool wide = c->merge_big_last > c->n / 64; // many nodes overflowed the survivor buffer last time
-    const int surv = wide ? 1024 : 512;
+    const char *wd = getenv("KCNA_MERGE_WIDE_DIV"); // tuning override of the threshold below
+    const uint32_t wide_div = wd ? std::max(1, atoi(wd)) : 32; // 64 and 16 measured slower at C2 1M
+    const bool wide = c->merge_big_last > c->n / wide_div; // many nodes overflowed the survivor buffer last time
+    const char *sv = getenv("KCNA_MERGE_SURV");   // tuning override: 512 or 1024
+    const int surv = sv ? (atoi(sv) >= 1024 ? 1024 : 512) : wide ? 1024 : 512;
     const size_t smw = merge_warp_bytes(c->cap, surv) * MW_WARPS;
     auto launch_warp = [&](auto kern) -> kcna_status {
         KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1089,7 +1092,7 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
         kern<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
         return KCNA_OK;
     };
-    if (wide)
+    if (surv == 1024) // the template must match the shared memory sized above
         KCNA_TRY(launch_warp(merge_warp_kernel<1024>));
     else
         KCNA_TRY(launch_warp(merge_warp_kernel<512>));
