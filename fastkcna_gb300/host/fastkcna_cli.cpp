@@ -9,7 +9,8 @@
 // "--name=value", "-K value" and "-K100" are accepted.
 //
 // GB300 additions: --screen fp32|bf16 (row precision / Gram-tile join),
-// --learned 0|1 (learned initial graph), --device N, and --print-params,
+// --learned 0|1 (learned initial graph), --refine bridge|pool (the
+// refinement between prune loops), --device N, and --print-params,
 // which prints the parsed parameters as JSON and exits without touching a GPU.
 #include <stdio.h>
 #include <stdlib.h>
@@ -82,6 +83,7 @@ const Opt kHidden[] = {
     {"l2norm", "", true, "l2-normalize data, so as to mimic cosine similarity"},
     {"screen", "", false, "GB300: row precision fp32 | bf16"},
     {"learned", "", false, "GB300: 1 = learned initial graph"},
+    {"refine", "", false, "GB300: refinement between prune loops, bridge | pool"},
     {"device", "", false, "GB300: CUDA device"},
     {"print-params", "", true, "GB300: print the parsed parameters as JSON and exit"},
 };
@@ -169,11 +171,11 @@ void print_params(const KGraph::IndexParams &p, const std::string &data, const s
            "\"S\": %u, \"R\": %u, \"iterations\": %u, \"controls\": %u, \"seed\": %u, \"nthreads\": %u, "
            "\"delta\": %g, \"recall\": %g, \"nsg_R\": %u, \"search_L\": %u, \"search_K\": %u, \"step\": %u, "
            "\"massq_S\": %u, \"loop_i\": %u, \"tau\": %g, \"angle\": %g, \"prune\": %u, \"reverse\": %d, "
-           "\"screen\": %u, \"learned_seed\": %u}\n",
+           "\"screen\": %u, \"learned_seed\": %u, \"refine\": %u}\n",
            kToolNames[KCNA_CLI], data.c_str(), out.c_str(), res.c_str(), p.K, p.L, p.S, p.R, p.iterations,
            p.controls, p.seed, p.nthreads, (double)p.delta, (double)p.recall, p.nsg_R, p.search_L, p.search_K,
            p.step, p.massq_S, p.loop_i, (double)p.tau, (double)p.angle, p.prune, p.reverse, p.screen,
-           p.learned_seed);
+           p.learned_seed, p.refine);
 }
 
 template <typename T>
@@ -311,6 +313,15 @@ int run(int argc, char **argv) {
             params.screen = 1;
         else
             throw invalid_argument("--screen must be fp32 or bf16");
+    }
+    if (a.has("refine")) {
+        const std::string s = a.v["refine"];
+        if (s == "bridge" || s == "0")
+            params.refine = 0;
+        else if (s == "pool" || s == "1")
+            params.refine = 1;
+        else
+            throw invalid_argument("--refine must be bridge or pool");
     }
     if (a.has("device")) setenv("KCNA_DEVICE", a.v["device"].c_str(), 1);
     const bool lshkit = !a.has("raw");

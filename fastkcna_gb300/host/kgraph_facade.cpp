@@ -74,6 +74,7 @@ kcna_params to_params(const KGraph::IndexParams &p) {
     k.angle = p.angle;
     k.screen = p.screen;
     k.learned_seed = p.learned_seed;
+    k.refine = p.refine;
     k.verbosity = verbosity;
     return k;
 }

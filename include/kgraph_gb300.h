@@ -137,9 +137,12 @@ public:
         unsigned iter;
         unsigned qid, Lcon, sidx, B, P;
         /* GB300 build options (no reference counterpart): screening precision
-         * (0 FP32, 1 BF16) and the learned initial graph (0 off, 1 on) */
+         * (0 FP32, 1 BF16), the learned initial graph (0 off, 1 on) and the
+         * refinement between prune loops (0 BridgeView as the reference's
+         * builds, 1 the per-node pool search, inSearch) */
         unsigned screen;
         unsigned learned_seed;
+        unsigned refine;
         IndexParams()
             : nsg_R(default_nsgr), search_L(default_searchl), search_K(default_searchk), step(default_step),
               tau(default_tau), angle(default_angle), nt(0), massq_S(default_massqS), loop_i(default_loop_i),
@@ -147,7 +150,7 @@ public:
               controls(default_controls), seed(default_seed), nthreads(default_nthreads), delta(default_delta),
               recall(default_recall), prune(default_prune), reverse(default_reverse), num0(default_num0),
               incr_r(default_incr_r), sl(0), iter(default_iter), qid(0), Lcon(0), sidx(0), B(0), P(default_P),
-              screen(0), learned_seed(0) {}
+              screen(0), learned_seed(0), refine(0) {}
     };
 
     struct SearchParams {

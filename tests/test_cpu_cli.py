@@ -55,6 +55,15 @@ def test_cli_flag_forms():
     assert p["tau"] == 10 and p["angle"] == pytest.approx(55.5)
     assert p["delta"] == pytest.approx(0.01) and p["recall"] == pytest.approx(0.99)
     assert p["screen"] == 1 and p["learned_seed"] == 1
+    assert p["refine"] == 0
+
+
+def test_cli_refine_flag():
+    assert _params("fastnsg", "d.lshkit", "o.nsg", "--refine", "pool")["refine"] == 1
+    assert _params("fasttaumng", "d.lshkit", "o.nsg", "--refine=bridge")["refine"] == 0
+    r = subprocess.run([_tool("fastnsg"), "d.lshkit", "o.nsg", "--refine", "beam", "--print-params"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "--refine must be bridge or pool" in r.stderr
 
 
 def test_cli_usage_and_errors():
