@@ -97,3 +97,13 @@ def test_cli_hnsw(c1_files, tool):
         assert idx["maxlevel"] == len(pn) - 1 == int(GOLD["maxlevel_hnsw"])
         assert np.array_equal(idx["levels"], np.repeat(np.arange(len(pn) - 1, -1, -1), pn[::-1]))
     assert rec >= float(GOLD[f"recall_{tag}"]) - TOL, (rec, float(GOLD[f"recall_{tag}"]))
+
+
+def test_cli_nsg_with_pool_search_refinement(c1_files):
+    """`--refine pool`: the per-node pool search between prune loops, through
+    the command line and the C++ facade; recall@10 within the same bar."""
+    td, data, X, Q, truth = c1_files
+    out = os.path.join(td, "pool.nsg")
+    _run("fastnsg", data, out, "--result", os.path.join(td, "pool.csv"), "--refine", "pool", *FLAGS)
+    rec, _, _ = _nsg_recall(out, X, Q, truth)
+    assert rec >= float(GOLD["recall_nsg"]) - TOL, (rec, float(GOLD["recall_nsg"]))
