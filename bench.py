@@ -256,6 +256,45 @@ def search_recall10(ix, Q, truth, n, L=100):
     return hit / (10.0 * Q.shape[0]), Q.shape[0] / statistics.median(times)
 
 
+def run_search_sweep(args, local):
+    """Query-time search over the graphs of both builds (learned+BF16 and plain
+    FP32) at beam widths 10-320: recall@10 against the exact 10-NN, the same
+    with ties at the 10th distance counted as hits, and queries per second.
+    One JSON line; not the timed build measurement."""
+    from fastkcna_gb300 import kcna, synth
+
+    n = args.n
+    X = synth.base("c2", n)
+    Q = synth.queries("c2", 10000)
+    ix = kcna.Index(local)
+    ix.upload(X)
+    truth, tdist = ix.knn_queries(Q, 10)
+    curves = {}
+    for mode in ("learned_bf16", "plain"):
+        p = kcna.params(**FLAGS, **(dict(learned_seed=1, screen=1) if mode == "learned_bf16" else {}))
+        ix.build("nsg", p)
+        _, _, ep = ix.graph()
+        rows = []
+        for L in (10, 20, 40, 80, 100, 160, 320):
+            rng = np.random.default_rng(7)
+            extra = rng.choice(n, size=L, replace=False)
+            start = np.concatenate([[ep], extra[extra != ep][: L - 1]]).astype(np.uint32)
+            init = np.broadcast_to(start, (Q.shape[0], L)).copy()
+            found, fd = ix.search(Q, L, 10, init_ids=init)
+            times = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                ix.search(Q, L, 10, init_ids=init)
+                times.append(time.perf_counter() - t0)
+            rec = sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth)) / (10.0 * Q.shape[0])
+            ties = float(np.mean(np.minimum((fd <= tdist[:, 9:10]).sum(1), 10) / 10.0))
+            rows.append(dict(L=L, recall10=round(rec, 4), recall10_ties=round(ties, 4),
+                             qps=round(Q.shape[0] / statistics.median(times))))
+        curves[mode] = rows
+    print(json.dumps({"search_sweep": curves, "n": n, "queries": int(Q.shape[0]),
+                      "start": "entry point + L-1 seeded random nodes"}), flush=True)
+
+
 def run_gpu(args, ws, rank, local):
     import torch
 
@@ -402,9 +441,14 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=50_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="learned_bf16", choices=["learned_bf16", "plain"])
+    ap.add_argument("--search-sweep", action="store_true",
+                    help="print the recall@10 / QPS curve of the query-time search instead of timing builds")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.search_sweep:
+        if rank == 0:
+            run_search_sweep(args, local)
+    elif args.impl == "reference":
         run_reference(args, ws, rank)
     else:
         run_gpu(args, ws, rank, local)
