@@ -11,10 +11,11 @@ from fastkcna_gb300 import index_io, kcna, synth
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n,d", [(3000, 128), (200_000, 37)])
+@pytest.mark.parametrize("n,d", [(3000, 128), (1_000_000, 37)])
 def test_upload_lshkit_equals_host_upload(tmp_path, n, d):
-    """Rows from the file (several 64 MiB chunks at 200k x 37 padded to 40)
-    give the same exact k-NN as the same rows uploaded from host memory."""
+    """Rows from the file (at 1M x 37, padded to 40 on the device: three 64 MiB
+    chunks, so a staging buffer is reused after its event) give the same exact
+    k-NN as the same rows uploaded from host memory."""
     X = np.random.default_rng(n).normal(size=(n, d)).astype(np.float32)
     path = str(tmp_path / "x.lshkit")
     synth.write_lshkit(path, X)
