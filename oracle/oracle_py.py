@@ -234,9 +234,11 @@ class Oracle(_Lib):
 class Reference(_Lib):
     """The reference's own code (compiled by oracle/build_ref.sh)."""
 
-    def __init__(self, path=REF_SO):
+    def __init__(self, path=REF_SO, trap_faults=True):
         super().__init__(path, "kref_")
         self.lib.kref_l2.restype = C.c_float
+        if trap_faults:  # a crash in the reference's code exits 70 with a stack trace
+            self.lib.kref_trap_faults()
 
     @staticmethod
     def available(path=REF_SO) -> bool:
@@ -301,6 +303,27 @@ class Reference(_Lib):
                                C.c_uint32(loopcount), C.c_int(nthreads), _ptr(oi), _ptr(od), _ptr(oc), C.byref(scan))
         return oi, od, oc, scan.value
 
+    def refine(self, X, p, pid, pd, pcnt, g_ids, g_deg, loop, pflags=None, g_old=None, g_old_deg=None, nthreads=1):
+        """UpdateNhoods + BridgeView of P2K loop `loop` (harness kref_refine):
+        returns (pool ids, dists, counts, flags, isnew flags of g, comps)."""
+        X, pid, pd, pcnt, g_ids, g_deg = _f32(X), _u32(pid), _f32(pd), _u32(pcnt), _u32(g_ids), _u32(g_deg)
+        n, d = X.shape
+        cap, W = pid.shape[1], g_ids.shape[1]
+        pf = None if pflags is None else np.ascontiguousarray(pflags, dtype=np.uint8)
+        go = None if g_old is None else _u32(g_old)
+        god = None if g_old_deg is None else _u32(g_old_deg)
+        oi = np.empty((n, cap), np.uint32)
+        od = np.empty((n, cap), np.float32)
+        oc = np.empty(n, np.uint32)
+        of = np.empty((n, cap), np.uint8)
+        isnew = np.empty((n, W), np.uint8)
+        comps = C.c_uint64(0)
+        self.fn("refine")(_ptr(X), C.c_uint64(d), C.c_uint32(n), C.c_uint32(d), C.byref(p), _ptr(pid), _ptr(pd),
+                          _ptr(pcnt), _ptr(pf), C.c_uint32(cap), _ptr(g_ids), _ptr(g_deg), _ptr(go), _ptr(god),
+                          C.c_uint32(W), C.c_uint32(loop), C.c_int(nthreads), _ptr(oi), _ptr(od), _ptr(oc), _ptr(of),
+                          _ptr(isnew), C.byref(comps))
+        return oi, od, oc, of, isnew, comps.value
+
     def beam_search(self, X, g_ids, g_deg, Q, init_ids, L, k):
         X, g_ids, g_deg, Q, init_ids = _f32(X), _u32(g_ids), _u32(g_deg), _f32(Q), _u32(init_ids)
         n, d = X.shape
@@ -341,6 +364,28 @@ class Reference(_Lib):
             g = read_nsg(ip)
             csv = open(cp).read() if os.path.exists(cp) else ""
         return g + (csv,)
+
+
+def parse_run_csv(text):
+    """Rows of the reference's run CSV (SaveResult, src/kgraph.cpp:1725-1807):
+    {"kgraph time": [...], "recall": [...], "con time": [...], ...} as floats,
+    plus "params" (the PG_type,K,L,... row as a dict)."""
+    out = {}
+    lines = [ln for ln in text.splitlines() if ln.strip()]
+    for i, ln in enumerate(lines):
+        f = ln.split(",")
+        if f[0] == "PG_type" and i + 1 < len(lines):
+            out["params"] = dict(zip(f, lines[i + 1].split(",")))
+            continue
+        vals = []
+        for x in f[1:]:
+            try:
+                vals.append(float(x))
+            except ValueError:
+                pass
+        if f[0] and not f[0][0].isdigit():
+            out[f[0]] = vals
+    return out
 
 
 def read_nsg(path):

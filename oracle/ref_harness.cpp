@@ -29,6 +29,9 @@
 #include <unordered_set>
 #include <vector>
 #include <sys/resource.h>
+#include <execinfo.h>
+#include <signal.h>
+#include <unistd.h>
 #include <omp.h>
 #include <boost/timer/timer.hpp>
 #include <boost/progress.hpp>
@@ -126,6 +129,31 @@ void store_graph(KGraphConstructor *con, unsigned n, uint32_t *out_ids, float *o
 } // namespace
 
 extern "C" {
+
+// A fault inside the reference's code (CPU) prints the stack of function names
+// to stderr and ends the process with status 70 instead of dying by a signal,
+// so that a run log says where it happened.
+static void kref_fault_handler(int sig) {
+    void *frames[64];
+    const int n = backtrace(frames, 64);
+    const char msg[] = "kref: fault in the reference's code, stack:\n";
+    (void)!write(2, msg, sizeof msg - 1);
+    backtrace_symbols_fd(frames, n, 2);
+    (void)sig;
+    _exit(70);
+}
+
+int kref_trap_faults(void) {
+    struct sigaction sa;
+    std::memset(&sa, 0, sizeof sa);
+    sa.sa_handler = kref_fault_handler;
+    int rc = 0;
+    rc |= sigaction(SIGSEGV, &sa, nullptr);
+    rc |= sigaction(SIGBUS, &sa, nullptr);
+    rc |= sigaction(SIGFPE, &sa, nullptr);
+    rc |= sigaction(SIGILL, &sa, nullptr);
+    return rc;
+}
 
 float kref_l2(const float *a, const float *b, uint32_t d) { return metric::l2sqr::apply<float>(a, b, d); }
 
@@ -257,6 +285,63 @@ int kref_pool_search(const float *X, uint64_t stride, uint32_t n, uint32_t d, co
         for (unsigned j = 0; j < cap; ++j) {
             out_ids[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].id : 0xFFFFFFFFu;
             out_d[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].dist : INFINITY;
+        }
+    }
+    delete con;
+    return 0;
+}
+
+// One P2K refinement step as buildFastNSG runs it between prune loops
+// (src/kgraph.cpp:3813-3843): UpdateNhoods over the graph g (:3537-3584),
+// then BridgeView (:2478-2663) with loopcount `loop`.  Pools in: ids,
+// distances, counts and per-entry flags (bit 0 flag, bit 1 isnew) when
+// `pflags` is given, else flag = isnew = false.  For loop 1 every edge of g is
+// new; for loop >= 2 an edge is new when it is not in g_old.  Out: the pools
+// with their flags, the isnew flag of every edge of g (n x width bytes) and
+// the distance evaluations of the BridgeView join.
+int kref_refine(const float *X, uint64_t stride, uint32_t n, uint32_t d, const kcna_params *p, const uint32_t *pid,
+                const float *pd, const uint32_t *pcnt, const uint8_t *pflags, uint32_t cap, const uint32_t *g_ids,
+                const uint32_t *g_deg, const uint32_t *g_old, const uint32_t *g_old_deg, uint32_t width, uint32_t loop,
+                int nthreads, uint32_t *out_ids, float *out_d, uint32_t *out_cnt, uint8_t *out_flags,
+                uint8_t *out_isnew, uint64_t *comps) {
+    Quiet quiet;
+    omp_set_num_threads(nthreads);
+    Matrix<float> M;
+    fill(M, X, stride, n, d);
+    RefOracle O(M);
+    KGraphConstructor *con = empty_constructor(O, p, pid, pd, pcnt, cap);
+    for (unsigned i = 0; i < n; ++i) {
+        auto &h = con->nhoods[i];
+        for (unsigned j = 0; j < h.L && pflags; ++j) {
+            h.pool[j].flag = (pflags[(uint64_t)i * cap + j] & 1) != 0;
+            h.pool[j].isnew = (pflags[(uint64_t)i * cap + j] & 2) != 0;
+        }
+        h.old_nsg.clear();
+        for (unsigned j = 0; g_old && j < std::min(g_old_deg[i], width); ++j)
+            h.old_nsg.push_back(g_old[(uint64_t)i * width + j]);
+        h.nn_nsg.clear();
+        for (unsigned j = 0; j < std::min(g_deg[i], width); ++j)
+            h.nn_nsg.push_back(Neighbor(g_ids[(uint64_t)i * width + j], 0.f, false));
+    }
+    con->loopcount = loop - 1; // buildFastNSG: UpdateNhoods at the end of buildNSG, then loopcount++
+    con->UpdateNhoods();
+    for (unsigned i = 0; i < n; ++i)
+        for (uint32_t j = 0; j < width; ++j)
+            out_isnew[(uint64_t)i * width + j] =
+                j < con->nhoods[i].nn_nsg.size() ? (con->nhoods[i].nn_nsg[j].isnew ? 1 : 0) : 0;
+    con->loopcount = loop;
+    con->BridgeView();
+    // the reference keeps only the scan rate cc / (n (n - 1) / 2), summed in FP32 over the rounds
+    const float rate = con->search_cc.empty() ? 0.f : con->search_cc.back();
+    *comps = (uint64_t)std::llround((double)rate * ((double)n * (double)(n - 1) / 2.0));
+    for (unsigned i = 0; i < n; ++i) {
+        auto &h = con->nhoods[i];
+        out_cnt[i] = std::min<uint32_t>(h.L, cap);
+        for (unsigned j = 0; j < cap; ++j) {
+            out_ids[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].id : 0xFFFFFFFFu;
+            out_d[(uint64_t)i * cap + j] = j < h.L ? h.pool[j].dist : INFINITY;
+            out_flags[(uint64_t)i * cap + j] =
+                j < h.L ? (uint8_t)((h.pool[j].flag ? 1 : 0) | (h.pool[j].isnew ? 2 : 0)) : 0;
         }
     }
     delete con;
