@@ -53,8 +53,10 @@ kcna_status kcna_check_device_err(kcna_ctx *c, const char *phase) {
     const char *what = h == 1 ? "index outside its buffer (access skipped)"
                        : h == 2 ? "bounded wait gave up"
                        : h == 3 ? "graph row ran out of slots"
+                       : h == 4 ? "more than 1024 rows tie at the k-th distance"
                                 : "unknown";
-    return kcna_fail(c, h == 2 ? KCNA_E_TIMEOUT : KCNA_E_CUDA, std::string(phase) + ": device error: " + what);
+    const kcna_status st = h == 2 ? KCNA_E_TIMEOUT : h == 4 ? KCNA_E_LIMIT : KCNA_E_CUDA;
+    return kcna_fail(c, st, std::string(phase) + ": device error: " + what);
 }
 
 kcna_status kcna_phase_begin(kcna_ctx *c) {

@@ -143,6 +143,7 @@ enum {
     KCNA_DERR_BOUNDS = 1,   // an index fell outside its buffer
     KCNA_DERR_SPIN = 2,     // a bounded wait gave up
     KCNA_DERR_DEGREE = 3,   // a graph row ran out of slots
+    KCNA_DERR_TIES = 4,     // more rows tie at the k-th distance than the selection holds
 };
 __device__ __forceinline__ void kcna_set_err(int *err, int code) {
     if (err) atomicCAS(err, 0, code);

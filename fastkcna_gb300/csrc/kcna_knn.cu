@@ -164,7 +164,8 @@ __global__ void __launch_bounds__(SEL_T) select_kernel(const float *__restrict__
     }
     __syncthreads();
     uint32_t nless = s_nout, ntie = s_ntie;
-    if (ntie > SEL_TIES || nless >= k) kcna_set_err(err, KCNA_DERR_BOUNDS);
+    if (ntie > SEL_TIES) kcna_set_err(err, KCNA_DERR_TIES);
+    if (nless >= k) kcna_set_err(err, KCNA_DERR_BOUNDS);
     ntie = min(ntie, (uint32_t)SEL_TIES);
     nless = min(nless, k);
     int tp = kcna_pow2_ceil_d((int)ntie);
@@ -215,6 +216,7 @@ kcna_status kcna_knn_device(kcna_ctx *c, const float *dQ, uint32_t m, const uint
     uint64_t row_bytes = (uint64_t)c->n * sizeof(float);
     uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(m, (1ull << 30) / row_bytes));
     batch = std::max<uint32_t>(batch - batch % TQ, std::min<uint32_t>(batch, TQ));
+    batch = std::min<uint32_t>(batch, 65535u * TQ); // grid.y limit of the distance tiles
     void *buf = nullptr;
     KCNA_TRY(kcna_scratch(c, (uint64_t)batch * row_bytes, &buf));
     float *D = (float *)buf;

@@ -13,6 +13,7 @@
 //
 // Results are those of kcna_knn_queries: the canonical FMA-chain distance and
 // ties broken by the lower row id.
+#include <algorithm>
 #include <mutex>
 
 #include "kcna_common.cuh"
@@ -160,7 +161,8 @@ __global__ void __launch_bounds__(SEL_T) na_select_kernel(const float *__restric
     }
     __syncthreads();
     uint32_t nless = s_nout, ntie = s_ntie;
-    if (threadIdx.x == 0 && (ntie > SEL_TIES || nless >= k)) atomicCAS(err, 0, KCNA_DERR_BOUNDS);
+    if (threadIdx.x == 0 && ntie > SEL_TIES) atomicCAS(err, 0, KCNA_DERR_TIES);
+    if (threadIdx.x == 0 && nless >= k) atomicCAS(err, 0, KCNA_DERR_BOUNDS);
     ntie = min(ntie, (uint32_t)SEL_TIES);
     nless = min(nless, k);
     int tp = kcna_pow2_ceil_d((int)ntie);
@@ -221,6 +223,9 @@ extern "C" kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n,
     kcna_status st = scratch_address(dev, &base);
     if (st != KCNA_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // a runtime error left pending on this host thread by earlier work is
+    // reported, and left in place for its owner, rather than consumed here
+    if (cudaPeekAtLastError() != cudaSuccess) return KCNA_E_CUDA;
     int *err = reinterpret_cast<int *>(base);
     float *D = reinterpret_cast<float *>(base + HEADER);
     // the scratch keeps the previous call's contents: the error word must start at zero
@@ -228,7 +233,9 @@ extern "C" kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n,
         (void)cudaGetLastError();
         return KCNA_E_CUDA;
     }
-    const uint32_t batch = (uint32_t)(rows_bytes / ((uint64_t)n * sizeof(float)));
+    // rows of distances that fit the scratch, and at most 65,535 query tiles
+    // (the grid's y limit) per launch
+    const uint32_t batch = (uint32_t)std::min<uint64_t>(rows_bytes / ((uint64_t)n * sizeof(float)), 65535ull * TQ);
     const uint64_t qs = q_stride_bytes / 4, xs = base_stride_bytes / 4;
     for (uint32_t q0 = 0; q0 < m; q0 += batch) {
         const uint32_t mb = m - q0 < batch ? m - q0 : batch;
@@ -236,7 +243,10 @@ extern "C" kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n,
         na_dist_kernel<<<grid, 256, 0, s>>>(d_queries + (uint64_t)q0 * qs, mb, qs, d_base, n, xs, (int)d, D);
         na_select_kernel<<<mb, SEL_T, 0, s>>>(D, n, k, d_out_ids + (uint64_t)q0 * k, d_out_dists + (uint64_t)q0 * k,
                                               err);
-        if (cudaGetLastError() != cudaSuccess) return KCNA_E_CUDA;
+        if (cudaPeekAtLastError() != cudaSuccess) {
+            (void)cudaGetLastError(); // this call's own launch error
+            return KCNA_E_CUDA;
+        }
     }
     int h = 0;
     if (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -244,5 +254,6 @@ extern "C" kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n,
         (void)cudaGetLastError();
         return KCNA_E_CUDA;
     }
-    return h ? KCNA_E_CUDA : KCNA_OK; // h != 0: more than 1024 rows tie at the k-th distance
+    if (h == KCNA_DERR_TIES) return KCNA_E_LIMIT; // more than 1024 rows tie at the k-th distance
+    return h ? KCNA_E_CUDA : KCNA_OK;
 }

@@ -22,7 +22,7 @@ SCREEN_FP32, SCREEN_BF16 = 0, 1
 MAX_ITERS, MAX_LOOPS, NUM_PHASES = 64, 16, 12
 PHASES = ["join", "merge", "sample", "prune", "link", "p2k", "ep", "tree", "controls", "init", "other", "spare"]
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "cuda error", 4: "timeout", 5: "io error",
-          6: "bad call order"}
+          6: "bad call order", 7: "limit exceeded"}
 
 
 class KcnaError(RuntimeError):

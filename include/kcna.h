@@ -30,7 +30,9 @@ typedef enum {
     KCNA_E_CUDA = 3,    /* a CUDA call failed; maps to kgraph::runtime_error */
     KCNA_E_TIMEOUT = 4, /* a bounded device-side wait gave up (error flag set) */
     KCNA_E_IO = 5,      /* maps to kgraph::io_error (src/kgraph.h:373-376) */
-    KCNA_E_STATE = 6    /* call order violated (e.g. prune before build) */
+    KCNA_E_STATE = 6,   /* call order violated (e.g. prune before build) */
+    KCNA_E_LIMIT = 7    /* a data-dependent capacity was exceeded: more than 1024 rows
+                           tie at the k-th distance of an exact k-NN query */
 } kcna_status;
 
 /* Graph kinds.  The numbers equal the reference's PG_type column of the run CSV
@@ -267,13 +269,19 @@ void *kcna_stream(const kcna_ctx *ctx);
  * exits; queries are processed in batches of (16 MiB - 256 B) / (4 n) rows.
  * Limits (KCNA_E_ARG otherwise): n * 4 <= 16 MiB - 256 B (n <= 4,194,240),
  * 1 <= k <= min(n, 1024), d a multiple of 4, strides multiples of 16 bytes,
- * 16-byte aligned pointers.  Runs on `stream` (a cudaStream_t, NULL = the
- * legacy default stream) of the current device and synchronises it before
- * returning.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  All calls share the one array: calls whose kernels
- * overlap on the GPU (other streams, other host threads) race and must be
- * serialised by the caller.  Each call clears the array's error word itself. */
+ * 16-byte aligned pointers.  KCNA_E_LIMIT: more than 1024 base rows tie at the
+ * k-th distance of some query (a property of the data, e.g. many duplicate
+ * rows); the outputs are then unspecified and the next call starts clean.
+ * KCNA_E_CUDA: a CUDA call failed, or a runtime error was already pending on
+ * this host thread when the call began (it is left pending for its owner).
+ * Runs on `stream` (a cudaStream_t, NULL = the legacy default stream) of the
+ * current device, copies a 4-byte status word to a host stack variable and
+ * synchronises the stream (cudaStreamSynchronize) before returning.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * All calls share the one array: calls whose kernels overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Each call clears the array's error word itself. */
 #define KCNA_NOALLOC_SCRATCH_BYTES (16u << 20)
 kcna_status kcna_knn_queries_noalloc(const float *d_base, uint32_t n, uint32_t d, uint64_t base_stride_bytes,
                                      const float *d_queries, uint32_t m, uint64_t q_stride_bytes, uint32_t k,

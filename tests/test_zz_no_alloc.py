@@ -19,7 +19,7 @@ from fastkcna_gb300 import kcna, synth
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(lib, base, queries, k, stream):
+def _noalloc(lib, base, queries, k, stream, expect=0):
     import torch
 
     n, d = base.shape
@@ -32,7 +32,7 @@ def _noalloc(lib, base, queries, k, stream):
                   C.c_void_p, C.c_void_p, C.c_void_p]
     rc = f(base.data_ptr(), n, d, base.stride(0) * 4, queries.data_ptr(), m, queries.stride(0) * 4, k,
            out_i.data_ptr(), out_d.data_ptr(), stream)
-    assert rc == 0, rc
+    assert rc == expect, rc
     return out_i.cpu().numpy().view(np.uint32), out_d.cpu().numpy()
 
 
@@ -73,3 +73,23 @@ def test_noalloc_rejects_oversize():
     assert f(t.data_ptr(), 5_000_000, 16, 64, t.data_ptr(), 1, 64, 10, t.data_ptr(), t.data_ptr(), None) == 1
     assert f(t.data_ptr(), 8, 15, 64, t.data_ptr(), 1, 64, 4, t.data_ptr(), t.data_ptr(), None) == 1  # d % 4
     assert f(t.data_ptr(), 8, 16, 64, t.data_ptr(), 1, 64, 9, t.data_ptr(), t.data_ptr(), None) == 1  # k > n
+
+
+def test_noalloc_tie_overflow_status_and_recovery():
+    """More than 1024 base rows at the k-th distance is a property of the data:
+    the call reports KCNA_E_LIMIT (7), and the next call, which clears the shared
+    error word, succeeds with the same results as the allocating entry point."""
+    import torch
+
+    lib = kcna.load_library()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    X = np.ones((1100, 16), np.float32)  # 1,100 identical rows: every distance ties
+    _noalloc(lib, torch.from_numpy(X).to(dev), torch.from_numpy(X[:2].copy()).to(dev), 4, stream, expect=7)
+    Y = synth.base("c1", 3000)
+    Yq = synth.queries("c1", 20)
+    with kcna.Index(0) as ix:
+        ix.upload(Y)
+        ref_i, ref_d = ix.knn_queries(Yq, 8)
+    got_i, got_d = _noalloc(lib, torch.from_numpy(Y).to(dev), torch.from_numpy(Yq).to(dev), 8, stream)
+    assert np.array_equal(got_i, ref_i) and np.array_equal(got_d, ref_d)
