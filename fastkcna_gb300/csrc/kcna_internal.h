@@ -77,6 +77,8 @@ struct kcna_ctx {
 
     // controls (exact MAXL-NN of sampled nodes) for the recall estimate
     std::vector<uint32_t> control_ids;
+    std::vector<uint32_t> control_cache; // the reference's control order for control_cache_n rows
+    uint32_t control_cache_n = 0;
     uint32_t *d_controls = nullptr, *d_control_knn = nullptr;
     uint32_t control_k = 0;
 

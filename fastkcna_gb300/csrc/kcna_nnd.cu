@@ -25,6 +25,8 @@
 // candidates at its end.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <random>
 
 #include "kcna_internal.h"
@@ -1147,19 +1149,33 @@ kcna_status kcna_pools_set_radius(kcna_ctx *c, uint32_t limit) {
 }
 
 // Controls: C random nodes and their exact MAXL-NN (GenerateControl,
-// src/kgraph.cpp:363-387); nodes drawn with mt19937(seed).
+// src/kgraph.cpp:363-387).  The nodes are the reference's own: the first C of
+// 0..n-1 after std::random_shuffle driven by the C library's rand() in its
+// initial state (the reference never seeds it), i.e. for i = 1..n-1 swap
+// index[i] with index[rand() % (i + 1)].  The same generator runs here on a
+// private state (random_r seeded with 1, the state rand() starts from), so
+// the caller's rand() sequence is left alone; the order is cached per (n, C).
 kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     uint32_t C = std::min<uint32_t>(p->controls, c->n - 1);
     c->control_ids.clear();
     if (C == 0) return KCNA_OK;
-    std::vector<uint32_t> idx(c->n);
-    for (uint32_t i = 0; i < c->n; ++i) idx[i] = i;
-    std::mt19937 rng(p->seed);
-    for (uint32_t i = 0; i < C; ++i) {
-        uint32_t j = i + rng() % (c->n - i);
-        std::swap(idx[i], idx[j]);
+    if (c->control_cache_n != c->n || c->control_cache.size() != C) {
+        std::vector<uint32_t> idx(c->n);
+        for (uint32_t i = 0; i < c->n; ++i) idx[i] = i;
+        struct random_data rd;
+        char state[128];
+        std::memset(&rd, 0, sizeof rd);
+        std::memset(state, 0, sizeof state);
+        if (initstate_r(1u, state, sizeof state, &rd) != 0) return kcna_fail(c, KCNA_E_CUDA, "initstate_r failed");
+        for (uint32_t i = 1; i < c->n; ++i) {
+            int32_t r = 0;
+            random_r(&rd, &r);
+            std::swap(idx[i], idx[(uint32_t)r % (i + 1)]);
+        }
+        c->control_cache.assign(idx.begin(), idx.begin() + C);
+        c->control_cache_n = c->n;
     }
-    c->control_ids.assign(idx.begin(), idx.begin() + C);
+    c->control_ids = c->control_cache;
     c->control_k = maxl;
     KCNA_TRY(kcna_alloc(c, &c->d_controls, C, "controls"));
     KCNA_TRY(kcna_alloc(c, &c->d_control_knn, (size_t)C * maxl, "control knn"));
