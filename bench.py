@@ -15,10 +15,11 @@ prune + link, entry point, tree_grow, P2K refinement).
   e2e    the same build through the C ABI with host buffers: every step copies
          the rows from pinned host memory, builds, and reads the graph back.
 
---impl reference times the reference's CPU build of the same workload on the
-host cores (the reference compiled from its sources when that library loads
-on this machine, else the oracle port), on a bounded sample of N rows,
-reported in the same unit (seconds scaled linearly to 1M rows).
+--impl reference times the reference's own CPU build of the same workload on
+this machine's host cores: the reference compiled from its sources for this
+machine (oracle/build_ref.sh), whole 1M-row buildFastNSG runs through its
+public API, as many as fit --ref-budget seconds, each timed by the
+reference's own CSV "con time".  The GPU arm's cpu_baseline is one such build.
 """
 from __future__ import annotations
 
@@ -40,6 +41,12 @@ METRIC = "1M×128 graph build s @0.99 KNN recall: learned+BF16 vs plain FP32 (1 
 UNIT = "s"
 FLAGS = dict(K=500, L=500, S=12, R=100, iterations=12, search_L=80, nsg_R=50, search_K=500, massq_S=10,
              loop_i=2, step=10, angle=60.0, recall=0.99, controls=100, seed=2024)
+
+
+def static_config(n):
+    """The workload, identical in the GPU arm and the reference arm."""
+    return {"workload": "c2 FastNSG 1M x 128 (integer-valued 256-cluster mixture)", "n": n,
+            "l2_policy": "inputs larger than L2 (rows 512 MB, pools 4 GB)", **FLAGS}
 
 
 def peaks():
@@ -135,28 +142,44 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
-def cpu_build_seconds(n_sample: int, threads: int, prefer_reference: bool):
-    """One CPU build of an n_sample-row sample; returns (seconds, kind, recall)."""
+def _reference_lib():
+    """The reference compiled from its own sources for this machine
+    (oracle/build_ref.sh, run by build()), or None with the reason."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
-    from fastkcna_gb300 import synth
 
-    X = synth.base("c2", n_sample)
+    if not oracle_py.Reference.available():
+        return None, "oracle/_ref/libkcna_ref.so is absent (the reference sources were not staged here)"
+    try:
+        return oracle_py.Reference(), None
+    except OSError as e:  # built for another architecture
+        return None, f"oracle/_ref/libkcna_ref.so does not load here: {e}"
+
+
+def reference_builds(X, threads, budget_s, max_builds):
+    """Whole FastNSG builds of X by the reference (buildFastNSG through its
+    public API, src/kgraph.cpp:3796-3851), as many as fit budget_s (at least
+    one, at most max_builds).  Each build's time is the reference's own CSV
+    "con time" (last entry: from the start of buildFastNSG to the end of the
+    last buildNSG, src/kgraph.cpp:3797,3823-3826).  Returns (builds, graph of
+    the last build, kind, note); without a loadable reference the oracle port
+    builds instead (kind "port", its own wall time)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    ref, why = _reference_lib()
     p = oracle_py.params(**{**FLAGS, "nthreads": threads})
-    if prefer_reference and oracle_py.Reference.available():
-        try:
-            ref = oracle_py.Reference()
-        except OSError:
-            ref = None  # the library was built for another architecture
+    builds, graph = [], None
+    t_all = time.perf_counter()
+    while len(builds) < max(1, max_builds):
+        t0 = time.perf_counter()
         if ref is not None:
             sys.stdout.flush()
             saved = os.dup(1)  # the reference prints progress with printf
             devnull = os.open(os.devnull, os.O_WRONLY)
             os.dup2(devnull, 1)
             try:
-                t = time.perf_counter()
-                ref.build(oracle_py.KCNA_NSG, X, p, nthreads=threads)
-                dt = time.perf_counter() - t
+                rows, ep, width, csv = ref.build(oracle_py.KCNA_NSG, X, p, nthreads=threads)
             finally:
                 import ctypes
 
@@ -164,36 +187,106 @@ def cpu_build_seconds(n_sample: int, threads: int, prefer_reference: bool):
                 os.dup2(saved, 1)
                 os.close(saved)
                 os.close(devnull)
-            return dt, "reference", None
-    O = oracle_py.Oracle()
-    t = time.perf_counter()
-    _, _, st = O.build(oracle_py.KCNA_NSG, X, p, width=64, nthreads=threads)
-    return time.perf_counter() - t, "port", float(st.loop_recall[max(st.loops - 1, 0)])
+            wall = time.perf_counter() - t0
+            r = oracle_py.parse_run_csv(csv)
+            con = r.get("con time", [])
+            builds.append(dict(seconds=con[-1] if con else wall, wall=wall, recall=r.get("recall", []),
+                               con_time=con, aod=(r.get("AOD") or [None])[0]))
+            graph = (rows, ep, width)
+        else:
+            O = oracle_py.Oracle()
+            gi, deg, st = O.build(oracle_py.KCNA_NSG, X, p, width=2 * FLAGS["nsg_R"] + 64, nthreads=threads)
+            wall = time.perf_counter() - t0
+            rec = list(st.iter_recall[: st.iterations]) + list(st.loop_recall[1: st.loops])
+            builds.append(dict(seconds=wall, wall=wall, recall=rec, con_time=[], aod=int(st.aod)))
+            graph = ([gi[i, : deg[i]] for i in range(gi.shape[0])], int(st.ep), int(st.width))
+        elapsed = time.perf_counter() - t_all
+        if elapsed + builds[-1]["wall"] > budget_s:
+            break
+    kind = "reference" if ref is not None else "port"
+    return builds, graph, kind, why
+
+
+def exact_knn_host(X, Q, k, chunk=256):
+    """Exact k-NN of Q in X on the host (numpy), ties broken by the lower id.
+    Squared L2 from |x|^2 + |q|^2 - 2<x, q> in float64."""
+    X64 = X.astype(np.float64)
+    xn = (X64 * X64).sum(1)
+    out = np.empty((Q.shape[0], k), np.int64)
+    for s in range(0, Q.shape[0], chunk):
+        q = Q[s: s + chunk].astype(np.float64)
+        d = xn[None, :] + (q * q).sum(1)[:, None] - 2.0 * (q @ X64.T)
+        part = np.argpartition(d, k, axis=1)[:, : k + 1]
+        for i in range(q.shape[0]):
+            c = part[i]
+            o = np.lexsort((c, d[i, c]))[:k]
+            out[s + i] = c[o]
+    return out
+
+
+def reference_search_recall10(X, graph, Q, truth, L=100):
+    """Search recall@10 of the reference's own graph with the reference's own
+    beam search (get_neighbors, src/kgraph.cpp:1560-1623), started from the
+    entry point + L-1 seeded random nodes as in the GPU arm's measurement."""
+    rows, ep, width = graph
+    n = X.shape[0]
+    W = max(1, max(len(r) for r in rows))
+    g = np.full((n, W), 0xFFFFFFFF, np.uint32)
+    deg = np.zeros(n, np.uint32)
+    for i, r in enumerate(rows):
+        g[i, : len(r)] = r
+        deg[i] = len(r)
+    rng = np.random.default_rng(7)
+    extra = rng.choice(n, size=L, replace=False)
+    start = np.concatenate([[ep], extra[extra != ep][: L - 1]]).astype(np.uint32)
+    init = np.broadcast_to(start, (Q.shape[0], L)).copy()
+    ref, _ = _reference_lib()
+    if ref is None:
+        return None
+    found, _ = ref.beam_search(X, g, deg, Q, init, L, 10)
+    hit = sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth))
+    return hit / (10.0 * Q.shape[0])
 
 
 def run_reference(args, ws, rank):
+    """The reference's own CPU build of the same workload on this machine's host
+    cores: whole builds of the named size, as many as fit --ref-budget seconds."""
     if rank != 0:
         return
+    from fastkcna_gb300 import synth
+
     threads = os.cpu_count() or 1
-    n = args.cpu_n
-    scale = 1_000_000 / n
-    for _ in range(args.warmup):
-        cpu_build_seconds(n, threads, True)
-    times, kind = [], None
-    for _ in range(args.steps):
-        t, kind, rec = cpu_build_seconds(n, threads, True)
-        times.append(t * scale)
-    v = statistics.median(times)
-    sample = (f"FastNSG build of a {n:,}-row sample of the 1M x 128 workload (same flags), "
-              f"{threads} host threads, seconds x {scale:g} (linear in N)")
+    X = synth.base("c2", args.n)
+    builds, graph, kind, why = reference_builds(X, threads, args.ref_budget, args.steps)
+    v = statistics.median(b["seconds"] for b in builds)
+    Q = synth.queries("c2", 10000)
+    truth = exact_knn_host(X, Q, 10)
+    rec10 = reference_search_recall10(X, graph, Q, truth) if kind == "reference" else None
+    sample = (f"{len(builds)} whole FastNSG build(s) of the {args.n:,}-row workload (same flags), "
+              f"{threads} host threads, seconds from the reference's CSV con time")
+    if kind == "port":
+        sample = f"oracle port (the reference does not load here: {why}); " + sample.replace(
+            "seconds from the reference's CSV con time", "wall seconds")
+    last = builds[-1]
     print(json.dumps({
-        "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(v * 1000, 1), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c2 FastNSG 1M x 128 (CPU sample)", "n_sample": n, **FLAGS},
-        "impl": "reference",
-        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
-        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": ws, "steps": len(builds),
+        "warmup": 0, "ms_per_step": round(v * 1000, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": static_config(args.n),
+        "impl": "reference", "mode": f"reference CPU build ({kind})",
+        "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "results": {"build_seconds": [round(b["seconds"], 3) for b in builds],
+                    "build_wall_seconds": [round(b["wall"], 3) for b in builds],
+                    "con_time": [round(x, 3) for x in last["con_time"]],
+                    "recall_per_iteration_and_loop": [round(x, 5) for x in last["recall"]],
+                    "knn_recall_at_K": round(last["recall"][-1], 5) if last["recall"] else None,
+                    "avg_degree": last["aod"],
+                    "search_recall_at_10": round(rec10, 4) if rec10 is not None else None,
+                    "search": "10,000 queries, the reference's own beam search (get_neighbors), beam 100 from the "
+                              "entry point + 99 seeded random nodes, exact 10-NN",
+                    "host": {"machine": os.uname().machine, "threads": threads},
+                    "warmup_note": "no warm-up build: one build takes minutes and its first-touch of memory is "
+                                   "part of the reference's own build"},
     }), flush=True)
 
 
@@ -219,20 +312,9 @@ def roofline(st, hbm_gbs, ld, n, search_k):
     per_launch_s = ms / 1000.0 / nl
     achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     return name, {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
-                  "frac": round(achieved / hbm_gbs, 4), "traffic": traffic_from_profile(kernels[name]),
+                  "frac": round(achieved / hbm_gbs, 4), "traffic": None,
+                  "traffic_note": "DRAM bytes are not measured by this run (ncu captures are separate)",
                   "kernel": kernels[name], "phase": name, "launches_per_step": int(nl)}
-
-
-def traffic_from_profile(name):
-    """DRAM bytes per launch from the committed ncu summary, when present."""
-    path = os.path.join(ROOT, "profiles", f"{name}_c2.txt")
-    try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full_size:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
 
 
 def search_recall10(ix, Q, truth, n, L=100):
@@ -381,38 +463,38 @@ def run_gpu(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": round(ms / 1000.0, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c2 FastNSG 1M x 128 (integer-valued 256-cluster mixture)", "n": n,
-                   "mode": "learned seed + BF16" if args.mode == "learned_bf16" else "plain FP32",
-                   "l2_policy": "inputs larger than L2 (rows 512 MB, pools 4 GB)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU", **FLAGS,
-                   "knn_recall_at_K": round(final_recall, 4),
-                   "nndescent_iterations": st["iterations"],
-                   "nndescent_recall": [round(x, 4) for x in st["iter_recall"]],
-                   "phase_ms": {k: round(v, 2) for k, v in st["phase_ms"].items() if v},
-                   "dist_evals_per_s": round((st["n_comps"] + st["prune_comps"] + st["bridge_comps"]) / (ms / 1000.0)),
-                   "cand_overflow": sum(st["iter_cand_overflow"]), "cand_emitted": st["cand_emitted"],
-                   "cand_merged": st["cand_merged"], "tree_attached": st["tree_attached"],
-                   "avg_degree": st["aod"],
-                   "iter_join_ms": [round(x, 1) for x in st["iter_join_ms"]],
-                   "iter_merge_ms": [round(x, 1) for x in st["iter_merge_ms"]],
-                   "iter_cand_M": [round(x / 1e6, 1) for x in st["iter_cand"]],
-                   "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]],
-                   "bf16_rows": st["bf16_rows"], "seed_ms": round(st["seed_total_ms"], 1),
-                   "seed_train_ms": round(st["seed_train_ms"], 1),
-                   "seed_recall": round(st["seed_recall"], 4),
-                   "plain_fp32_s": round(plain_ms / 1000.0, 4) if plain_ms else None,
-                   "plain_fp32_knn_recall_at_K": round(plain_stats[-1]["loop_recall"][-1], 4) if plain_ms else None,
-                   "plain_fp32_nndescent_iterations": plain_stats[-1]["iterations"] if plain_ms else None,
-                   "plain_fp32_nndescent_recall": [round(x, 4) for x in plain_stats[-1]["iter_recall"]] if plain_ms else None,
-                   "plain_fp32_phase_ms": {k: round(v, 2) for k, v in plain_stats[-1]["phase_ms"].items() if v}
-                   if plain_ms else None,
-                   "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None,
-                   "search_recall_at_10": round(rec10, 4),
-                   "plain_fp32_search_recall_at_10": round(plain_rec10, 4) if plain_rec10 is not None else None,
-                   "search_qps": round(qps),
-                   "plain_fp32_search_qps": round(plain_qps) if plain_ms else None,
-                   "search": "10,000 queries, beam 100 from the entry point + 99 seeded random nodes, exact 10-NN"},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": static_config(n),
+        "mode": "learned seed + BF16" if args.mode == "learned_bf16" else "plain FP32",
+        "parallelism": "replicas" if ws > 1 else "single GPU",
+        "results": {"knn_recall_at_K": round(final_recall, 4),
+                    "nndescent_iterations": st["iterations"],
+                    "nndescent_recall": [round(x, 4) for x in st["iter_recall"]],
+                    "loop_recall": [round(x, 4) for x in st["loop_recall"]],
+                    "phase_ms": {k: round(v, 2) for k, v in st["phase_ms"].items() if v},
+                    "dist_evals_per_s": round((st["n_comps"] + st["prune_comps"] + st["bridge_comps"]) / (ms / 1000.0)),
+                    "cand_overflow": sum(st["iter_cand_overflow"]), "cand_emitted": st["cand_emitted"],
+                    "cand_merged": st["cand_merged"], "tree_attached": st["tree_attached"],
+                    "avg_degree": st["aod"],
+                    "iter_join_ms": [round(x, 1) for x in st["iter_join_ms"]],
+                    "iter_merge_ms": [round(x, 1) for x in st["iter_merge_ms"]],
+                    "iter_cand_M": [round(x / 1e6, 1) for x in st["iter_cand"]],
+                    "iter_inserted_M": [round(x / 1e6, 1) for x in st["iter_inserted"]],
+                    "iter_cand_overflow_M": [round(x / 1e6, 1) for x in st["iter_cand_overflow"]],
+                    "bf16_rows": st["bf16_rows"], "seed_ms": round(st["seed_total_ms"], 1),
+                    "seed_train_ms": round(st["seed_train_ms"], 1),
+                    "seed_recall": round(st["seed_recall"], 4),
+                    "plain_fp32_s": round(plain_ms / 1000.0, 4) if plain_ms else None,
+                    "plain_fp32_knn_recall_at_K": round(plain_stats[-1]["loop_recall"][-1], 4) if plain_ms else None,
+                    "plain_fp32_nndescent_iterations": plain_stats[-1]["iterations"] if plain_ms else None,
+                    "plain_fp32_nndescent_recall": [round(x, 4) for x in plain_stats[-1]["iter_recall"]] if plain_ms else None,
+                    "plain_fp32_phase_ms": {k: round(v, 2) for k, v in plain_stats[-1]["phase_ms"].items() if v}
+                    if plain_ms else None,
+                    "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None,
+                    "search_recall_at_10": round(rec10, 4),
+                    "plain_fp32_search_recall_at_10": round(plain_rec10, 4) if plain_rec10 is not None else None,
+                    "search_qps": round(qps),
+                    "plain_fp32_search_qps": round(plain_qps) if plain_ms else None,
+                    "search": "10,000 queries, beam 100 from the entry point + 99 seeded random nodes, exact 10-NN"},
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
                 "d2h_bytes_per_step": int(n * W * 4 + n * 4 + 8)},
@@ -421,11 +503,14 @@ def run_gpu(args, ws, rank, local):
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        t, kind, rec = cpu_build_seconds(args.cpu_n, threads, True)
-        scale = 1_000_000 / args.cpu_n
-        line["cpu_baseline"] = {"value": round(t * scale, 3), "unit": UNIT, "cores": threads, "kind": kind,
-                                "sample": f"one FastNSG build of a {args.cpu_n:,}-row sample of the workload, "
-                                          f"same flags, {t:.2f} s x {scale:g} (linear in N)"}
+        builds, _, kind, why = reference_builds(X, threads, 0.0, 1)
+        b = builds[0]
+        line["cpu_baseline"] = {
+            "value": round(b["seconds"], 3), "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": ("one whole FastNSG build of the same 1M-row workload and flags by the reference compiled "
+                       "from its sources for this host, seconds from its CSV con time" if kind == "reference" else
+                       f"one whole FastNSG build of the same 1M-row workload by the oracle port ({why}), wall seconds"),
+            "knn_recall_at_K": round(b["recall"][-1], 5) if b["recall"] else None}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ix.close()
@@ -438,7 +523,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--cpu-n", type=int, default=50_000)
+    ap.add_argument("--ref-budget", type=float, default=1200.0,
+                    help="seconds of whole reference builds in --impl reference (at least one build)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="learned_bf16", choices=["learned_bf16", "plain"])
     ap.add_argument("--search-sweep", action="store_true",

@@ -115,14 +115,21 @@ def test_oracle_nndescent_recall_tracks_reference(oracle):
 
 
 def test_bench_reference_arm_prints_one_json_line():
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--cpu-n", "3000"], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "3",
+                        "--warmup", "0", "--n", "3000", "--ref-budget", "0"], capture_output=True, text=True,
+                       timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
     j = json.loads(lines[0])
     assert j["impl"] == "reference" and j["unit"] == "s" and j["higher_is_better"] is False
     assert j["cpu_baseline"]["kind"] in ("reference", "port") and j["e2e"]["h2d_bytes_per_step"] == 0
+    # whole builds of the named size, as many as the budget allows (here one): no extrapolation
+    assert j["steps"] == 1 == len(j["results"]["build_seconds"]) and j["config"]["n"] == 3000
+    assert j["value"] == j["cpu_baseline"]["value"] == j["e2e"]["value"]
+    import bench
+
+    assert j["config"] == bench.static_config(3000)  # the GPU arm prints the same config
 
 
 def _rank_main(rank, world, port, q):
