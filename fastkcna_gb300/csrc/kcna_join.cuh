@@ -22,6 +22,7 @@ struct JoinArgs {
     const float *radius;
     uint64_t *cand;
     uint32_t *cand_cnt;
+    uint32_t *cand_src; // the joiner of each candidate, beside its key (found credit in the merge)
     uint32_t CB;
     uint8_t *found;
     unsigned long long *counters; // [0] pairs evaluated, [5] rows gathered, [6] candidates emitted

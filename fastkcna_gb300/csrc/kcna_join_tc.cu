@@ -28,7 +28,7 @@
 // hand work to each other through mbarriers:
 //   warp 0      packer: walks the block's range of nodes, copies row and
 //               column ids into a tile stage (cp.async), marks each packed
-//               node's found flag 0, then the radius and norm of every row and
+//               node's found flag 0 (the merge credits it), then the radius and norm of every row and
 //               column (cp.async); two stages;
 //   warps 18-21 row loaders: the rows' and columns' BF16 rows by 16-byte
 //               cp.async into the stage in the 128-byte swizzled K-major layout
@@ -39,8 +39,9 @@
 //               fourth 16-column group of the span its rows cover; a count
 //               pass (row and column emissions, column masks by ballots), one
 //               atomicAdd per row and per column to reserve the runs in the
-//               targets' candidate buffers, a write pass reading TMEM again;
-//               a row that emits sets its node's found flag.
+//               targets' candidate buffers, a write pass reading TMEM again
+//               that stores every candidate's key and its joiner (the tile
+//               row's node) for the merge's found credit.
 // Every wait is bounded; a wait that gives up stops the block, sets the error
 // word and lets in-flight copies and products finish before TMEM is released.
 #include <algorithm>
@@ -366,7 +367,6 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
             // count pass: the row's emissions as bits, the columns' as ballots
             uint64_t rmask = 0;
             uint32_t cm[GPW] = {0u, 0u, 0u, 0u}; // lane x: rows emitting into column 16 g_k + x
-            bool any_c = false;                  // this row emits into some column's buffer
 #pragma unroll
             for (int k = 0; k < GPW; ++k) {
                 const int g = gl + h + 4 * k;
@@ -383,7 +383,6 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                         pair_rule<SCREEN>(M, i, __uint_as_float(raw[x]), id_j, rad_j, n_j, rr_j, aa_j, rp, cp, dd);
                     }
                     rmask |= (uint64_t)rp << (16 * k + x);
-                    any_c |= cp;
                     const unsigned m = __ballot_sync(KCNA_FULL, cp);
                     if (lane == x) cm[k] = m;
                 }
@@ -404,10 +403,11 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                     nct += __popc(cm[k]);
                 }
             }
-            if (nr > 0 || any_c) a.found[M.row_node[r]] = 1;
             emitted += (unsigned long long)(nr + nct);
             if (__any_sync(KCNA_FULL, nr > 0 || nct > 0)) { // write pass; the distances are read again from TMEM
                 uint64_t *dst = a.cand + (uint64_t)id_j * a.CB;
+                uint32_t *dsrc = a.cand_src + (uint64_t)id_j * a.CB;
+                const uint32_t joiner = rowv ? M.row_node[r] : 0u; // the node whose join made this tile row
 #pragma unroll
                 for (int k = 0; k < GPW; ++k) {
                     const int g = gl + h + 4 * k;
@@ -428,12 +428,18 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                             const float dd = fmaxf(
                                 __fsub_rn(__fadd_rn(n_j, M.col_nrm[i]), 2.f * __uint_as_float(raw[x])), 0.f);
                             if ((gm >> x) & 1u) {
-                                if (p < a.CB) dst[p] = kcna_key(dd, M.col_id[i], flags);
+                                if (p < a.CB) {
+                                    dst[p] = kcna_key(dd, M.col_id[i], flags);
+                                    dsrc[p] = joiner;
+                                }
                                 ++p;
                             }
                             if ((m >> lane) & 1u) {
                                 const uint32_t pc = cbx + __popc(m & kcna_lanemask_lt());
-                                if (pc < a.CB) a.cand[(uint64_t)M.col_id[i] * a.CB + pc] = kcna_key(dd, id_j, flags);
+                                if (pc < a.CB) {
+                                    a.cand[(uint64_t)M.col_id[i] * a.CB + pc] = kcna_key(dd, id_j, flags);
+                                    a.cand_src[(uint64_t)M.col_id[i] * a.CB + pc] = joiner;
+                                }
                             }
                         }
                     }

@@ -117,8 +117,7 @@ constexpr int JKP = JKC + 4; // padded row pitch in shared memory
 
 template <int RI, class R> // rows per thread = RI, tile rows = 32 * RI
 __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, const uint32_t *s_A, int na, const uint32_t *s_B, int nb,
-                           float *s_As, float *s_Bs, float *s_D, const float *s_radA, int *s_any,
-                           unsigned *s_emit) {
+                           float *s_As, float *s_Bs, float *s_D, const float *s_radA, unsigned *s_emit) {
     constexpr int RA = 32 * RI;
     const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3; // 8 col groups x 32 row groups
     const int ncol = na + nb;
@@ -200,18 +199,22 @@ __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, cons
             if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
             base = __shfl_sync(KCNA_FULL, base, 0);
             uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
+            uint32_t *dsrc = a.cand_src + (uint64_t)tgt * a.CB;
             if (ok[0]) {
                 uint32_t p = base + __popc(m0 & kcna_lanemask_lt());
-                if (p < a.CB) dst[p] = keys[0];
+                if (p < a.CB) {
+                    dst[p] = keys[0];
+                    dsrc[p] = node;
+                }
             }
             if (ok[1]) {
                 uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
-                if (p < a.CB) dst[p] = keys[1];
+                if (p < a.CB) {
+                    dst[p] = keys[1];
+                    dsrc[p] = node;
+                }
             }
-            if (lane == 0) {
-                *s_any = 1;
-                atomicAdd(s_emit, (unsigned)cnt);
-            }
+            if (lane == 0) atomicAdd(s_emit, (unsigned)cnt);
         }
         // column targets: column id receives row ids
         for (int cl = warp; cl < cend; cl += nwarp) {
@@ -241,19 +244,20 @@ __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, cons
             if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
             base = __shfl_sync(KCNA_FULL, base, 0);
             uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
+            uint32_t *dsrc = a.cand_src + (uint64_t)tgt * a.CB;
             uint32_t run = base;
 #pragma unroll
             for (int h = 0; h < RI; ++h) {
                 if (mk[h] & (1u << lane)) {
                     uint32_t p = run + __popc(mk[h] & kcna_lanemask_lt());
-                    if (p < a.CB) dst[p] = keys[h];
+                    if (p < a.CB) {
+                        dst[p] = keys[h];
+                        dsrc[p] = node;
+                    }
                 }
                 run += __popc(mk[h]);
             }
-            if (lane == 0) {
-                *s_any = 1;
-                atomicAdd(s_emit, (unsigned)cnt);
-            }
+            if (lane == 0) atomicAdd(s_emit, (unsigned)cnt);
         }
         __syncthreads();
     }
@@ -268,10 +272,8 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
     float *s_radA = s_D + 128 * (JCOLS + 1);                      // capA
     uint32_t *s_A = reinterpret_cast<uint32_t *>(s_radA + a.capA); // capA
     uint32_t *s_B = s_A + a.capA;                                 // capB
-    __shared__ int s_any;
     __shared__ unsigned s_emit;
     const uint32_t node = blockIdx.x;
-    if (threadIdx.x == 0) s_any = 0;
     // new list: forward new then a random subset (<= R) of reverse new
     uint32_t fn = min(a.fwd_new_cnt[node], a.fwd_new_cap);
     for (uint32_t i = threadIdx.x; i < fn; i += blockDim.x) s_A[i] = a.fwd_new[(uint64_t)node * a.fwd_new_cap + i];
@@ -295,15 +297,12 @@ __global__ void __launch_bounds__(JT, 3) join_kernel(JoinArgs a, R rows) {
         s_emit = 0;
     }
     if (na <= 32)
-        join_tiles<1>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+        join_tiles<1>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_emit);
     else if (na <= 64)
-        join_tiles<2>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
+        join_tiles<2>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_emit);
     else
-        join_tiles<4>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_any, &s_emit);
-    if (threadIdx.x == 0) {
-        a.found[node] = s_any ? 1 : 0;
-        if (s_emit) atomicAdd(a.counters + 6, (unsigned long long)s_emit);
-    }
+        join_tiles<4>(a, rows, node, s_A, na, s_B, nb, s_As, s_Bs, s_D, s_radA, &s_emit);
+    if (threadIdx.x == 0 && s_emit) atomicAdd(a.counters + 6, (unsigned long long)s_emit);
 }
 
 // ---------------------------------------------------------------------------
@@ -320,6 +319,15 @@ struct MergeArgs {
     uint32_t *cand_cnt;
     uint32_t CB;
     unsigned long long *counters; // [1] flagged in top-K, [2] overflow, [3] inserted
+    // found credit (NN-descent merges): the joiner of every candidate, and the
+    // flags the merge sets.  A distinct candidate inserted at rank < K credits
+    // the lowest joiner id that emitted it: the reference's join credits the
+    // joiner whose parallel_try_insert landed the entry below K
+    // (src/kgraph.cpp:1107-1112), which in its increasing-node parallel loop is
+    // in practice the first joiner to reach the pair.
+    const uint32_t *cand_src;
+    uint8_t *found;
+    uint32_t n_nodes;
 };
 
 // Warp-per-node merge, survivors first.  Every candidate is looked up in the
@@ -334,12 +342,18 @@ struct MergeArgs {
 // SURV is 512, or 1024 while the previous merge queued more than n/32 nodes
 // (the first iterations, when the pools are filling): twice the shared memory
 // per warp and fewer warps per SM, but fewer nodes left to the block merge.
+// With CREDIT (NN-descent merges) the joiners are credited after the pool is
+// written: survivors placed at rank < K are marked (bit 0 of their key in
+// s_sv), the pool copy in shared memory is then reused as one u32 per marked
+// survivor, a pass over the node's candidates takes the lowest joiner
+// (atomicMin) of every candidate equal to a marked survivor, and those
+// joiners' found flags are set.
 constexpr int MW_WARPS = 8;
 __host__ __device__ constexpr size_t merge_warp_bytes(uint32_t cap, int surv) {
     return ((size_t)cap * 8 + (size_t)surv * 8 + 16 + 15) & ~(size_t)15;
 }
 
-template <int SURV>
+template <int SURV, bool CREDIT>
 __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, uint32_t N, uint32_t *big_list,
                                                                   uint32_t *big_cnt) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -349,6 +363,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
     uint64_t *s_pool = reinterpret_cast<uint64_t *>(base);
     uint64_t *s_sv = s_pool + a.cap;         // survivors (keys without flags)
     uint64_t *s_last = s_sv + SURV;          // key landing at rank limit-1
+    uint32_t *s_min = reinterpret_cast<uint32_t *>(s_pool); // CREDIT, after the pool is written
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
     if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
     __syncthreads();
@@ -438,20 +453,51 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 }
             }
             // survivors at their rank
+            unsigned long long placed = 0;
+            bool credit = false;
             for (uint32_t j = lane; j < nu; j += 32) {
                 const uint64_t k = s_sv[j];
                 const uint32_t r = j + (uint32_t)kcna_lower_bound(s_pool, (int)np, k);
                 if (r < newcnt) {
                     gp[r] = k | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
-                    if (r < a.K) ++flagged;
+                    ++placed;
+                    if (r < a.K) {
+                        ++flagged;
+                        credit = true;
+                    }
                     if (r + 1 == a.limit) *s_last = k;
                 }
             }
             flagged = kcna_warp_sum(flagged);
+            placed = kcna_warp_sum(placed);
+            if (CREDIT && __any_sync(KCNA_FULL, credit)) {
+                // survivors u < K (rank u + lower bound >= u) can be credited:
+                // mark those placed below K, then reuse the pool copy for their joiners
+                const uint32_t nk = min(nu, a.K);
+                __syncwarp();
+                for (uint32_t j = lane; j < nk; j += 32) {
+                    const uint64_t k = s_sv[j];
+                    if (j + (uint32_t)kcna_lower_bound(s_pool, (int)np, k) < a.K) s_sv[j] = k | 1ull;
+                }
+                __syncwarp();
+                for (uint32_t j = lane; j < nk; j += 32) s_min[j] = KCNA_NONE;
+                __syncwarp();
+                const uint32_t *gsrc = a.cand_src + (uint64_t)node * a.CB;
+                for (uint32_t j = lane; j < nc; j += 32) {
+                    const uint64_t k = kcna_key_noflags(gc[j]);
+                    if (k == KCNA_EMPTY_KEY_NOFLAGS) continue;
+                    const int u = kcna_lower_bound(s_sv, (int)nk, k); // a marked twin k | 1 sorts right after k
+                    if ((uint32_t)u < nk && (s_sv[u] & 1ull) && (s_sv[u] >> 2) == (k >> 2))
+                        atomicMin(&s_min[u], gsrc[j]);
+                }
+                __syncwarp();
+                for (uint32_t j = lane; j < nk; j += 32)
+                    if (s_min[j] < a.n_nodes) a.found[s_min[j]] = 1;
+            }
             __syncwarp();
             if (lane == 0) {
                 if (flagged) atomicAdd(&s_stat[0], flagged);
-                atomicAdd(&s_stat[1], (unsigned long long)(newcnt - min(np, newcnt)));
+                if (placed) atomicAdd(&s_stat[1], placed);
                 atomicAdd(&s_stat[2], (unsigned long long)nc);
                 atomicAdd(&s_stat[3], (unsigned long long)newcnt);
                 if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
@@ -523,11 +569,13 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
     uint64_t *s_pool = reinterpret_cast<uint64_t *>(smem); // cap
     uint64_t *s_c = s_pool + a.cap;                        // cbp (candidate keys, then bitonic scratch)
     uint64_t *s_sorted = s_c + cbp;                        // cbp
-    uint32_t *s_b = reinterpret_cast<uint32_t *>(s_sorted + cbp); // cbp  bucket per candidate
-    uint32_t *s_kept = s_b + cbp;                          // cbp + 1
-    uint32_t *s_hist = s_kept + cbp + 1;                   // cap + 2
+    uint32_t *s_b = reinterpret_cast<uint32_t *>(s_sorted + cbp); // cbp  bucket per candidate, then scratch
+    uint32_t *s_ss = s_b + cbp;                            // cbp  joiner of each sorted candidate (credit)
+    uint32_t *s_hist = s_ss + cbp;                         // cap + 2
     uint32_t *s_off = s_hist + a.cap + 2;                  // cap + 2
     uint32_t *s_giant = s_off + a.cap + 2;                 // cap + 2
+    uint32_t *s_kept = reinterpret_cast<uint32_t *>(s_c);  // cbp + 1, once s_c's sorting is done
+    const bool credit = a.cand_src != nullptr;
     __shared__ uint32_t s_warp[MT / 32];
     __shared__ uint32_t s_ngiant;
     __shared__ unsigned long long s_flagged;
@@ -584,10 +632,14 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < nc; j += MT) {
             const uint32_t b = s_b[j];
-            if (b != KCNA_NONE) s_sorted[s_off[b] + atomicAdd(&s_hist[b], 1u)] = s_c[j];
+            if (b != KCNA_NONE) {
+                const uint32_t q = s_off[b] + atomicAdd(&s_hist[b], 1u);
+                s_sorted[q] = s_c[j];
+                s_ss[q] = credit ? a.cand_src[(uint64_t)node * a.CB + j] : 0u;
+            }
         }
         __syncthreads();
-        // sort inside buckets
+        // sort inside buckets, by key then joiner
         for (uint32_t b = threadIdx.x; b <= np; b += MT) {
             const uint32_t lo = s_off[b], hi = s_off[b + 1];
             if (hi - lo > 32) {
@@ -595,12 +647,15 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
             } else {
                 for (uint32_t x = lo + 1; x < hi; ++x) {
                     const uint64_t v = s_sorted[x];
+                    const uint32_t vs = s_ss[x];
                     uint32_t y = x;
-                    while (y > lo && s_sorted[y - 1] > v) {
+                    while (y > lo && (s_sorted[y - 1] > v || (s_sorted[y - 1] == v && s_ss[y - 1] > vs))) {
                         s_sorted[y] = s_sorted[y - 1];
+                        s_ss[y] = s_ss[y - 1];
                         --y;
                     }
                     s_sorted[y] = v;
+                    s_ss[y] = vs;
                 }
             }
         }
@@ -610,9 +665,15 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
             const uint32_t b = s_giant[g];
             const uint32_t lo = s_off[b], len = s_off[b + 1] - lo;
             const int p2 = kcna_pow2_ceil_d((int)len);
-            for (int i = threadIdx.x; i < p2; i += MT) s_c[i] = i < (int)len ? s_sorted[lo + i] : KCNA_EMPTY_KEY;
-            kcna_cta_bitonic(s_c, p2);
-            for (uint32_t i = threadIdx.x; i < len; i += MT) s_sorted[lo + i] = s_c[i];
+            for (int i = threadIdx.x; i < p2; i += MT) {
+                s_c[i] = i < (int)len ? s_sorted[lo + i] : KCNA_EMPTY_KEY;
+                s_b[i] = i < (int)len ? s_ss[lo + i] : KCNA_NONE; // s_b is free after the scatter
+            }
+            kcna_cta_bitonic_kv(s_c, s_b, p2);
+            for (uint32_t i = threadIdx.x; i < len; i += MT) {
+                s_sorted[lo + i] = s_c[i];
+                s_ss[lo + i] = s_b[i];
+            }
             __syncthreads();
         }
         // duplicates among candidates are now adjacent
@@ -621,7 +682,7 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
         __syncthreads();
         const uint32_t kept = block_exclusive_scan(s_kept, (int)total, s_warp);
         const uint32_t newcnt = min(a.limit, np + kept);
-        unsigned long long flagged = 0;
+        unsigned long long flagged = 0, placed = 0;
         for (uint32_t i = threadIdx.x; i < np; i += MT) {
             const uint64_t k = s_pool[i];
             const uint32_t r = i + s_kept[s_off[i + 1]];
@@ -644,16 +705,21 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
             const uint32_t r = (uint32_t)lo + s_kept[j];
             if (r < newcnt) {
                 gp[r] = s_sorted[j] | KCNA_FLAG_NEW | KCNA_FLAG_ISNEW;
-                if (r < a.K) ++flagged;
+                ++placed;
+                if (r < a.K) {
+                    ++flagged;
+                    if (credit && s_ss[j] < a.n_nodes) a.found[s_ss[j]] = 1; // lowest joiner of this key
+                }
             }
         }
         flagged = kcna_warp_sum(flagged);
+        placed = kcna_warp_sum(placed);
         if ((threadIdx.x & 31) == 0 && flagged) atomicAdd(&s_flagged, flagged);
+        if ((threadIdx.x & 31) == 0 && placed) atomicAdd(a.counters + 3, placed);
         __syncthreads();
         if (threadIdx.x == 0) {
             atomicAdd(a.counters + 1, s_flagged);
             if (raw > a.CB) atomicAdd(a.counters + 2, (unsigned long long)(raw - a.CB));
-            atomicAdd(a.counters + 3, (unsigned long long)(newcnt - min(np, newcnt)));
             atomicAdd(a.counters + 7, (unsigned long long)nc);
             atomicAdd(a.counters + 9, (unsigned long long)newcnt);
             a.pool_cnt[node] = newcnt;
@@ -915,7 +981,7 @@ size_t join_smem_bytes(uint32_t capA, uint32_t capB) {
 }
 size_t merge_smem_bytes(uint32_t cap, uint32_t CB) {
     size_t cp = (size_t)kcna_pow2_ceil((int)CB);
-    return cap * 8 + cp * 8 * 2 + cp * 4 + (cp + 1) * 4 + (size_t)(cap + 2) * 4 * 3;
+    return cap * 8 + cp * 8 * 2 + cp * 4 * 2 + (size_t)(cap + 2) * 4 * 3;
 }
 
 } // namespace
@@ -950,6 +1016,7 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     KCNA_TRY(kcna_alloc(c, &c->rold, N * c->RB, "rold"));
     KCNA_TRY(kcna_alloc(c, &c->rold_cnt, N, "rold_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
+    KCNA_TRY(kcna_alloc(c, &c->cand_src, N * c->CB, "candidate joiners"));
     KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->big_list, N, "merge queue"));
     KCNA_TRY(kcna_alloc(c, &c->big_cnt, 1, "merge queue count"));
@@ -1003,6 +1070,7 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     a.radius = c->radius;
     a.cand = c->cand;
     a.cand_cnt = c->cand_cnt;
+    a.cand_src = c->cand_src;
     a.CB = c->CB;
     a.found = c->found;
     a.counters = c->counters;
@@ -1017,6 +1085,9 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
                              "join smem attr"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 8 * 8, c->stream), "memset"));
+    // found (src/kgraph.cpp:1104,1116): cleared for every node, then set by the
+    // merge for the joiners whose candidates it inserts below K
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->found, 0, c->n, c->stream), "memset"));
     KCNA_TRY(kcna_phase_begin(c));
     if ((c->gram_exact || c->bf16_screen) && kcna_join_tc_fits(a)) {
         KCNA_TRY(kcna_join_tc_launch(c, a));
@@ -1057,7 +1128,7 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
 }
 
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
-                       uint64_t *merged, uint64_t *inserted) {
+                       uint64_t *merged, uint64_t *inserted, bool credit_found) {
     MergeArgs a;
     a.pool = c->pool;
     a.pool_cnt = c->pool_cnt;
@@ -1069,6 +1140,9 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     a.cand_cnt = c->cand_cnt;
     a.CB = c->CB;
     a.counters = c->counters;
+    a.cand_src = credit_found ? c->cand_src : nullptr;
+    a.found = c->found;
+    a.n_nodes = c->n;
     size_t sm = merge_smem_bytes(c->cap, c->CB);
     KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)std::max<size_t>(sm, 48 * 1024)),
@@ -1094,10 +1168,11 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
         kern<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
         return KCNA_OK;
     };
-    if (surv == 1024) // the template must match the shared memory sized above
-        KCNA_TRY(launch_warp(merge_warp_kernel<1024>));
+    // the template must match the shared memory sized above
+    if (credit_found)
+        KCNA_TRY(surv == 1024 ? launch_warp(merge_warp_kernel<1024, true>) : launch_warp(merge_warp_kernel<512, true>));
     else
-        KCNA_TRY(launch_warp(merge_warp_kernel<512>));
+        KCNA_TRY(surv == 1024 ? launch_warp(merge_warp_kernel<1024, false>) : launch_warp(merge_warp_kernel<512, false>));
     merge_kernel<<<std::max(1, c->num_sms) * 4, MT, sm, c->stream>>>(a, c->big_list, c->big_cnt);
     c->launches += 2;
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
@@ -1264,7 +1339,7 @@ kcna_status kcna_nndescent_run(kcna_ctx *c, const kcna_params *pin, kcna_stats *
         uint64_t comps = 0, overflow = 0, flagged = 0, merged = 0, inserted = 0;
         const double j0 = c->phase_ms[KCNA_PHASE_JOIN], m0 = c->phase_ms[KCNA_PHASE_MERGE];
         KCNA_TRY(kcna_nnd_join(c, &P, (int)it + iter_base, &comps));
-        KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged, &merged, &inserted));
+        KCNA_TRY(kcna_merge(c, P.L, P.K, &overflow, &flagged, &merged, &inserted, true));
         if (it < KCNA_MAX_ITERS) {
             st->iter_join_ms[it] = c->phase_ms[KCNA_PHASE_JOIN] - j0;
             st->iter_merge_ms[it] = c->phase_ms[KCNA_PHASE_MERGE] - m0;

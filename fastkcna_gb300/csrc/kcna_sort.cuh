@@ -45,6 +45,33 @@ __device__ __forceinline__ void kcna_warp_bitonic(uint64_t *s, int n) {
     __syncwarp();
 }
 
+// Ascending bitonic sort of n (a power of two) (key, value) pairs in shared
+// memory by the whole thread block, ordered by key then value: among equal
+// keys the pair with the smallest value comes first.  Ends with a
+// __syncthreads.
+__device__ __forceinline__ void kcna_cta_bitonic_kv(uint64_t *s, uint32_t *v, int n) {
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+                int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                int j = i + stride;
+                bool asc = (i & size) == 0;
+                uint64_t a = s[i], b = s[j];
+                uint32_t va = v[i], vb = v[j];
+                const bool gt = a > b || (a == b && va > vb);
+                if (gt == asc) {
+                    s[i] = b;
+                    s[j] = a;
+                    v[i] = vb;
+                    v[j] = va;
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // Register bitonic sort of 32 keys, one per lane, ascending by lane.
 __device__ __forceinline__ uint64_t kcna_warp_sort32(uint64_t v) {
     const int lane = kcna_lane();
