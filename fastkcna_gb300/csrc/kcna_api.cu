@@ -697,6 +697,35 @@ kcna_status kcna_pool_search(kcna_ctx *c, const kcna_params *p, uint32_t loopcou
     return kcna_check_device_err(c, "pool search");
 }
 
+kcna_status kcna_refine_pools(kcna_ctx *c, const kcna_params *p, uint32_t loopcount, uint64_t *comps) {
+    if (!c || !p) return kcna_fail(c, KCNA_E_ARG, "refine: null argument");
+    if (loopcount == 0) return kcna_fail(c, KCNA_E_ARG, "refine: loopcount must be >= 1");
+    if (!c->has_pools || !c->has_graph) return kcna_fail(c, KCNA_E_STATE, "refine: needs pools and a graph");
+    KCNA_TRY(bind(c));
+    uint32_t used = 0;
+    KCNA_TRY(prepare_rows(c, p, &used));
+    KCNA_TRY(kcna_cand_alloc(c, p));
+    // as kcna_build between prune loops: UpdateNhoods of the loop that built
+    // this graph (loopcount - 1; 0 marks every edge new), then the refinement
+    KCNA_TRY(kcna_update_nhoods(c, (int)loopcount - 1));
+    uint64_t cc = 0;
+    if (p->refine == KCNA_REFINE_POOL_SEARCH)
+        KCNA_TRY(kcna_pool_search_run(c, p, c->cap, (int)loopcount, &cc));
+    else
+        KCNA_TRY(kcna_bridge_view(c, p, c->cap, (int)loopcount, &cc));
+    if (comps) *comps = cc;
+    return kcna_check_device_err(c, "refine");
+}
+
+kcna_status kcna_get_edge_isnew(kcna_ctx *c, uint8_t *isnew) {
+    if (!c || !isnew) return kcna_fail(c, KCNA_E_ARG, "get_edge_isnew: null argument");
+    if (!c->has_graph || !c->g_isnew) return kcna_fail(c, KCNA_E_STATE, "get_edge_isnew: no graph");
+    KCNA_TRY(bind(c));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(isnew, c->g_isnew, (size_t)c->n * c->W, cudaMemcpyDeviceToHost,
+                                                c->stream), "d2h"));
+    return kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
 kcna_status kcna_set_graph(kcna_ctx *c, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep) {
     if (!c || !c->X) return kcna_fail(c, KCNA_E_STATE, "set_graph: no rows");
     if (!ids || !degrees || width == 0 || width > 4096 || ep >= c->n) return kcna_fail(c, KCNA_E_ARG, "set_graph: bad argument");

@@ -150,6 +150,8 @@ kcna_status kcna_tc_gemm(cudaStream_t s, const void *A, int64_t lda, int a_fp32,
 // kcna_nnd.cu: NN-descent phases
 kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
+// candidate buffers for a refinement run outside a build (kcna_refine_pools), when absent
+kcna_status kcna_cand_alloc(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);  // iter 0: init lists
 // Merges every node's candidate buffer into its pool.  credit_found: the
 // candidates of an NN-descent join, whose joiners (cand_src) are credited with

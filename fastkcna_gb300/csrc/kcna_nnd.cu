@@ -1031,6 +1031,22 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     return KCNA_OK;
 }
 
+kcna_status kcna_cand_alloc(kcna_ctx *c, const kcna_params *p) {
+    if (c->cand && c->cand_cnt && c->big_list && c->big_cnt && c->counters) return KCNA_OK;
+    const uint64_t N = c->n;
+    const char *cb = getenv("KCNA_CAND_CAP");
+    uint32_t CB = cb ? (uint32_t)atoi(cb) : 4 * std::max<uint32_t>(p->L, 64);
+    CB = std::min<uint32_t>(std::max<uint32_t>(CB, 64), 8192);
+    c->CB = (uint32_t)kcna_pow2_ceil((int)CB);
+    KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
+    KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
+    KCNA_TRY(kcna_alloc(c, &c->big_list, N, "merge queue"));
+    KCNA_TRY(kcna_alloc(c, &c->big_cnt, 1, "merge queue count"));
+    if (!c->counters) KCNA_TRY(kcna_alloc(c, &c->counters, 64, "counters"));
+    KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->cand_cnt, 0, N * 4, c->stream), "memset"));
+    return KCNA_OK;
+}
+
 kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p) {
     if (p->S == 0 || p->S > 31) return kcna_fail(c, KCNA_E_ARG, "S must be in [1, 31]");
     KCNA_TRY(kcna_phase_begin(c));

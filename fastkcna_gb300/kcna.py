@@ -135,6 +135,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "kcna_wait_writes": ([P], C.c_int),
         "kcna_upload_lshkit": ([P, C.c_char_p], C.c_int),
         "kcna_pool_search": ([P, C.POINTER(Params), U32, C.POINTER(U64)], C.c_int),
+        "kcna_refine_pools": ([P, C.POINTER(Params), U32, C.POINTER(U64)], C.c_int),
+        "kcna_get_edge_isnew": ([P, P], C.c_int),
     }
     for name, (argt, rest) in sig.items():
         f = getattr(lib, name)
@@ -285,6 +287,24 @@ class Index:
         cc = C.c_uint64(0)
         self._check(self.lib.kcna_pool_search(self.h, C.byref(p), C.c_uint32(loopcount), C.byref(cc)))
         return int(cc.value)
+
+    def refine(self, loopcount: int, p: Params | None = None, **kw) -> int:
+        """UpdateNhoods + the pool refinement of loop `loopcount` (BridgeView,
+        or the pool search when p.refine says so) over the current graph, as a
+        build runs it between prune loops; returns the distance evaluations."""
+        p = p or params(**kw)
+        cc = C.c_uint64(0)
+        self._check(self.lib.kcna_refine_pools(self.h, C.byref(p), C.c_uint32(loopcount), C.byref(cc)))
+        return int(cc.value)
+
+    def edge_isnew(self):
+        """isnew flag of every graph edge (n, width) uint8, as UpdateNhoods set it."""
+        w = C.c_uint32()
+        ep = C.c_uint32()
+        self._check(self.lib.kcna_get_graph(self.h, None, None, C.byref(ep), C.byref(w)))
+        out = np.empty((self.n, w.value), np.uint8)
+        self._check(self.lib.kcna_get_edge_isnew(self.h, _ptr(out)))
+        return out
 
     def set_pools(self, ids, dists, counts, p: Params | None = None, **kw):
         p = p or params(**kw)

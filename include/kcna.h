@@ -238,6 +238,19 @@ kcna_status kcna_link(kcna_ctx *ctx, const kcna_params *params, kcna_kind kind);
  * prune loops when params->refine is KCNA_REFINE_POOL_SEARCH.  comps (may be
  * NULL) receives the distance evaluations. */
 kcna_status kcna_pool_search(kcna_ctx *ctx, const kcna_params *params, uint32_t loopcount, uint64_t *comps);
+/* One refinement step of the pools between prune loops, as kcna_build runs it
+ * after the prune loop that made the context graph: UpdateNhoods marks every
+ * graph edge new when loopcount is 1, else new iff it is absent from the graph
+ * of the previous refinement step (src/kgraph.cpp:3537-3584); then the pools
+ * are refined over the graph for loop `loopcount` (>= 1): BridgeView
+ * (src/kgraph.cpp:2478-2663), or the per-node pool search when params->refine
+ * is KCNA_REFINE_POOL_SEARCH.  Needs pools (a build or kcna_set_pools) and a
+ * graph (a build or kcna_set_graph).  comps (may be NULL) receives the
+ * distance evaluations of the refinement's joins. */
+kcna_status kcna_refine_pools(kcna_ctx *ctx, const kcna_params *params, uint32_t loopcount, uint64_t *comps);
+/* The isnew flag of every graph edge as UpdateNhoods last set it (n*width
+ * bytes, 1 = new; replaces reading nn_nsg[j].isnew, src/kgraph.cpp:3548-3555). */
+kcna_status kcna_get_edge_isnew(kcna_ctx *ctx, uint8_t *isnew);
 /* Installs a caller graph (ids n*width padded with 0xFFFFFFFF, degrees n). */
 kcna_status kcna_set_graph(kcna_ctx *ctx, const uint32_t *ids, const uint32_t *degrees, uint32_t width, uint32_t ep);
 
