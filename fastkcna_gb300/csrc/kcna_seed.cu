@@ -3,7 +3,7 @@
 // The reference starts NN-descent from S random pool entries per node
 // (src/kgraph.cpp:1001-1044).  This file replaces that start, when
 // kcna_params.learned_seed is set, with pools drawn from learned codes:
-//   1. a random subsample (up to 50,000 rows) gets a short GPU NN-descent;
+//   1. a random subsample (up to 100,000 rows) gets a short GPU NN-descent;
 //      its pools give (anchor, neighbour) pairs;
 //   2. an MLP encoder x -> GELU(W1 x + b1) -> W2 . + b2 -> L2-normalise
 //      (D -> 256 -> 64) is trained with the triplet loss
@@ -528,7 +528,7 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     Dev dev{c, {}};
     // --- 1. input scale: rows are divided by their global RMS so the encoder sees O(1) values
     // --- subsample and its NN-descent (a separate context on the same device)
-    const uint32_t ns = std::min<uint32_t>(N, 50000);
+    const uint32_t ns = std::min<uint32_t>(N, 100000);
     std::vector<uint32_t> sub(N);
     for (uint32_t i = 0; i < N; ++i) sub[i] = i;
     std::mt19937 rng(p->seed ^ 0x5EEDu);

@@ -16,7 +16,17 @@ stores its outputs:
     order of equal-rank reverse entries fixed as oracle/ref_harness.cpp states;
   * into ref_pool_search_*.npz, the per-node pool search (inSearch,
     src/kgraph.cpp:2340-2414, 3667-3688) of the stored pools over the stored
-    NSG link graph, loops 1 and 2.
+    NSG link graph, loops 1 and 2;
+  * into ref_refine_*.npz, two P2K refinement steps as buildFastNSG runs them
+    between prune loops (src/kgraph.cpp:3813-3843): UpdateNhoods
+    (:3537-3584) + BridgeView (:2478-2663) of loop 1 on the stored pools over
+    the stored NSG link graph g1, then the NSG link g2 of the refined pools
+    and UpdateNhoods + BridgeView of loop 2 over g2 (edges new against g1);
+    pools, pool flags, edge flags and distance evaluations of each step;
+  * into ref_prune_large_*.npz, sync_prune and Link of the three kinds at the
+    C2 flags' sizes (nsg_R = 50, search_K = 500) on 500-entry pools: the
+    exact 500-NN lists (LinearSearch) of 2,000 rows, so that the input pools
+    are deterministic and need not be stored.
 The datasets are stored with the outputs (C2-like rows as uint8).
 
 Usage: python tests/golden/make_golden.py   (needs oracle/_ref built here)
@@ -91,6 +101,48 @@ def make_pool_search(name):
     np.savez_compressed(os.path.join(HERE, f"ref_pool_search_{name}.npz"), **out)
 
 
+def make_refine(name):
+    """Two refinement steps (UpdateNhoods + BridgeView, loops 1 and 2) on the
+    pools and NSG link graph of ref_<name>.npz, one thread."""
+    ref = oracle_py.Reference()
+    z = dict(np.load(os.path.join(HERE, f"ref_{name}.npz")))
+    X = z["X"].astype(np.float32)
+    p = oracle_py.params(**PARAMS, tau=float(z["tau"]), step=8)
+    g1, d1 = z["link_nsg_ids"], z["link_nsg_deg"]
+    i1, dd1, c1, f1, n1, cc1 = ref.refine(X, p, z["pool_ids"], z["pool_d"], z["pool_cnt"], g1, d1, 1)
+    g2, _, d2 = ref.link(1, X, p, i1, dd1, c1, g1.shape[1])
+    i2, dd2, c2, f2, n2, cc2 = ref.refine(X, p, i1, dd1, c1, g2, d2, 2, pflags=f1, g_old=g1, g_old_deg=d1)
+    out = dict(loop1_ids=i1, loop1_d=dd1, loop1_cnt=c1, loop1_flags=f1, loop1_isnew=n1, loop1_comps=np.uint64(cc1),
+               g2_ids=g2, g2_deg=d2, loop2_ids=i2, loop2_d=dd2, loop2_cnt=c2, loop2_flags=f2, loop2_isnew=n2,
+               loop2_comps=np.uint64(cc2))
+    np.savez_compressed(os.path.join(HERE, f"ref_refine_{name}.npz"), **out)
+
+
+LARGE_N, LARGE_K, LARGE_W = 2000, 500, 64
+LARGE_PARAMS = dict(K=500, L=500, S=12, R=100, iterations=6, search_L=80, nsg_R=50, search_K=500, controls=20,
+                    massq_S=10, angle=60.0)
+
+
+def make_prune_large(name, tau):
+    """Prune and Link of the three kinds with nsg_R = 50, search_K = 500 on the
+    exact 500-NN pools of 2,000 rows (ids stored as uint16)."""
+    ref = oracle_py.Reference()
+    X = synth.base(name, LARGE_N)
+    if name == "c2":
+        X = X.astype(np.uint8).astype(np.float32)
+    ids = np.arange(LARGE_N, dtype=np.uint32)
+    pid, pd = ref.linear_search(X, ids, LARGE_K)
+    pc = np.full(LARGE_N, LARGE_K, np.uint32)
+    p = oracle_py.params(**LARGE_PARAMS, tau=tau)
+    out = {"X": X.astype(np.uint8) if name == "c2" else X, "tau": np.float32(tau)}
+    for kind, tag in ((1, "nsg"), (3, "tau"), (4, "alpha")):
+        gi, _, deg = ref.prune(kind, X, p, pid, pd, pc, LARGE_W)
+        out[f"prune_{tag}_ids"], out[f"prune_{tag}_deg"] = gi.astype(np.uint16), deg.astype(np.uint16)
+        gi, _, deg = ref.link(kind, X, p, pid, pd, pc, 2 * LARGE_W)
+        out[f"link_{tag}_ids"], out[f"link_{tag}_deg"] = gi.astype(np.uint16), deg.astype(np.uint16)
+    np.savez_compressed(os.path.join(HERE, f"ref_prune_large_{name}.npz"), **out)
+
+
 if __name__ == "__main__":
     if not oracle_py.Reference.available():
         sys.exit("oracle/_ref/libkcna_ref.so is missing: run oracle/build_ref.sh")
@@ -100,4 +152,8 @@ if __name__ == "__main__":
     make_cagra("c2")
     make_pool_search("c1")
     make_pool_search("c2")
+    make_refine("c1")
+    make_refine("c2")
+    make_prune_large("c1", 0.05)
+    make_prune_large("c2", 10.0)
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

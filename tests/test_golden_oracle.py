@@ -105,3 +105,28 @@ def test_pool_search(oracle, name, loop):
         assert np.array_equal(od, g[f"loop{loop}_d"])
     n = z["X"].shape[0]
     assert cc / (n * (n - 1) / 2) == pytest.approx(float(g[f"loop{loop}_scan"]), rel=1e-5)
+
+
+PL = dict(K=500, L=500, S=12, R=100, iterations=6, search_L=80, nsg_R=50, search_K=500, controls=20, massq_S=10,
+          angle=60.0)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_prune_link_large(oracle, name):
+    """nsg_R = 50, search_K = 500 on the exact 500-NN of 2,000 rows (golden
+    ref_prune_large_*.npz): the oracle's edge lists equal the reference's."""
+    z = dict(np.load(os.path.join(HERE, f"ref_prune_large_{name}.npz")))
+    X = z["X"].astype(np.float32)
+    n = X.shape[0]
+    pid, pd = oracle.knn(X, np.arange(n, dtype=np.uint32), 500)
+    pc = np.full(n, 500, np.uint32)
+    p = oracle_py.params(**PL, tau=float(z["tau"]))
+    for kind, tag in KINDS:
+        gi, _, deg = oracle.prune(kind, X, p, pid, pd, pc, 64)
+        assert np.array_equal(deg, z[f"prune_{tag}_deg"].astype(np.uint32)), tag
+        for i in range(n):
+            assert np.array_equal(gi[i, : deg[i]], z[f"prune_{tag}_ids"][i, : deg[i]].astype(np.uint32)), (tag, i)
+        gi, _, deg = oracle.link(kind, X, p, pid, pd, pc, 128)
+        assert np.array_equal(deg, z[f"link_{tag}_deg"].astype(np.uint32)), tag
+        for i in range(n):
+            assert set(gi[i, : deg[i]].tolist()) == set(z[f"link_{tag}_ids"][i, : deg[i]].tolist()), (tag, i)

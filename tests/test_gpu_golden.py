@@ -59,3 +59,97 @@ def test_gpu_beam_search_vs_reference(index, name):
     assert np.array_equal(bi, z["bs_ids"])
     if name == "c2":
         assert np.array_equal(bd, z["bs_d"])
+
+
+def _same_pools(gi, gd, gc, ri, rd, rc):
+    """Pools equal as the reference builds them, up to the order of entries at
+    one distance (the reference appends an equal distance after the existing
+    ones, src/kgraph.cpp:261-298; the GPU orders them by id) and, in a full
+    pool, up to which of the entries tied at its last distance it keeps.
+    Returns the number of nodes that differ."""
+    bad = 0
+    for i in range(gi.shape[0]):
+        if gc[i] != rc[i]:
+            bad += 1
+            continue
+        c = int(gc[i])
+        a = sorted(zip(gd[i, :c].tolist(), gi[i, :c].tolist()))
+        b = sorted(zip(rd[i, :c].tolist(), ri[i, :c].tolist()))
+        if a == b:
+            continue
+        last = a[-1][0]
+        if c > 0 and last == b[-1][0] and [x for x in a if x[0] < last] == [x for x in b if x[0] < last]:
+            continue
+        bad += 1
+    return bad
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("screen", [0, 1])
+def test_gpu_refine_vs_reference(index, name, screen):
+    """Two P2K refinement steps (UpdateNhoods + BridgeView, loops 1 and 2) from
+    the reference's pools and NSG link graph: the GPU's pools, the edges'
+    isnew flags and the join's distance evaluations equal the reference's own
+    (golden ref_refine_*.npz), up to the order of equal distances.  screen = 1
+    runs the BF16 mode (Gram-tile P2K on the integer C2 rows)."""
+    z = load(name)
+    r = dict(np.load(os.path.join(HERE, f"ref_refine_{name}.npz")))
+    p = kcna.params(**P, tau=float(z["tau"]), step=8, screen=screen)
+    index.upload(z["X"])
+    index.set_pools(z["pool_ids"], z["pool_d"], z["pool_cnt"], p)
+    index.set_graph(z["link_nsg_ids"], z["link_nsg_deg"], 0)
+    comps1 = index.refine(1, p)
+    deg1 = z["link_nsg_deg"]
+    isnew = index.edge_isnew()
+    for i in range(isnew.shape[0]):
+        assert isnew[i, : deg1[i]].all()  # loop 1: every edge new
+    gi, gd, gc = index.pools()
+    W = r["loop1_ids"].shape[1]
+    assert _same_pools(gi[:, :W], gd[:, :W], gc, r["loop1_ids"], r["loop1_d"], r["loop1_cnt"]) == 0
+    assert abs(comps1 - int(r["loop1_comps"])) <= 1e-4 * int(r["loop1_comps"]) + 2, (comps1, int(r["loop1_comps"]))
+    index.set_graph(r["g2_ids"], r["g2_deg"], 0)
+    comps2 = index.refine(2, p)
+    isnew = index.edge_isnew()
+    for i in range(isnew.shape[0]):
+        d = int(r["g2_deg"][i])
+        assert np.array_equal(isnew[i, :d], r["loop2_isnew"][i, :d]), i
+    gi, gd, gc = index.pools()
+    assert _same_pools(gi[:, :W], gd[:, :W], gc, r["loop2_ids"], r["loop2_d"], r["loop2_cnt"]) == 0
+    assert abs(comps2 - int(r["loop2_comps"])) <= 1e-4 * int(r["loop2_comps"]) + 2, (comps2, int(r["loop2_comps"]))
+
+
+PL = dict(K=500, L=500, S=12, R=100, iterations=6, search_L=80, nsg_R=50, search_K=500, controls=20, massq_S=10,
+          angle=60.0)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("screen", [0, 1])
+def test_gpu_prune_link_large_vs_reference(index, name, screen):
+    """sync_prune and Link at the C2 flags' sizes (nsg_R = 50, search_K = 500)
+    on 500-entry pools, the exact 500-NN of 2,000 rows: the GPU's edge lists
+    equal the reference's own (golden ref_prune_large_*.npz).  screen = 1
+    selects the BF16 mode (on C2's integer rows: the Gram-tile prune)."""
+    z = dict(np.load(os.path.join(HERE, f"ref_prune_large_{name}.npz")))
+    X = z["X"].astype(np.float32)
+    p = kcna.params(**PL, tau=float(z["tau"]), screen=screen)
+    index.upload(X)
+    n = X.shape[0]
+    pid, pd = index.knn_exact(np.arange(n, dtype=np.uint32), 500)
+    pc = np.full(n, 500, np.uint32)
+    for kind, tag in KINDS:
+        index.set_pools(pid, pd, pc, p)
+        index.prune(kind, p)
+        g, deg, _ = index.graph()
+        ref_deg = z[f"prune_{tag}_deg"].astype(np.uint32)
+        ref_ids = z[f"prune_{tag}_ids"].astype(np.uint32)
+        assert np.array_equal(deg, ref_deg), (kind, screen)
+        for i in range(n):
+            assert np.array_equal(g[i, : deg[i]], ref_ids[i, : deg[i]]), (kind, screen, i)
+        index.set_pools(pid, pd, pc, p)
+        index.link(kind, p)
+        g, deg, _ = index.graph()
+        ref_deg = z[f"link_{tag}_deg"].astype(np.uint32)
+        ref_ids = z[f"link_{tag}_ids"].astype(np.uint32)
+        assert np.array_equal(deg, ref_deg), (kind, screen)
+        for i in range(n):
+            assert set(g[i, : deg[i]].tolist()) == set(ref_ids[i, : deg[i]].tolist()), (kind, screen, i)
