@@ -1,0 +1,111 @@
+"""Build quality against the reference CPU build at the 0.002 bar.
+
+NN-descent is stochastic, so the GPU build is held to the reference's own
+builds (tests/golden/ref_quality_c2.npz, made by
+tests/golden/make_golden_quality.py with the reference compiled from its
+sources) on the same rows and flags: the C2 workload's first 100,000 and
+200,000 rows, -K 500 -L 500 -S 12 -R 100 --search_L 80 --nsg_R 50
+--search_K 500 --massq_S 10 --loop_i 2 --step 10, -I 12 --recall 0.99.
+Both sides are scored on the same nodes and queries:
+  * recall@K: control recall on the reference's own 100 control nodes
+    (GenerateControl, src/kgraph.cpp:363-387; the GPU library draws the same
+    nodes), after NN-descent and after every BridgeView loop;
+  * search recall@10 over 10,000 C2 queries, beam L from the entry point plus
+    L - 1 seeded random nodes (the GPU beam search is bit-identical to the
+    reference's get_neighbors on the same graph).
+Bar: within 0.002 of the reference.  The reference's two builds of the same
+rows differ from each other by up to 0.006 (OpenMP timing), so a GPU value
+passes when it lies within 0.002 of the interval the reference's builds span.
+At 100,000 rows the reference's NN-descent stalls near recall 0.80 (few nodes
+keep finding new neighbours); matching that level checks the join's
+semantics (found flags, sampling, reverse lists), not just convergence.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from fastkcna_gb300 import kcna, synth
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = np.load(os.path.join(HERE, "golden", "ref_quality_c2.npz"))
+FLAGS = dict(K=500, L=500, S=12, R=100, iterations=12, search_L=80, nsg_R=50, search_K=500, massq_S=10,
+             loop_i=2, step=10, angle=60.0, recall=0.99, controls=100, seed=2024)
+TOL = 0.002
+
+
+def _within(value, refs, tol=TOL):
+    refs = np.asarray(refs, np.float64)
+    return refs.min() - tol <= value <= refs.max() + tol
+
+
+def _ref_recalls(n):
+    """(recall after NN-descent, after loop 1, after loop 2) of each reference
+    build: the CSV recall row ends with the value after NN-descent and one
+    value per BridgeView loop (loop_i = 2)."""
+    out = []
+    for row in GOLD[f"recall_{n}"]:
+        r = row[~np.isnan(row)]
+        out.append((r[-3], r[-2], r[-1]))
+    return np.asarray(out)
+
+
+def _search10(ix, Q, truth, n, ep, L):
+    rng = np.random.default_rng(7)
+    extra = rng.choice(n, size=L, replace=False)
+    start = np.concatenate([[ep], extra[extra != ep][: L - 1]]).astype(np.uint32)
+    init = np.broadcast_to(start, (Q.shape[0], L)).copy()
+    found, _ = ix.search(Q, L, 10, init_ids=init)
+    hit = sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth))
+    return hit / (10.0 * Q.shape[0])
+
+
+@pytest.fixture(scope="module", params=[100_000, 200_000])
+def built(request):
+    n = request.param
+    X = synth.base("c2", n)
+    Q = synth.queries("c2", int(GOLD["nq"]))
+    out = {"n": n}
+    with kcna.Index(0) as ix:
+        ix.upload(X)
+        truth, _ = ix.knn_queries(Q, 10)
+        for mode, extra in (("plain", {}), ("learned_bf16", dict(learned_seed=1, screen=1))):
+            st = ix.build("nsg", kcna.params(**FLAGS, **extra))
+            _, _, ep = ix.graph()
+            out[mode] = dict(stats=st, search={int(L): _search10(ix, Q, truth, n, ep, int(L))
+                                               for L in GOLD["beams"]})
+    return out
+
+
+def test_plain_build_recall_within_reference(built):
+    n, st = built["n"], built["plain"]["stats"]
+    ref = _ref_recalls(n)
+    got = (st["loop_recall"][0], st["loop_recall"][1], st["loop_recall"][2])
+    names = ("after NN-descent", "after loop 1", "after loop 2")
+    for i, name in enumerate(names):
+        assert _within(got[i], ref[:, i]), (n, name, got, ref.tolist())
+
+
+def test_plain_build_search_recall_within_reference(built):
+    n = built["n"]
+    ref = GOLD[f"search10_{n}"]
+    got = [built["plain"]["search"][int(L)] for L in GOLD["beams"]]
+    for j, L in enumerate(GOLD["beams"]):
+        assert _within(got[j], ref[:, j]), (n, int(L), got, ref.tolist())
+
+
+def test_learned_bf16_search_recall_within_plain(built):
+    """The learned seed + BF16 form against the plain FP32 GPU build on the
+    same rows: search recall@10 within 0.002 at every beam where both builds
+    converge (200,000 rows; at 100,000 rows the seeded NN-descent stalls at a
+    different level than the random-init one, as the reference's own stall
+    level depends on its start)."""
+    if built["n"] != 200_000:
+        pytest.skip("the seeded and random-init NN-descent stall at different levels at 100,000 rows")
+    a = [built["learned_bf16"]["search"][int(L)] for L in GOLD["beams"]]
+    b = [built["plain"]["search"][int(L)] for L in GOLD["beams"]]
+    for j, L in enumerate(GOLD["beams"]):
+        assert abs(a[j] - b[j]) <= TOL, (int(L), a, b)
+    assert built["learned_bf16"]["stats"]["loop_recall"][-1] >= built["plain"]["stats"]["loop_recall"][-1] - TOL
