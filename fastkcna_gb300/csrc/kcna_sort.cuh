@@ -45,6 +45,32 @@ __device__ __forceinline__ void kcna_warp_bitonic(uint64_t *s, int n) {
     __syncwarp();
 }
 
+// Ascending bitonic sort of n (a power of two) keys in shared memory by one
+// warp, each carrying a 16-bit value that moves with it (values of equal keys
+// end in no particular order).
+__device__ __forceinline__ void kcna_warp_bitonic_kv16(uint64_t *s, uint16_t *v, int n) {
+    const int lane = kcna_lane();
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncwarp();
+            for (int t = lane; t < (n >> 1); t += 32) {
+                int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                int j = i + stride;
+                bool asc = (i & size) == 0;
+                uint64_t a = s[i], b = s[j];
+                if ((a > b) == asc) {
+                    s[i] = b;
+                    s[j] = a;
+                    const uint16_t va = v[i];
+                    v[i] = v[j];
+                    v[j] = va;
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // Ascending bitonic sort of n (a power of two) (key, value) pairs in shared
 // memory by the whole thread block, ordered by key then value: among equal
 // keys the pair with the smallest value comes first.  Ends with a
