@@ -96,9 +96,51 @@ static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
     st->tree_attached = c->tree_attached;
 }
 
+kcna_status kcna_dev_malloc(kcna_ctx *c, size_t bytes, void **out, const char *what) {
+    *out = nullptr;
+    // smallest cached block that holds `bytes` without wasting more than half of it
+    auto it = c->free_blocks.lower_bound(bytes);
+    if (it != c->free_blocks.end() && it->first <= 2 * bytes + (1u << 20)) {
+        *out = it->second;
+        c->free_blocks.erase(it);
+        return KCNA_OK;
+    }
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e == cudaErrorMemoryAllocation && !c->free_blocks.empty()) {
+        (void)cudaGetLastError();
+        kcna_release_all(c);
+        e = cudaMalloc(out, bytes);
+    }
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        (void)cudaGetLastError();
+        return kcna_fail(c, KCNA_E_OOM, std::string("cudaMalloc failed for ") + what);
+    }
+    c->block_bytes[*out] = bytes;
+    return KCNA_OK;
+}
+
+void kcna_release(kcna_ctx *c, void *p) {
+    if (!p) return;
+    auto it = c->block_bytes.find(p);
+    if (it == c->block_bytes.end()) {
+        cudaFree(p);
+        return;
+    }
+    c->free_blocks.emplace(it->second, p);
+}
+
+void kcna_release_all(kcna_ctx *c) {
+    for (auto &b : c->free_blocks) {
+        c->block_bytes.erase(b.second);
+        cudaFree(b.second);
+    }
+    c->free_blocks.clear();
+}
+
 static kcna_status grow(kcna_ctx *c, void **p, size_t *cur, size_t bytes) {
     if (*cur >= bytes && *p) return KCNA_OK;
-    if (*p) cudaFree(*p);
+    if (*p) kcna_release(c, *p);
     *p = nullptr;
     *cur = 0;
     cudaError_t e = cudaMalloc(p, bytes);
@@ -138,7 +180,7 @@ static void free_state(kcna_ctx *c) {
                     c->cand_src, c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
                     c->d_control_knn, c->big_list, c->big_cnt};
     for (void *b : bufs)
-        if (b) cudaFree(b);
+        if (b) kcna_release(c, b);
     c->pool = nullptr;
     c->pool_cnt = nullptr;
     c->radius = nullptr;
@@ -203,8 +245,8 @@ __global__ void gram_check_kernel(const float *__restrict__ X, uint32_t n, uint3
 }
 
 static void release_row_copies(kcna_ctx *c) {
-    if (c->Xh) cudaFree(c->Xh);
-    if (c->norms) cudaFree(c->norms);
+    if (c->Xh) kcna_release(c, c->Xh);
+    if (c->norms) kcna_release(c, c->norms);
     c->Xh = nullptr;
     c->norms = nullptr;
     c->gram_exact = c->bf16_exact = c->bf16_screen = false;
@@ -282,7 +324,7 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
         c->gram_exact = true;
         if (gram) *gram = 1;
     } else {
-        cudaFree(c->norms);
+        kcna_release(c, c->norms);
         c->norms = nullptr;
     }
     return KCNA_OK;
@@ -292,7 +334,7 @@ kcna_status kcna_rows_reset(kcna_ctx *c, uint32_t n, uint32_t d) {
     if (n < 2 || d == 0 || n > KCNA_MAX_ID) return kcna_fail(c, KCNA_E_ARG, "upload: need n >= 2, d >= 1, n < 2^30");
     KCNA_TRY(bind(c));
     free_state(c);
-    if (c->X) cudaFree(c->X);
+    if (c->X) kcna_release(c, c->X);
     c->X = nullptr;
     release_row_copies(c);
     c->d = d;
@@ -362,12 +404,15 @@ void kcna_destroy(kcna_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_state(c);
-    if (c->X) cudaFree(c->X);
+    if (c->X) kcna_release(c, c->X);
     release_row_copies(c);
-    if (c->scratch) cudaFree(c->scratch);
-    if (c->scratch2) cudaFree(c->scratch2);
-    if (c->d_err) cudaFree(c->d_err);
-    if (c->counters) cudaFree(c->counters);
+    if (c->scratch) kcna_release(c, c->scratch);
+    if (c->scratch2) kcna_release(c, c->scratch2);
+    if (c->d_err) kcna_release(c, c->d_err);
+    if (c->counters) kcna_release(c, c->counters);
+    kcna_release_all(c);
+    for (auto &b : c->block_bytes) cudaFree(b.first); // blocks still held by no pointer of the context
+    c->block_bytes.clear();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -416,7 +461,7 @@ static kcna_status to_device_rows(kcna_ctx *c, const float *q, uint32_t m, uint6
                                                  cudaMemcpyHostToDevice, c->stream),
                             "query copy");
     if (s != KCNA_OK) {
-        cudaFree(dq);
+        kcna_release(c, dq);
         return s;
     }
     *out = dq;
@@ -444,10 +489,10 @@ kcna_status kcna_knn_exact(kcna_ctx *c, const uint32_t *ids, uint32_t m, uint32_
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
     if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "knn sync");
-    cudaFree(did);
-    cudaFree(rows);
-    cudaFree(oid);
-    cudaFree(od);
+    kcna_release(c, did);
+    kcna_release(c, rows);
+    kcna_release(c, oid);
+    kcna_release(c, od);
     return s == KCNA_OK ? kcna_check_device_err(c, "knn_exact") : s;
 }
 
@@ -468,9 +513,9 @@ kcna_status kcna_knn_queries(kcna_ctx *c, const float *queries, uint32_t m, uint
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
     if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "knn sync");
-    cudaFree(dq);
-    cudaFree(oid);
-    cudaFree(od);
+    kcna_release(c, dq);
+    kcna_release(c, oid);
+    kcna_release(c, od);
     return s == KCNA_OK ? kcna_check_device_err(c, "knn_queries") : s;
 }
 
@@ -735,7 +780,7 @@ kcna_status kcna_set_graph(kcna_ctx *c, const uint32_t *ids, const uint32_t *deg
     if (c->W != width) {
         c->W = 0;
         if (c->g_ids) {
-            cudaFree(c->g_ids);
+            kcna_release(c, c->g_ids);
             c->g_ids = nullptr;
         }
     }
@@ -791,10 +836,10 @@ kcna_status kcna_search(kcna_ctx *c, const float *queries, uint32_t m, uint64_t 
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(out_dists, od, (size_t)m * k * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
     if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "search sync");
-    cudaFree(dq);
-    cudaFree(di);
-    cudaFree(oid);
-    cudaFree(od);
+    kcna_release(c, dq);
+    kcna_release(c, di);
+    kcna_release(c, oid);
+    kcna_release(c, od);
     return s == KCNA_OK ? kcna_check_device_err(c, "search") : s;
 }
 

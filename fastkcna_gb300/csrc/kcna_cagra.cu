@@ -203,11 +203,11 @@ kcna_status kcna_cagra_prune(kcna_ctx *c, const kcna_params *p) {
     uint64_t *off = nullptr, *rev = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
-        cudaFree(fwd);
-        cudaFree(indeg);
-        cudaFree(cursor);
-        cudaFree(off);
-        cudaFree(rev);
+        kcna_release(c, fwd);
+        kcna_release(c, indeg);
+        kcna_release(c, cursor);
+        kcna_release(c, off);
+        kcna_release(c, rev);
     };
     if ((s = kcna_alloc(c, &fwd, (uint64_t)N * PK, "CAGRA kept ranks")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &indeg, N, "CAGRA in-degrees")) != KCNA_OK) return cleanup(), s;

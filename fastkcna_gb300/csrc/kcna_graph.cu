@@ -1057,7 +1057,7 @@ kcna_status exclusive_scan(kcna_ctx *c, const uint32_t *in, uint64_t n, uint64_t
     if (s == KCNA_OK && total_h)
         s = kcna_cuda_check(c, cudaMemcpyAsync(total_h, sums + nb, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
     if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "scan sync");
-    cudaFree(sums);
+    kcna_release(c, sums);
     return s;
 }
 
@@ -1127,10 +1127,10 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     uint64_t *off = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
-        cudaFree(indeg);
-        cudaFree(cursor);
-        cudaFree(rev);
-        cudaFree(off);
+        kcna_release(c, indeg);
+        kcna_release(c, cursor);
+        kcna_release(c, rev);
+        kcna_release(c, off);
     };
     if ((s = kcna_alloc(c, &indeg, N, "indeg")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
@@ -1178,7 +1178,7 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
         s = launch_link(RowsB16{c->Xh, (int)c->ld});
     else
         s = launch_link(RowsF32{c->X, (int)c->ld});
-    cudaFree(blist);
+    kcna_release(c, blist);
     unsigned long long h = 0;
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 17, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
@@ -1220,11 +1220,11 @@ kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     float *od = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
-        cudaFree(part);
-        cudaFree(center);
-        cudaFree(init);
-        cudaFree(oid);
-        cudaFree(od);
+        kcna_release(c, part);
+        kcna_release(c, center);
+        kcna_release(c, init);
+        kcna_release(c, oid);
+        kcna_release(c, od);
     };
     const uint32_t Lw = std::max<uint32_t>(1, std::min<uint32_t>(p->search_L, c->n - 1));
     if ((s = kcna_alloc(c, &part, (size_t)nb * d, "centroid")) != KCNA_OK) return cleanup(), s;
@@ -1270,10 +1270,10 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     uint32_t *vis = nullptr, *qa = nullptr, *qb = nullptr, *cntd = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
-        cudaFree(vis);
-        cudaFree(qa);
-        cudaFree(qb);
-        cudaFree(cntd);
+        kcna_release(c, vis);
+        kcna_release(c, qa);
+        kcna_release(c, qb);
+        kcna_release(c, cntd);
     };
     if ((s = kcna_alloc(c, &vis, words, "visited")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &qa, N, "frontier")) != KCNA_OK) return cleanup(), s;
@@ -1297,8 +1297,8 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     cudaMemsetAsync(c->counters + 18, 0, 16, c->stream);
     uint32_t *targeted = nullptr, *localmin = nullptr;
     auto cleanup2 = [&]() {
-        cudaFree(targeted);
-        cudaFree(localmin);
+        kcna_release(c, targeted);
+        kcna_release(c, localmin);
     };
     if ((s = kcna_alloc(c, &targeted, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
     if ((s = kcna_alloc(c, &localmin, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
@@ -1381,11 +1381,11 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     uint64_t *off = nullptr, *pushes = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
-        cudaFree(tcount);
-        cudaFree(cursor);
-        cudaFree(rnn);
-        cudaFree(off);
-        cudaFree(pushes);
+        kcna_release(c, tcount);
+        kcna_release(c, cursor);
+        kcna_release(c, rnn);
+        kcna_release(c, off);
+        kcna_release(c, pushes);
     };
     if ((s = kcna_alloc(c, &tcount, N, "push counts")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
@@ -1424,13 +1424,13 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             KCNA_LAUNCHED(c);
             uint64_t np2 = 0;
             s = exclusive_scan(c, tc2, N, off, &np2);
-            cudaFree(tc2);
+            kcna_release(c, tc2);
             if (s != KCNA_OK) return cleanup(), s;
             np_all = np2; // uncapped count covers the capped pushes too
         }
-        cudaFree(pushes);
+        kcna_release(c, pushes);
         pushes = nullptr;
-        cudaFree(rnn);
+        kcna_release(c, rnn);
         rnn = nullptr;
         if ((s = kcna_alloc(c, &pushes, std::max<uint64_t>(np_all, 1), "pushes")) != KCNA_OK) return cleanup(), s;
         if ((s = kcna_alloc(c, &rnn, std::max<uint64_t>(np_all, 1), "rnn")) != KCNA_OK) return cleanup(), s;

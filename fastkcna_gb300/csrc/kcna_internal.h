@@ -4,8 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "kcna.h"
@@ -89,6 +91,13 @@ struct kcna_ctx {
     void *scratch2 = nullptr;
     size_t scratch2_bytes = 0;
 
+    // device memory cache: blocks from kcna_dev_malloc that kcna_release handed
+    // back, kept (by size) for the next kcna_alloc instead of cudaFree, so that
+    // repeated builds of one size allocate once; freed at kcna_destroy, or
+    // when cudaMalloc runs out of memory
+    std::multimap<size_t, void *> free_blocks;
+    std::unordered_map<void *, size_t> block_bytes;
+
     kcna_stats *stats = nullptr;
     double t0 = 0;
 
@@ -111,19 +120,27 @@ kcna_status kcna_cuda_check(kcna_ctx *c, cudaError_t e, const char *what);
 kcna_status kcna_check_device_err(kcna_ctx *c, const char *phase);
 kcna_status kcna_scratch(kcna_ctx *c, size_t bytes, void **out);
 kcna_status kcna_scratch2(kcna_ctx *c, size_t bytes, void **out);
+#define KCNA_TRY_ALLOC(x)                            \
+    do {                                             \
+        kcna_status _s = (x);                        \
+        if (_s != KCNA_OK) return _s;                \
+    } while (0)
+// Device memory through the context's cache (kcna_internal.h kcna_ctx::free_blocks).
+// All of a context's kernels run on its one stream, so a block released and
+// handed out again is ordered after every use of its previous owner.
+kcna_status kcna_dev_malloc(kcna_ctx *c, size_t bytes, void **out, const char *what);
+void kcna_release(kcna_ctx *c, void *p); // back to the cache; cudaFree for a block not from the cache
+void kcna_release_all(kcna_ctx *c);      // cudaFree of every cached block
 template <typename T>
 kcna_status kcna_alloc(kcna_ctx *c, T **p, size_t count, const char *what) {
     if (*p) {
-        cudaFree(*p);
+        kcna_release(c, *p);
         *p = nullptr;
     }
     if (count == 0) return KCNA_OK;
-    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        (void)cudaGetLastError();
-        return kcna_fail(c, KCNA_E_OOM, std::string("cudaMalloc failed for ") + what);
-    }
+    void *q = nullptr;
+    KCNA_TRY_ALLOC(kcna_dev_malloc(c, count * sizeof(T), &q, what));
+    *p = static_cast<T *>(q);
     return KCNA_OK;
 }
 #define KCNA_TRY(x)                                  \

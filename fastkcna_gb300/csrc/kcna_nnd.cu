@@ -1290,8 +1290,8 @@ kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl
     if (st == KCNA_OK) st = kcna_gather_rows(c, c->d_controls, C, rows);
     if (st == KCNA_OK) st = kcna_knn_device(c, rows, C, c->d_controls, maxl, c->d_control_knn, dd);
     if (st == KCNA_OK) st = kcna_phase_end(c, KCNA_PHASE_CONTROLS);
-    cudaFree(dd);
-    cudaFree(rows);
+    kcna_release(c, dd);
+    kcna_release(c, rows);
     return st;
 }
 

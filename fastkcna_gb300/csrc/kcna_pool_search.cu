@@ -215,7 +215,7 @@ kcna_status kcna_pool_search_run(kcna_ctx *c, const kcna_params *p, uint32_t max
         if (s == KCNA_OK)
             s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 24, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
         if (s == KCNA_OK) s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "pool search sync");
-        cudaFree(vis);
+        kcna_release(c, vis);
         if (s == KCNA_OK && comps) *comps = h;
         return s;
     };

@@ -450,7 +450,7 @@ struct Dev {
     kcna_ctx *c;
     std::vector<void *> bufs;
     ~Dev() {
-        for (void *b : bufs) cudaFree(b);
+        for (void *b : bufs) kcna_release(c, b);
     }
     template <typename T>
     kcna_status get(T **p, size_t n, const char *what) {
