@@ -523,7 +523,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--ref-budget", type=float, default=1200.0,
+    ap.add_argument("--ref-budget", type=float, default=600.0,
                     help="seconds of whole reference builds in --impl reference (at least one build)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="learned_bf16", choices=["learned_bf16", "plain"])

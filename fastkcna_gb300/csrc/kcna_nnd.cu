@@ -351,8 +351,10 @@ struct MergeArgs {
 // candidate slot (16 bits, CB <= 8192) and moves with its key through the
 // sort; before the survivors are deduplicated, each distinct survivor placed
 // at rank < K loads the joiners of its copies (MergeArgs.cand_src) and
-// credits the lowest.  Three blocks of eight warps still share an SM.
+// credits the lowest.  Three blocks of eight warps still share an SM; with
+// 1024 survivor slots a block has seven warps so that two blocks share one.
 constexpr int MW_WARPS = 8;
+__host__ __device__ constexpr int merge_warps(int surv, bool credit) { return surv == 1024 && credit ? 7 : MW_WARPS; }
 __host__ __device__ constexpr size_t merge_warp_bytes(uint32_t cap, int surv, bool credit) {
     return ((size_t)cap * 8 + (size_t)surv * 8 + 16 + (credit ? (size_t)surv * 2 : 0) + 15) & ~(size_t)15;
 }
@@ -371,7 +373,8 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
     if (threadIdx.x < 4) s_stat[threadIdx.x] = 0;
     __syncthreads();
-    for (uint32_t node = blockIdx.x * MW_WARPS + w; node < N; node += gridDim.x * MW_WARPS) {
+    constexpr int NW = merge_warps(SURV, CREDIT);
+    for (uint32_t node = blockIdx.x * NW + w; node < N; node += gridDim.x * NW) {
         const uint32_t raw = a.cand_cnt[node];
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
@@ -1178,20 +1181,21 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     const bool wide = c->merge_big_last > c->n / wide_div; // many nodes overflowed the survivor buffer last time
     const char *sv = getenv("KCNA_MERGE_SURV");   // tuning override: 512 or 1024
     const int surv = sv ? (atoi(sv) >= 1024 ? 1024 : 512) : wide ? 1024 : 512;
-    const size_t smw = merge_warp_bytes(c->cap, surv, credit_found) * MW_WARPS;
+    const int nw = merge_warps(surv, credit_found);
+    const size_t smw = merge_warp_bytes(c->cap, surv, credit_found) * nw;
     auto launch_warp = [&](auto kern) -> kcna_status {
         KCNA_TRY(kcna_cuda_check(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          (int)std::max<size_t>(smw, 48 * 1024)),
                                  "merge smem attr"));
         int mw_per_sm = 0;
-        KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mw_per_sm, kern, MW_WARPS * 32, smw),
+        KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mw_per_sm, kern, nw * 32, smw),
                                  "merge occupancy"));
         const uint32_t mw_grid = (uint32_t)std::min<uint64_t>(
-            kcna_div_up(c->n, MW_WARPS), (uint64_t)std::max(c->num_sms, 1) * std::max(mw_per_sm, 1));
+            kcna_div_up(c->n, nw), (uint64_t)std::max(c->num_sms, 1) * std::max(mw_per_sm, 1));
         KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters, 0, 10 * 8, c->stream), "memset"));
         KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->big_cnt, 0, 4, c->stream), "memset"));
         KCNA_TRY(kcna_phase_begin(c));
-        kern<<<mw_grid, MW_WARPS * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
+        kern<<<mw_grid, nw * 32, smw, c->stream>>>(a, c->n, c->big_list, c->big_cnt);
         return KCNA_OK;
     };
     // the template must match the shared memory sized above
