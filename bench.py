@@ -377,6 +377,116 @@ def run_search_sweep(args, local):
                       "start": "entry point + L-1 seeded random nodes"}), flush=True)
 
 
+C3_FLAGS = dict(K=200, L=200, S=10, R=100, iterations=6, search_L=40, nsg_R=40, search_K=200, massq_S=10,
+                loop_i=2, step=10)
+C4_FLAGS = dict(K=500, L=500, S=12, R=100, iterations=6, search_L=80, nsg_R=50, search_K=500, massq_S=10,
+                loop_i=2, step=10, tau=10.0)
+C5_FLAGS = dict(K=500, L=500, S=12, R=100, iterations=12, search_L=80, nsg_R=50, search_K=500, massq_S=10,
+                loop_i=2, step=10, angle=60.0, recall=0.99)
+
+
+def _recall10(found, truth):
+    return sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth)) / (10.0 * truth.shape[0])
+
+
+def _search_from_entry(ix, Q, truth, n, ep, L, labels=None):
+    rng = np.random.default_rng(7)
+    extra = rng.choice(n, size=L, replace=False)
+    start = np.concatenate([[ep], extra[extra != ep][: L - 1]]).astype(np.uint32)
+    found, _ = ix.search(Q, L, 10, init_ids=np.broadcast_to(start, (Q.shape[0], L)).copy())
+    if labels is not None:
+        found = labels[found]
+    return _recall10(found, truth)
+
+
+def run_workload(args, local):
+    """The other named workloads at full size, one JSON line each (not the
+    headline measurement): c3 = the layered FastHNSW command line on 1M x 96
+    unit rows, FP32 and BF16-screened; c4 = FastTauMNG on 1M x 960 (FP32
+    kernels); c5 = FastAlphaPG on 2M x 128 integer rows, learned+BF16 and
+    plain FP32.  Times are one build each after the data is on the device
+    (c3: the command line's own indexing time, file load excluded)."""
+    import tempfile
+
+    import torch
+
+    from fastkcna_gb300 import build as kbuild
+    from fastkcna_gb300 import index_io, kcna, synth
+
+    torch.cuda.set_device(local)
+    w = args.workload
+    out = {"workload": w}
+    if w == "c3":
+        X = synth.base("c3")
+        Q = synth.queries("c3", 10000)
+        with kcna.Index(local) as ix:
+            ix.upload(X)
+            truth, _ = ix.knn_queries(Q, 10)
+        td = tempfile.mkdtemp()
+        data = os.path.join(td, "c3.lshkit")
+        synth.write_lshkit(data, X)
+        flags = []
+        for k, v in C3_FLAGS.items():
+            flags += [f"--{k}" if len(k) > 1 else f"-{k}", str(v)]
+        flags = [f.replace("--iterations", "-I") for f in flags]
+        for screen in ("fp32", "bf16"):
+            path = os.path.join(td, f"c3_{screen}.bin")
+            t0 = time.perf_counter()
+            r = subprocess.run([os.path.join(kbuild.BIN, "fasthnsw"), data, path, "--result",
+                                os.path.join(td, f"c3_{screen}.csv"), "--screen", screen, *flags],
+                               capture_output=True, text=True, timeout=3000)
+            wall = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+            secs = [float(ln.split(":")[-1]) for ln in r.stdout.splitlines() if "indexing time" in ln]
+            idx = index_io.read_hnswlib(path)
+            labels = np.asarray(idx["labels"], np.uint32)
+            W = max(len(a) for a in idx["level0"])
+            g = np.full((X.shape[0], W), 0xFFFFFFFF, np.uint32)
+            deg = np.zeros(X.shape[0], np.uint32)
+            for i, a in enumerate(idx["level0"]):
+                g[i, : len(a)] = a
+                deg[i] = len(a)
+            with kcna.Index(local) as ix:
+                ix.upload(X[labels])
+                ep = int(idx["enterpoint"])
+                ix.set_graph(g, deg, ep)
+                rec = {L: round(_search_from_entry(ix, Q, truth, X.shape[0], ep, L, labels), 4) for L in (40, 100)}
+            out[screen] = {"indexing_s": secs[-1] if secs else None, "wall_s": round(wall, 2),
+                           "level0_avg_degree": round(float(deg.mean()), 2), "search_recall_at_10": rec}
+        out["flags"] = C3_FLAGS
+        out["search"] = "level-0 graph, beam L from the entry point + L-1 seeded random nodes, 10,000 queries"
+    elif w == "c4":
+        X = synth.base("c4")
+        Q = synth.queries("c4", 1000)
+        with kcna.Index(local) as ix:
+            ix.upload(X)
+            truth, _ = ix.knn_queries(Q, 10)
+            t0 = time.perf_counter()
+            st = ix.build("taumng", kcna.params(**C4_FLAGS))
+            wall = time.perf_counter() - t0
+            _, deg, ep = ix.graph()
+            rec = {L: round(_search_from_entry(ix, Q, truth, X.shape[0], ep, L), 4) for L in (80, 160)}
+        out.update(build_s=round(st["total_time"], 3), wall_s=round(wall, 3), phase_ms={k: round(v, 1) for k, v in
+                   st["phase_ms"].items() if v}, nndescent_iterations=st["iterations"],
+                   knn_recall_at_K=round(st["loop_recall"][-1], 4), n_comps=st["n_comps"],
+                   cand_emitted=st["cand_emitted"], prune_comps=st["prune_comps"], bridge_comps=st["bridge_comps"],
+                   avg_degree=st["aod"], search_recall_at_10=rec, flags=C4_FLAGS, mode="plain FP32")
+    elif w == "c5":
+        X = synth.base("c5")
+        with kcna.Index(local) as ix:
+            ix.upload(X)
+            for mode, extra in (("learned_bf16", dict(learned_seed=1, screen=1)), ("plain", {})):
+                st = ix.build("alphapg", kcna.params(**C5_FLAGS, **extra))
+                out[mode] = dict(build_s=round(st["total_time"], 3), iterations=st["iterations"],
+                                 iter_recall=[round(x, 4) for x in st["iter_recall"]],
+                                 knn_recall_at_K=round(st["loop_recall"][-1], 4),
+                                 phase_ms={k: round(v, 1) for k, v in st["phase_ms"].items() if v})
+        out["ratio"] = round(out["learned_bf16"]["build_s"] / out["plain"]["build_s"], 4)
+        out["flags"] = C5_FLAGS
+    print(json.dumps(out), flush=True)
+
+
 def run_gpu(args, ws, rank, local):
     import torch
 
@@ -527,11 +637,16 @@ def main():
                     help="seconds of whole reference builds in --impl reference (at least one build)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="learned_bf16", choices=["learned_bf16", "plain"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                    help="c2: the headline build benchmark; c3/c4/c5: one JSON line for that named workload")
     ap.add_argument("--search-sweep", action="store_true",
                     help="print the recall@10 / QPS curve of the query-time search instead of timing builds")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
-    if args.search_sweep:
+    if args.workload != "c2":
+        if rank == 0:
+            run_workload(args, local)
+    elif args.search_sweep:
         if rank == 0:
             run_search_sweep(args, local)
     elif args.impl == "reference":
