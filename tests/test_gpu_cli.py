@@ -18,7 +18,12 @@ from graph_search import beam_search, hnsw_search, seeded_entries
 pytestmark = pytest.mark.gpu
 
 GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_cli_c1.npz"))
-TOL = 0.01  # recall@10 below the reference's by at most this much
+TOL = 0.002  # recall@10 within this of the range the reference's own two builds span (1,000 queries)
+
+
+def _near_ref(rec, tag):
+    r = np.atleast_1d(GOLD[f"recall_{tag}"]).astype(np.float64)
+    return r.min() - TOL <= rec <= r.max() + TOL
 FLAGS = ["-K", "100", "-L", "100", "-S", "10", "-R", "100", "-I", "6", "--search_L", "40", "--nsg_R", "32",
          "--search_K", "100", "--massq_S", "10", "--angle", "60", "--tau", "0.1"]
 
@@ -49,7 +54,7 @@ def _nsg_recall(path, X, Q, truth, ef=60):
 @pytest.fixture(scope="module")
 def c1_files():
     X = synth.base("c1", 20000)
-    Q = synth.queries("c1", 200)
+    Q = synth.queries("c1", int(GOLD["nq"]) if "nq" in GOLD.files else 1000)
     td = tempfile.mkdtemp()
     path = os.path.join(td, "c1.lshkit")
     synth.write_lshkit(path, X)
@@ -66,7 +71,7 @@ def test_cli_nsg_family(c1_files, tool):
     csv = open(res).read()
     assert csv.startswith("PG_type,K,L,S,R,I,searchL,searchK,nsgR,massqS,tau,angle,step")
     assert "con time" in csv and "AOD" in csv
-    assert rec >= float(GOLD[f"recall_{tool[4:]}"]) - TOL, (rec, float(GOLD[f"recall_{tool[4:]}"]))
+    assert _near_ref(rec, tool[4:]), (rec, GOLD[f"recall_{tool[4:]}"])
     assert rec >= 0.9
 
 
@@ -96,7 +101,7 @@ def test_cli_hnsw(c1_files, tool):
         assert np.array_equal(idx["labels"].astype(np.int64), d2f.astype(np.int64))
         assert idx["maxlevel"] == len(pn) - 1 == int(GOLD["maxlevel_hnsw"])
         assert np.array_equal(idx["levels"], np.repeat(np.arange(len(pn) - 1, -1, -1), pn[::-1]))
-    assert rec >= float(GOLD[f"recall_{tag}"]) - TOL, (rec, float(GOLD[f"recall_{tag}"]))
+    assert _near_ref(rec, tag), (rec, GOLD[f"recall_{tag}"])
 
 
 def test_cli_nsg_with_pool_search_refinement(c1_files):
@@ -106,4 +111,4 @@ def test_cli_nsg_with_pool_search_refinement(c1_files):
     out = os.path.join(td, "pool.nsg")
     _run("fastnsg", data, out, "--result", os.path.join(td, "pool.csv"), "--refine", "pool", *FLAGS)
     rec, _, _ = _nsg_recall(out, X, Q, truth)
-    assert rec >= float(GOLD["recall_nsg"]) - TOL, (rec, float(GOLD["recall_nsg"]))
+    assert _near_ref(rec, "nsg"), (rec, GOLD["recall_nsg"])

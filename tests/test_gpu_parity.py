@@ -130,8 +130,8 @@ def test_nndescent_recall_matches_oracle(index, oracle):
     _, _, _, ost = oracle.nndescent(X, oracle_py.params(**kw), nthreads=8)
     g = st["loop_recall"][0]
     o = ost.loop_recall[0]
-    # stochastic path: the GPU's batched joins must not lose recall against the reference loop
-    assert g >= o - 0.01, (g, o, st)
+    # stochastic path: control recall on the same control nodes within 0.002 either way
+    assert abs(g - o) <= 0.002, (g, o, st)
     # exact recall on a subset, independent of the control estimator
     pid, pd, pc = index.pools()
     ids = np.arange(0, X.shape[0], 200, dtype=np.uint32)
@@ -148,7 +148,7 @@ def test_nndescent_recall_matches_oracle(index, oracle):
 @pytest.mark.parametrize("kind", ["nsg", "taumng", "alphapg"])
 def test_build_search_recall(index, oracle, kind):
     X = synth.base("c1", 20000)
-    Q = synth.queries("c1", 500)
+    Q = synth.queries("c1", 2000)
     kw = dict(K=100, L=100, S=10, R=100, iterations=6, search_L=40, nsg_R=32, search_K=100, massq_S=10,
               angle=60.0, tau=0.05, loop_i=2)
     index.upload(X)
@@ -178,4 +178,4 @@ def test_build_search_recall(index, oracle, kind):
     index.set_graph(og, odeg, ost.ep)
     oi, _ = index.search(Q, 64, 10)
     r_orc = recall_at(oi, truth, 10)
-    assert r_gpu >= r_orc - 0.01, (r_gpu, r_orc, st)
+    assert abs(r_gpu - r_orc) <= 0.002, (r_gpu, r_orc, st)
