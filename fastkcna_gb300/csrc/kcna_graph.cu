@@ -677,7 +677,12 @@ __global__ void bfs_expand_kernel(const uint32_t *__restrict__ g_ids, const uint
 // are cycles) the nodes whose id is below all their unreached out-neighbours
 // are used.  The attach point is the reference's rule: the first pool entry
 // of u that is reached and has degree < nsg_R, else a random reached node with
-// degree < nsg_R * factor; slots are reserved with atomicAdd on the degree.
+// degree < nsg_R * factor (factor grows when every reached node has reached
+// the bound); slots are reserved with atomicAdd on the degree.  The random
+// pick draws from a list of the reached nodes below the bound, rebuilt each
+// round (collect_open_kernel), in place of the reference's retries over all
+// ids; a node's degree is capped at the graph width W (nsg_R + 8), where the
+// reference's list can grow without bound.
 __global__ void mark_targets_kernel(const uint32_t *__restrict__ g_ids, const uint32_t *__restrict__ g_deg,
                                     uint32_t W, uint32_t N, const uint32_t *__restrict__ visited,
                                     uint32_t *__restrict__ targeted, uint32_t *__restrict__ localmin,
@@ -701,6 +706,19 @@ __global__ void mark_targets_kernel(const uint32_t *__restrict__ g_ids, const ui
     }
 }
 
+// Reached nodes whose degree is below `limit` (and the width), appended to
+// `open` (order irrelevant: picks are random).
+__global__ void collect_open_kernel(const uint32_t *__restrict__ visited, const uint32_t *__restrict__ g_deg, uint32_t N,
+                                    uint32_t limit, uint32_t W, uint32_t *__restrict__ open, uint32_t *__restrict__ n_open) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = u < N && ((visited[u >> 5] >> (u & 31)) & 1u) && g_deg[u] < limit && g_deg[u] < W;
+    const unsigned m = __ballot_sync(KCNA_FULL, ok);
+    uint32_t base = 0;
+    if (kcna_lane() == 0 && m) base = atomicAdd(n_open, (uint32_t)__popc(m));
+    base = __shfl_sync(KCNA_FULL, base, 0);
+    if (ok) open[base + __popc(m & kcna_lanemask_lt())] = u;
+}
+
 __device__ __forceinline__ bool reserve_slot(uint32_t *g_deg, uint32_t r, uint32_t limit, uint32_t W, uint32_t *slot) {
     const uint32_t old = atomicAdd(g_deg + r, 1u);
     if (old < limit && old < W) {
@@ -717,6 +735,7 @@ __global__ void attach_sources_kernel(const float *__restrict__ X, int ld, uint3
                                       uint32_t *__restrict__ g_deg, uint32_t W, uint32_t nsg_R,
                                       const uint32_t *__restrict__ visited, const uint32_t *__restrict__ pick,
                                       uint32_t *__restrict__ frontier, uint32_t *__restrict__ nfront, uint64_t seed,
+                                      const uint32_t *__restrict__ open, uint32_t n_open, uint32_t open_limit,
                                       int *err, unsigned long long *attached) {
     const uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = kcna_lane();
@@ -744,17 +763,17 @@ __global__ void attach_sources_kernel(const float *__restrict__ X, int ld, uint3
             }
         }
     }
-    if (root == KCNA_NONE && lane == 0) { // random reached node, src/kgraph.cpp:2216-2230
-        for (uint64_t t = 1; t <= 64ull * N + 64; ++t) {
-            const uint32_t factor = (uint32_t)(t / N) + 1;
-            const uint32_t rid = kcna_rand32(seed, u, t) % N;
-            if (((visited[rid >> 5] >> (rid & 31)) & 1u) && g_deg[rid] < nsg_R * factor &&
-                reserve_slot(g_deg, rid, nsg_R * factor, W, &slot)) {
-                root = rid;
-                break;
-            }
+    if (root == KCNA_NONE && lane == 0 && n_open > 0) { // random reached node, src/kgraph.cpp:2216-2230
+        for (uint32_t t = 0; t < 64 && root == KCNA_NONE; ++t) {
+            const uint32_t rid = open[kcna_rand32(seed, u, t) % n_open];
+            if (reserve_slot(g_deg, rid, open_limit, W, &slot)) root = rid;
         }
-        if (root == KCNA_NONE) kcna_set_err(err, KCNA_DERR_SPIN);
+        // the list's nodes may have been filled by other attaches of this round: walk it once
+        const uint32_t o = kcna_rand32(seed, u, 64) % n_open;
+        for (uint32_t t = 0; t < n_open && root == KCNA_NONE; ++t) {
+            const uint32_t rid = open[(o + t) % n_open];
+            if (reserve_slot(g_deg, rid, open_limit, W, &slot)) root = rid;
+        }
     }
     if (lane == 0 && root != KCNA_NONE) {
         g_ids[(uint64_t)root * W + slot] = u;
@@ -1318,11 +1337,24 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
         // sources: unreached and not targeted (pick = ~targeted); none left -> local minima
         invert_kernel<<<kcna_div_up(words, 256), 256, 0, c->stream>>>(targeted, words);
         KCNA_LAUNCHED(c);
+        // reached nodes open for a random attach: below nsg_R, else below the width
+        uint32_t n_open = 0, open_limit = p->nsg_R;
+        for (int lim = 0; lim < 2 && n_open == 0; ++lim) {
+            open_limit = lim == 0 ? p->nsg_R : c->W;
+            cudaMemsetAsync(cntd, 0, 4, c->stream);
+            collect_open_kernel<<<kcna_div_up(N, 256), 256, 0, c->stream>>>(vis, c->g_deg, N, open_limit, c->W, qb,
+                                                                             cntd);
+            KCNA_LAUNCHED(c);
+            cudaMemcpyAsync(&n_open, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "open list")) != KCNA_OK)
+                return cleanup2(), cleanup(), s;
+        }
         for (int pass = 0; pass < 2; ++pass) {
             cudaMemsetAsync(cntd, 0, 4, c->stream);
             attach_sources_kernel<<<wblocks, 256, 0, c->stream>>>(
                 c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist, c->g_deg, c->W, p->nsg_R, vis,
-                pass == 0 ? targeted : localmin, qa, cntd, seed + round * 2 + pass, c->d_err, c->counters + 18);
+                pass == 0 ? targeted : localmin, qa, cntd, seed + round * 2 + pass, qb, n_open, open_limit, c->d_err,
+                c->counters + 18);
             KCNA_LAUNCHED(c);
             cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
             if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach")) != KCNA_OK)
