@@ -416,8 +416,10 @@ def run_workload(args, local):
     torch.cuda.set_device(local)
     w = args.workload
     out = {"workload": w}
+    size = None if args.n == 1_000_000 else args.n  # --n scales c3 / c4 / c5 down (profiling cases)
+    out["n"] = size or {"c3": 1_000_000, "c4": 1_000_000, "c5": 2_000_000}[w]
     if w == "c3":
-        X = synth.base("c3")
+        X = synth.base("c3", size)
         Q = synth.queries("c3", 10000)
         with kcna.Index(local) as ix:
             ix.upload(X)
@@ -457,7 +459,7 @@ def run_workload(args, local):
         out["flags"] = C3_FLAGS
         out["search"] = "level-0 graph, beam L from the entry point + L-1 seeded random nodes, 10,000 queries"
     elif w == "c4":
-        X = synth.base("c4")
+        X = synth.base("c4", size)
         Q = synth.queries("c4", 1000)
         with kcna.Index(local) as ix:
             ix.upload(X)
@@ -473,7 +475,7 @@ def run_workload(args, local):
                    cand_emitted=st["cand_emitted"], prune_comps=st["prune_comps"], bridge_comps=st["bridge_comps"],
                    avg_degree=st["aod"], search_recall_at_10=rec, flags=C4_FLAGS, mode="plain FP32")
     elif w == "c5":
-        X = synth.base("c5")
+        X = synth.base("c5", size)
         with kcna.Index(local) as ix:
             ix.upload(X)
             for mode, extra in (("learned_bf16", dict(learned_seed=1, screen=1)), ("plain", {})):
