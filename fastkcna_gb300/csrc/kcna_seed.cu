@@ -732,11 +732,7 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
 // M = S and found = 1 for every node, so that the first update samples the
 // S nearest pool entries as the new list (the reference's init sets M = S).
 kcna_status kcna_seed_finish(kcna_ctx *c, const kcna_params *p) {
-    // the sample window M of the first update (the reference starts at S); the
-    // seeded pools are full, so a wider first window samples more of them
-    const char *ms = getenv("KCNA_SEED_M");
-    const uint32_t M0 = ms ? std::min<uint32_t>(std::max(atoi(ms), 1), p->L) : p->S;
-    fill_u32_kernel<<<kcna_div_up(c->n, 256), 256, 0, c->stream>>>(c->M, M0, c->n);
+    fill_u32_kernel<<<kcna_div_up(c->n, 256), 256, 0, c->stream>>>(c->M, p->S, c->n);
     cudaMemsetAsync(c->found, 1, c->n, c->stream);
     KCNA_TRY(launch_ok(c, "seed finish"));
     c->has_pools = true;
