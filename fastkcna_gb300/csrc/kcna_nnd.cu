@@ -382,11 +382,6 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
 #pragma unroll 4
         for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
-        __syncwarp();
-        // the pool's 32 segment fences in registers: each search touches shared
-        // memory only inside one segment of G keys
-        const int G = np <= 512 ? 16 : 32;
-        const uint64_t fence = kcna_fence_of(s_pool, (int)np, G);
         // candidates in groups of 128 (four per lane), the next group's loads in
         // flight while this group is searched
         constexpr int CG = 4;
@@ -412,9 +407,10 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 const uint32_t j = b0 + 32 * u + lane;
                 bool surv = false;
                 const uint64_t k = kcna_key_noflags(cur[u]);
-                const int b = kcna_fenced_lower_bound(s_pool, (int)np, k, fence, G); // all lanes (shuffles)
-                if (j < nc && k != KCNA_EMPTY_KEY_NOFLAGS)
+                if (j < nc && k != KCNA_EMPTY_KEY_NOFLAGS) {
+                    const int b = kcna_lower_bound(s_pool, (int)np, k);
                     surv = (uint32_t)b < a.limit && !(b < (int)np && (s_pool[b] >> 2) == (k >> 2));
+                }
                 const unsigned m = __ballot_sync(KCNA_FULL, surv);
                 const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
                 if (surv && pos < (uint32_t)SURV) {

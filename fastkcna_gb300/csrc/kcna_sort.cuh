@@ -136,41 +136,6 @@ __device__ __forceinline__ int kcna_lower_bound(const uint64_t *a, int na, uint6
     }
     return lo;
 }
-// Lower bound in sorted a[0..na) through per-lane fences: lane l holds the
-// largest key of segment l, a[l*G .. l*G+G) (UINT64_MAX for an empty segment),
-// G a power of two with 32 * G >= na.  The segment comes from a binary search
-// over the fences by warp shuffles (no shared-memory traffic), then log2(G)
-// steps inside it.  Every lane of the warp must call it (the shuffles); each
-// lane's own key.
-__device__ __forceinline__ uint64_t kcna_fence_of(const uint64_t *a, int na, int G) {
-    const int lane = threadIdx.x & 31;
-    const int last = min(lane * G + G, na) - 1;
-    return lane * G < na ? a[last] : 0xFFFFFFFFFFFFFFFFull;
-}
-__device__ __forceinline__ int kcna_fenced_lower_bound(const uint64_t *a, int na, uint64_t key, uint64_t fence, int G) {
-    int lo = 0, hi = 32; // first segment whose fence >= key: 33 answers, six halvings
-#pragma unroll
-    for (int step = 0; step < 6; ++step) {
-        const int mid = (lo + hi) >> 1;
-        const uint64_t f = __shfl_sync(0xFFFFFFFFu, fence, min(mid, 31));
-        if (lo < hi) {
-            if (f < key)
-                lo = mid + 1;
-            else
-                hi = mid;
-        }
-    }
-    int b = lo * G, e = min(b + G, na);
-    if (b >= na) return na;
-    while (b < e) {
-        const int mid = (b + e) >> 1;
-        if (a[mid] < key)
-            b = mid + 1;
-        else
-            e = mid;
-    }
-    return b;
-}
 __device__ __forceinline__ int kcna_upper_bound(const uint64_t *a, int na, uint64_t key) {
     int lo = 0, hi = na;
     while (lo < hi) {
