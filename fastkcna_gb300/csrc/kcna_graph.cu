@@ -675,10 +675,15 @@ __global__ void bfs_expand_kernel(const uint32_t *__restrict__ g_ids, const uint
 // an unreached node is a source when no unreached node has an edge to it
 // (mark_targets_kernel); when every unreached node has such an edge (the rest
 // are cycles) the nodes whose id is below all their unreached out-neighbours
-// are used.  The attach point is the reference's rule: the first pool entry
-// of u that is reached and has degree < nsg_R, else a random reached node with
-// degree < nsg_R * factor (factor grows when every reached node has reached
-// the bound); slots are reserved with atomicAdd on the degree.  The random
+// are used.  The attach point is the reference's rule as it runs: findroot
+// scans `nhoods[id].pool` with an `id` read in its own initialiser
+// (src/kgraph.cpp:2207), which the reference's builds evaluate as 0, so the
+// root is the first entry of node 0's pool (over the first pool_cnt[u]
+// positions) that is reached and has degree < nsg_R, else a random reached
+// node with degree < nsg_R * factor (factor grows when every reached node has
+// reached the bound); slots are reserved with atomicAdd on the degree.  As in
+// the reference, whose first findroot takes the smallest unreached id, node 0
+// is attached first when the entry point does not reach it.  The random
 // pick draws from a list of the reached nodes below the bound, rebuilt each
 // round (collect_open_kernel), in place of the reference's retries over all
 // ids; a node's degree is capped at the graph width W (nsg_R + 8), where the
@@ -741,12 +746,12 @@ __global__ void attach_sources_kernel(const float *__restrict__ X, int ld, uint3
     const int lane = kcna_lane();
     if (u >= N || ((visited[u >> 5] >> (u & 31)) & 1u) || !((pick[u >> 5] >> (u & 31)) & 1u)) return;
     uint32_t root = KCNA_NONE, slot = 0;
-    const uint32_t cnt = min(pool_cnt[u], cap);
+    const uint32_t cnt = min(min(pool_cnt[u], pool_cnt[0]), cap);
     for (uint32_t b0 = 0; b0 < cnt && root == KCNA_NONE; b0 += 32) {
         const uint32_t i = b0 + lane;
         uint32_t cid = KCNA_NONE;
         if (i < cnt) {
-            cid = kcna_key_id(pool[(uint64_t)u * cap + i]);
+            cid = kcna_key_id(pool[i]); // node 0's pool
             if (!(cid < N && ((visited[cid >> 5] >> (cid & 31)) & 1u) && g_deg[cid] < nsg_R)) cid = KCNA_NONE;
         }
         unsigned mk = __ballot_sync(KCNA_FULL, cid != KCNA_NONE);
@@ -1286,42 +1291,82 @@ kcna_status kcna_compute_ep(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
 
 kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
     const uint32_t N = c->n, words = (N + 31) / 32;
-    uint32_t *vis = nullptr, *qa = nullptr, *qb = nullptr, *cntd = nullptr;
+    uint32_t *vis = nullptr, *qa = nullptr, *qb = nullptr, *cntd = nullptr, *targeted = nullptr, *localmin = nullptr;
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
         kcna_release(c, vis);
         kcna_release(c, qa);
         kcna_release(c, qb);
         kcna_release(c, cntd);
+        kcna_release(c, targeted);
+        kcna_release(c, localmin);
     };
     if ((s = kcna_alloc(c, &vis, words, "visited")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &qa, N, "frontier")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &qb, N, "frontier")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cntd, 1, "count")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &targeted, words, "marks")) != KCNA_OK) return cleanup(), s;
+    if ((s = kcna_alloc(c, &localmin, words, "marks")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
-    cudaMemsetAsync(vis, 0, (size_t)words * 4, c->stream);
-    uint32_t ep = c->ep, bit = 1u << (ep & 31);
-    cudaMemcpyAsync(vis + (ep >> 5), &bit, 4, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(qa, &ep, 4, cudaMemcpyHostToDevice, c->stream);
-    uint32_t nf = 1;
-    for (uint32_t level = 0; nf > 0 && level < N; ++level) {
+    // BFS levels from the nf nodes in qa (already marked reached)
+    auto bfs = [&](uint32_t nf) -> kcna_status {
+        for (uint32_t level = 0; nf > 0 && level < N; ++level) {
+            cudaMemsetAsync(cntd, 0, 4, c->stream);
+            bfs_expand_kernel<<<kcna_div_up((uint64_t)nf * 32, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W,
+                                                                                          N, qa, nf, vis, qb, cntd);
+            KCNA_LAUNCHED(c);
+            cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+            KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs"));
+            std::swap(qa, qb);
+        }
+        return KCNA_OK;
+    };
+    // reached nodes open for a random attach (list in qb): below nsg_R, else below the width
+    auto open_list = [&](uint32_t &n_open, uint32_t &open_limit) -> kcna_status {
+        n_open = 0;
+        for (int lim = 0; lim < 2 && n_open == 0; ++lim) {
+            open_limit = lim == 0 ? p->nsg_R : c->W;
+            cudaMemsetAsync(cntd, 0, 4, c->stream);
+            collect_open_kernel<<<kcna_div_up(N, 256), 256, 0, c->stream>>>(vis, c->g_deg, N, open_limit, c->W, qb,
+                                                                             cntd);
+            KCNA_LAUNCHED(c);
+            cudaMemcpyAsync(&n_open, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
+            KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "open list"));
+        }
+        return KCNA_OK;
+    };
+    // attaches the unreached nodes marked in `pick`; the attached ones go to qa, their count to nf
+    const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    auto attach = [&](const uint32_t *pick, uint64_t sd, uint32_t n_open, uint32_t open_limit,
+                      uint32_t &nf) -> kcna_status {
         cudaMemsetAsync(cntd, 0, 4, c->stream);
-        bfs_expand_kernel<<<kcna_div_up((uint64_t)nf * 32, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W, N, qa,
-                                                                                      nf, vis, qb, cntd);
+        attach_sources_kernel<<<wblocks, 256, 0, c->stream>>>(
+            c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist, c->g_deg, c->W, p->nsg_R, vis,
+            pick, qa, cntd, sd, qb, n_open, open_limit, c->d_err, c->counters + 18);
         KCNA_LAUNCHED(c);
         cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
-        if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs")) != KCNA_OK) return cleanup(), s;
-        std::swap(qa, qb);
-    }
-    cudaMemsetAsync(c->counters + 18, 0, 16, c->stream);
-    uint32_t *targeted = nullptr, *localmin = nullptr;
-    auto cleanup2 = [&]() {
-        kcna_release(c, targeted);
-        kcna_release(c, localmin);
+        KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach"));
+        if (nf > 0) {
+            mark_frontier_kernel<<<kcna_div_up(nf, 256), 256, 0, c->stream>>>(qa, nf, vis);
+            KCNA_LAUNCHED(c);
+        }
+        return KCNA_OK;
     };
-    if ((s = kcna_alloc(c, &targeted, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
-    if ((s = kcna_alloc(c, &localmin, words, "marks")) != KCNA_OK) return cleanup2(), cleanup(), s;
-    const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    cudaMemsetAsync(vis, 0, (size_t)words * 4, c->stream);
+    cudaMemsetAsync(c->counters + 18, 0, 16, c->stream);
+    const uint32_t ep = c->ep, bit = 1u << (ep & 31), node0 = 1u;
+    cudaMemcpyAsync(vis + (ep >> 5), &bit, 4, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(qa, &ep, 4, cudaMemcpyHostToDevice, c->stream);
+    if ((s = bfs(1)) != KCNA_OK) return cleanup(), s;
+    {   // node 0 first when the entry point does not reach it (attach skips a reached node)
+        uint32_t n_open = 0, open_limit = p->nsg_R, nf = 0;
+        cudaMemsetAsync(targeted, 0, (size_t)words * 4, c->stream);
+        cudaMemcpyAsync(targeted, &node0, 4, cudaMemcpyHostToDevice, c->stream);
+        if ((s = open_list(n_open, open_limit)) != KCNA_OK) return cleanup(), s;
+        if ((s = attach(targeted, seed ^ 0x9E3779B97F4A7C15ull, n_open, open_limit, nf)) != KCNA_OK)
+            return cleanup(), s;
+        if ((s = bfs(nf)) != KCNA_OK) return cleanup(), s;
+    }
     for (uint32_t round = 0; round < N; ++round) {
         cudaMemsetAsync(targeted, 0, (size_t)words * 4, c->stream);
         cudaMemsetAsync(localmin, 0, (size_t)words * 4, c->stream);
@@ -1332,54 +1377,23 @@ kcna_status kcna_tree_grow(kcna_ctx *c, const kcna_params *p, uint64_t seed) {
         unsigned long long unreached = 0;
         cudaMemcpyAsync(&unreached, c->counters + 19, 8, cudaMemcpyDeviceToHost, c->stream);
         if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "tree marks")) != KCNA_OK)
-            return cleanup2(), cleanup(), s;
+            return cleanup(), s;
         if (unreached == 0) break;
         // sources: unreached and not targeted (pick = ~targeted); none left -> local minima
         invert_kernel<<<kcna_div_up(words, 256), 256, 0, c->stream>>>(targeted, words);
         KCNA_LAUNCHED(c);
-        // reached nodes open for a random attach: below nsg_R, else below the width
-        uint32_t n_open = 0, open_limit = p->nsg_R;
-        for (int lim = 0; lim < 2 && n_open == 0; ++lim) {
-            open_limit = lim == 0 ? p->nsg_R : c->W;
-            cudaMemsetAsync(cntd, 0, 4, c->stream);
-            collect_open_kernel<<<kcna_div_up(N, 256), 256, 0, c->stream>>>(vis, c->g_deg, N, open_limit, c->W, qb,
-                                                                             cntd);
-            KCNA_LAUNCHED(c);
-            cudaMemcpyAsync(&n_open, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
-            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "open list")) != KCNA_OK)
-                return cleanup2(), cleanup(), s;
-        }
-        for (int pass = 0; pass < 2; ++pass) {
-            cudaMemsetAsync(cntd, 0, 4, c->stream);
-            attach_sources_kernel<<<wblocks, 256, 0, c->stream>>>(
-                c->X, (int)c->ld, N, c->pool, c->pool_cnt, c->cap, c->g_ids, c->g_dist, c->g_deg, c->W, p->nsg_R, vis,
-                pass == 0 ? targeted : localmin, qa, cntd, seed + round * 2 + pass, qb, n_open, open_limit, c->d_err,
-                c->counters + 18);
-            KCNA_LAUNCHED(c);
-            cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
-            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "attach")) != KCNA_OK)
-                return cleanup2(), cleanup(), s;
-            if (nf > 0) break;
-        }
+        uint32_t n_open = 0, open_limit = p->nsg_R, nf = 0;
+        if ((s = open_list(n_open, open_limit)) != KCNA_OK) return cleanup(), s;
+        for (int pass = 0; pass < 2 && nf == 0; ++pass)
+            if ((s = attach(pass == 0 ? targeted : localmin, seed + round * 2 + pass, n_open, open_limit, nf)) !=
+                KCNA_OK)
+                return cleanup(), s;
         if (nf == 0) {
             s = kcna_fail(c, KCNA_E_CUDA, "tree_grow: no attach point for an unreached node");
-            return cleanup2(), cleanup(), s;
+            return cleanup(), s;
         }
-        // mark the attached sources and BFS from them
-        mark_frontier_kernel<<<kcna_div_up(nf, 256), 256, 0, c->stream>>>(qa, nf, vis);
-        KCNA_LAUNCHED(c);
-        for (uint32_t level = 0; nf > 0 && level < N; ++level) {
-            cudaMemsetAsync(cntd, 0, 4, c->stream);
-            bfs_expand_kernel<<<kcna_div_up((uint64_t)nf * 32, 256), 256, 0, c->stream>>>(c->g_ids, c->g_deg, c->W,
-                                                                                          N, qa, nf, vis, qb, cntd);
-            KCNA_LAUNCHED(c);
-            cudaMemcpyAsync(&nf, cntd, 4, cudaMemcpyDeviceToHost, c->stream);
-            if ((s = kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bfs")) != KCNA_OK)
-                return cleanup2(), cleanup(), s;
-            std::swap(qa, qb);
-        }
+        if ((s = bfs(nf)) != KCNA_OK) return cleanup(), s;
     }
-    cleanup2();
     s = kcna_cuda_check(c, cudaGetLastError(), "attach");
     if (s == KCNA_OK) s = kcna_phase_end(c, KCNA_PHASE_TREE);
     unsigned long long att = 0;

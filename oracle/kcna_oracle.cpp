@@ -21,8 +21,10 @@
 // Two more points where the reference is ill-defined and this file states a
 // choice:
 //  * findroot (src/kgraph.cpp:2203-2214) declares an inner `id` initialised from
-//    itself (undefined behaviour); the intended meaning, scanning the pool of
-//    the unreached node, is implemented.
+//    itself (undefined behaviour).  The reference's builds evaluate that read
+//    as 0 (with -ftrivial-auto-var-init=zero, and likewise with plain -O3 on
+//    x86-64: the links between C2 clusters then start in node 0's cluster),
+//    so node 0's pool is scanned here too.
 //  * InterInsert (src/kgraph.cpp:2051-2084) runs under OpenMP with the order
 //    of appended reverse edges set by thread timing; here (and on the GPU) the
 //    reverse edges of a node are appended in increasing source id, and the
@@ -785,7 +787,8 @@ struct Builder {
         }
     }
 
-    // src/kgraph.cpp:2174-2236 (findroot), pool scan of the unreached node.
+    // src/kgraph.cpp:2174-2236 (findroot): node 0's pool is scanned over the
+    // unreached node's pool length (the self-initialised `id` read as 0).
     void findroot(std::vector<uint8_t> &flag, unsigned &root, unsigned &start, std::mt19937 &rng) {
         unsigned nd = D.n, id = nd;
         for (unsigned i = start; i < nd; i++)
@@ -797,7 +800,8 @@ struct Builder {
         if (id == nd) return;
         bool found = false;
         for (unsigned i = 0; i < nh[id].L; i++) {
-            unsigned cand = nh[id].pool[i].id;
+            if (i >= nh[0].pool.size()) break;
+            unsigned cand = nh[0].pool[i].id;
             if (cand < nd && flag[cand] && nh[cand].nn_nsg.size() < P.nsg_R) {
                 root = cand;
                 found = true;
