@@ -24,13 +24,13 @@ One measure is held to a wider bar, for a stated reason: search recall at
 200,000 rows.  There each of the 256 clusters holds more rows than K = 500,
 so the K-NN graph falls apart into one island per cluster and a beam reaches
 the query's cluster only through a start node inside it or through the links
-tree_grow adds between islands.  Those links are where the two builds differ
-by design: the GPU attaches an unreached node to the nearest reached member
-of its pool, the reference to a reached member of node 0's pool (its
-findroot reads an uninitialised variable, src/kgraph.cpp:2207; see
-oracle/build_ref.sh) or a random reached node.  Search recall at 200,000
-rows is held within 0.015 of the reference's builds; at 100,000 rows, where
-pools span clusters and the graph is one piece, within 0.002.
+tree_grow adds between islands.  Both builds add those links the same way
+(from node 0's pool: the reference's findroot reads its self-initialised id
+as 0, src/kgraph.cpp:2207), but which nodes they join is random, and two GPU
+builds with different seeds differ by up to 0.0032 in search recall there
+(measured at beams 20 and 80).  Search recall at 200,000 rows is held within
+0.005 of the reference's builds; at 100,000 rows, where pools span clusters
+and the graph is one piece, within 0.002.
 """
 import os
 
@@ -46,7 +46,7 @@ GOLD = np.load(os.path.join(HERE, "golden", "ref_quality_c2.npz"))
 FLAGS = dict(K=500, L=500, S=12, R=100, iterations=12, search_L=80, nsg_R=50, search_K=500, massq_S=10,
              loop_i=2, step=10, angle=60.0, recall=0.99, controls=100, seed=2024)
 TOL = 0.002
-ISLAND_TOL = 0.015  # search recall where the graph is one island per cluster (200,000 rows)
+ISLAND_TOL = 0.005  # search recall where the graph is one island per cluster (200,000 rows)
 
 
 def _within(value, refs, tol=TOL):
