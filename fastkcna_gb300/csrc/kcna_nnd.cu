@@ -335,15 +335,12 @@ struct MergeArgs {
     uint32_t n_nodes;
 };
 
-// Warp-per-node merge, survivors first.  A candidate whose id is in the
-// node's pool (a hash table of the pool's ids in shared memory, one or two
-// probes), or which would land at rank >= limit (one comparison with the
-// pool's last key when the pool is full), is dropped.  An id always comes with
-// the same distance to the node, so an id match is a key match.  In a
+// Warp-per-node merge, survivors first.  Every candidate is looked up in the
+// node's sorted pool by binary search (shared memory): a candidate equal to a
+// pool entry, or one that would land at rank >= limit, is dropped.  In a
 // converging NN-descent almost every candidate is such a repeat, so only the
-// few survivors are sorted, deduplicated and merged (against a copy of the
-// pool loaded over the table), and only the pool entries they displace are
-// written.  A node with more than SURV survivors is
+// few survivors are sorted, deduplicated and merged, and only the pool entries
+// they displace are written.  A node with more than SURV survivors is
 // queued for the block merge (merge_kernel).  Same result as merging all
 // candidates.  Persistent: each warp takes nodes grid-stride, so a block
 // meets its barrier once at the end instead of waiting for its slowest node.
@@ -358,37 +355,8 @@ struct MergeArgs {
 // 1024 survivor slots a block has seven warps so that two blocks share one.
 constexpr int MW_WARPS = 8;
 __host__ __device__ constexpr int merge_warps(int surv, bool credit) { return surv == 1024 && credit ? 7 : MW_WARPS; }
-// slots of the pool-id hash table: a power of two >= 2 cap (load <= 1/2)
-__host__ __device__ constexpr uint32_t merge_hash_slots(uint32_t cap) {
-    uint32_t h = 64;
-    while (h < 2 * cap) h <<= 1;
-    return h;
-}
-// the pool copy and the hash table share the first region
-__host__ __device__ constexpr size_t merge_pool_bytes(uint32_t cap) {
-    return ((size_t)cap * 8 > (size_t)merge_hash_slots(cap) * 4 ? (size_t)cap * 8 : (size_t)merge_hash_slots(cap) * 4);
-}
 __host__ __device__ constexpr size_t merge_warp_bytes(uint32_t cap, int surv, bool credit) {
-    return (merge_pool_bytes(cap) + (size_t)surv * 8 + 16 + (credit ? (size_t)surv * 2 : 0) + 15) & ~(size_t)15;
-}
-constexpr uint32_t HASH_EMPTY = 0xFFFFFFFFu;
-__device__ __forceinline__ uint32_t merge_hash(uint32_t id, uint32_t mask) { return (id * 0x9E3779B1u >> 7) & mask; }
-// ids are distinct: a slot is free or holds another id
-__device__ __forceinline__ void merge_hash_insert(uint32_t *t, uint32_t mask, uint32_t id) {
-    uint32_t h = merge_hash(id, mask);
-    for (uint32_t n = 0; n <= mask; ++n, h = (h + 1u) & mask) {
-        const uint32_t old = atomicCAS(t + h, HASH_EMPTY, id);
-        if (old == HASH_EMPTY || old == id) return;
-    }
-}
-__device__ __forceinline__ bool merge_hash_has(const uint32_t *t, uint32_t mask, uint32_t id) {
-    uint32_t h = merge_hash(id, mask);
-    for (uint32_t n = 0; n <= mask; ++n, h = (h + 1u) & mask) {
-        const uint32_t v = t[h];
-        if (v == id) return true;
-        if (v == HASH_EMPTY) return false;
-    }
-    return false;
+    return ((size_t)cap * 8 + (size_t)surv * 8 + 16 + (credit ? (size_t)surv * 2 : 0) + 15) & ~(size_t)15;
 }
 
 template <int SURV, bool CREDIT>
@@ -399,9 +367,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
     const size_t per_warp = merge_warp_bytes(a.cap, SURV, CREDIT);
     unsigned char *base = smem + w * per_warp;
     uint64_t *s_pool = reinterpret_cast<uint64_t *>(base);
-    uint32_t *s_hash = reinterpret_cast<uint32_t *>(base); // pool ids while the candidates are filtered
-    const uint32_t hslots = merge_hash_slots(a.cap), hmask = hslots - 1u;
-    uint64_t *s_sv = reinterpret_cast<uint64_t *>(base + merge_pool_bytes(a.cap)); // survivors (keys without flags)
+    uint64_t *s_sv = s_pool + a.cap;         // survivors (keys without flags)
     uint64_t *s_last = s_sv + SURV;          // key landing at rank limit-1
     uint16_t *s_j = reinterpret_cast<uint16_t *>(s_last + 2); // CREDIT: each survivor's candidate slot
     __shared__ unsigned long long s_stat[4]; // flagged, inserted, candidates, entries
@@ -414,13 +380,8 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
         const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
-        for (uint32_t i = lane; i < hslots / 4; i += 32)
-            reinterpret_cast<uint4 *>(s_hash)[i] = make_uint4(HASH_EMPTY, HASH_EMPTY, HASH_EMPTY, HASH_EMPTY);
-        __syncwarp();
 #pragma unroll 4
-        for (uint32_t i = lane; i < np; i += 32) merge_hash_insert(s_hash, hmask, kcna_key_id(gp[i]));
-        // a full pool: candidates from its last key on land at rank >= limit
-        const uint64_t last = np >= a.limit && np > 0 ? kcna_key_noflags(gp[np - 1]) : KCNA_EMPTY_KEY_NOFLAGS;
+        for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
         // candidates in groups of 128 (four per lane), the next group's loads in
         // flight while this group is searched
         constexpr int CG = 4;
@@ -446,8 +407,10 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                 const uint32_t j = b0 + 32 * u + lane;
                 bool surv = false;
                 const uint64_t k = kcna_key_noflags(cur[u]);
-                if (j < nc && k != KCNA_EMPTY_KEY_NOFLAGS && k < last)
-                    surv = !merge_hash_has(s_hash, hmask, kcna_key_id(k));
+                if (j < nc && k != KCNA_EMPTY_KEY_NOFLAGS) {
+                    const int b = kcna_lower_bound(s_pool, (int)np, k);
+                    surv = (uint32_t)b < a.limit && !(b < (int)np && (s_pool[b] >> 2) == (k >> 2));
+                }
                 const unsigned m = __ballot_sync(KCNA_FULL, surv);
                 const uint32_t pos = ns + __popc(m & kcna_lanemask_lt());
                 if (surv && pos < (uint32_t)SURV) {
@@ -460,11 +423,6 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         if (ns > (uint32_t)SURV) {
             if (lane == 0) big_list[atomicAdd(big_cnt, 1u)] = node;
         } else {
-            // the pool copy over the table, for the survivors' ranks
-            __syncwarp();
-#pragma unroll 4
-            for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
-            __syncwarp();
             uint32_t nu = 0; // distinct survivors
             if (ns > 0) {
                 const int p2 = kcna_pow2_ceil_d((int)ns);

@@ -11,17 +11,12 @@
 // so the kept lists are identical.
 //
 // Instead of testing candidates against the kept list one at a time, the
-// kernel resolves the sequential scan chunk by chunk (128 candidates each, up
-// to 4 chunks).  Within chunk J it evaluates the rule for every ordered pair
-// t < p (the upper triangle of the 128 x 128 diagonal tile) as bit masks:
-// O[t] is the set of later candidates of the chunk that t would occlude, and
-// the scan keeps t, adds O[t] to the dead set and jumps to the next live
-// candidate - one step per kept neighbour.  Between chunks only the kept
-// candidates matter as occluders: for each later chunk I the tile of chunk I's
-// rows (TMEM lanes) against chunk J's rows (columns) is read at the kept
-// columns alone, and a candidate of chunk I occluded by one of them is dead
-// before chunk I is scanned (with the rank of its first occluder, for the
-// comparison count).
+// kernel evaluates the occlusion rule for every ordered pair t < p of the
+// node's candidates (up to 512: the lower triangle of at most 4 x 4 tiles of
+// 128) and then resolves the sequential scan on bit masks: O[t] is the set of
+// later candidates that t would occlude, and the scan keeps t, adds O[t] to
+// the dead set and jumps to the next live candidate - one step per kept
+// neighbour.
 //
 // Block layout: persistent, one block per SM, warp-specialised; the roles
 // hand work to each other through mbarriers:
@@ -33,20 +28,17 @@
 //               into a ring of five 128-row chunk slots in the 128-byte
 //               swizzled K-major layout (each warp a quarter of every chunk,
 //               the copies of consecutive chunks overlapped);
-//   warp 1      MMA issuer (one thread): tiles (J, I), J <= I, in the order
-//               (0,0) (0,1) .. (0,3) (1,1) ..; a diagonal tile is chunk J
-//               against itself, an off-diagonal one has chunk I's rows as
-//               TMEM lanes and chunk J's as columns; chunk J's slot is
-//               released after its last tile; four 128-column accumulators;
-//   warps 2-17  tile readers: on a diagonal tile, warp w reads TMEM lane
-//               quarter w % 4 and column group (w - 2) / 4 (32 columns) and
-//               turns 32 distances per thread into a 32-bit word of O[t] (the
-//               sign of distance minus bound, collected by funnel shifts in
-//               four independent chains); on an off-diagonal tile, once the
-//               scan has finished chunk J, every fourth kept candidate of
-//               chunk J per warp, one TMEM column each;
-//   warp 18     scan: per node and chunk, the kept list by the bit-mask scan;
-//               graph row and degree written to global memory.
+//   warp 1      MMA issuer (one thread): tiles (J, I), J <= I, occluders of
+//               chunk J (M = 128 TMEM lanes) against candidates of chunk I
+//               (N = 128 columns), occluder-chunk major so that chunk J's slot
+//               is released after its last tile; four 128-column accumulators;
+//   warps 2-17  mask builders: warp w reads TMEM lane quarter w % 4 and
+//               column group (w - 2) / 4 (32 columns) of a tile, releases the
+//               accumulator, and turns 32 distances per thread into a 32-bit
+//               word of O[t] (the sign of distance minus bound, collected by
+//               funnel shifts in four independent chains);
+//   warp 18     scan: per node, the kept list by the bit-mask scan; graph row
+//               and degree written to global memory.
 // Every wait is bounded; a wait that gives up stops the block, sets the error
 // word and lets in-flight copies and products finish before TMEM is released.
 #include <algorithm>
@@ -74,13 +66,14 @@ constexpr int LOAD_WARP = SCAN_WARP + 1;          // first row-loader warp
 constexpr int NLOAD = 4;                          // row-loader warps
 constexpr int PG_THREADS = (LOAD_WARP + NLOAD) * 32;
 
-// Diagonal-tile masks: word w (candidates 128 J + 32 w .. + 31) of chunk-local
-// row t at (4 J + w) * MSTR + t.  The row stride 129 keeps both the tile
-// readers (fixed word, 32 consecutive rows) and the scan (fixed row, four
-// words) free of bank conflicts.
-constexpr int MSTR = PC + 1;
-constexpr int MASK_WORDS = 4 * MAXCH * MSTR;
-constexpr uint32_t NO_RANK = 0xFFFFFFFFu;
+// Occluder masks, word-major: word w (candidates 32w .. 32w+31) of row t is at
+// mask_base(w) + t; word w exists for rows t < 128 (w / 4 + 1) only (t < p).
+// mask_base(w) is w modulo 32, so both the mask builders (fixed w, 32
+// consecutive t) and the scan (fixed t, 16 words) are free of bank conflicts.
+__host__ __device__ constexpr int mask_base(int w) {
+    return 128 * ((w / 4) * (w / 4 + 1) / 2 * 4 + (w % 4) * (w / 4 + 1)) + w;
+}
+constexpr int MASK_WORDS = mask_base(MW);
 
 struct alignas(16) NodeMeta {
     uint64_t key[MAXC + 2]; // pool entries from an even index (16-byte bulk copy); candidate c at koff + c
@@ -93,16 +86,11 @@ struct alignas(16) NodeMeta {
 struct PgShared {
     uint64_t slot_full[NSLOT], slot_empty[NSLOT];
     uint64_t acc_full[NACC], acc_empty[NACC];
-    uint64_t keys_full[2], ids_ready[2], meta_full[2], bound_ready[2], node_empty[2];
-    uint64_t diag_full[2], scan_done[2]; // one phase per chunk of each node
+    uint64_t keys_full[2], ids_ready[2], meta_full[2], bound_ready[2], mask_full[2], node_empty[2];
     uint32_t tmem;
     int abort_flag;
     NodeMeta meta[2];
     uint32_t mask[2][MASK_WORDS];
-    uint32_t offdead[2][MW];      // occluded by a kept candidate of an earlier chunk
-    uint32_t rank_min[2][MAXC];   // 1-based kept rank of that candidate's first such occluder
-    uint16_t kept[2][MAXC];       // kept candidates (node-local index) in order
-    uint32_t kept_end[2][MAXCH];  // end of each chunk's kept run in kept[]
 };
 
 struct PgArgs {
@@ -170,9 +158,8 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             mbar_init(&S.keys_full[i], 1);        // metadata lane 0 (expect_tx); the bulk copy completes it
             mbar_init(&S.ids_ready[i], 1);        // metadata lane 0 after the keys are parsed
             mbar_init(&S.meta_full[i], 64);       // metadata lanes: stores done, norm copies landed
-            mbar_init(&S.bound_ready[i], EPI);    // tile readers' shares of the RNG column values
-            mbar_init(&S.diag_full[i], EPI);      // tile readers: a chunk's diagonal masks stored
-            mbar_init(&S.scan_done[i], 1);        // scan lane 0: a chunk's kept run stored
+            mbar_init(&S.bound_ready[i], EPI);    // mask builders' shares of the RNG column values
+            mbar_init(&S.mask_full[i], EPI);
             mbar_init(&S.node_empty[i], 2 + NLOAD); // scan, MMA issuer, loader warps
         }
         S.abort_flag = 0;
@@ -257,9 +244,6 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                 }
                 if (lane == 0) M.dead[i] = dm;
             }
-            // the slot's cross-chunk state (its previous node is finished)
-            if (lane < MW) S.offdead[sl][lane] = 0u;
-            for (int c = lane; c < nch * PC; c += 32) S.rank_min[sl][c] = NO_RANK;
             if (lane == 0) {
                 M.q = q;
                 M.nc = (uint32_t)nc;
@@ -352,13 +336,12 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                             break;
                         }
                         fence_after();
-                        // rows (TMEM lanes) chunk I, columns chunk J: <p, t> at lane p, column t
-                        const uint32_t cJ = slot0 + (gJ % NSLOT) * CHUNK_BYTES, rI = slot0 + (gI % NSLOT) * CHUNK_BYTES;
+                        const uint32_t aJ = slot0 + (gJ % NSLOT) * CHUNK_BYTES, bI = slot0 + (gI % NSLOT) * CHUNK_BYTES;
                         for (int kb = 0; kb < nkb; ++kb)
 #pragma unroll
                             for (int kk = 0; kk < 4; ++kk)
-                                mma_bf16(tmem + (uint32_t)(b * PC), desc_sw128(rI + kb * PC * KBB + kk * 32),
-                                         desc_sw128(cJ + kb * PC * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
+                                mma_bf16(tmem + (uint32_t)(b * PC), desc_sw128(aJ + kb * PC * KBB + kk * 32),
+                                         desc_sw128(bI + kb * PC * KBB + kk * 32), idesc, (kb | kk) ? 1u : 0u);
                         mma_commit(&S.acc_full[b]);
                         if (I == nch - 1) mma_commit(&S.slot_empty[gJ % NSLOT]); // chunk J's last tile
                     }
@@ -377,13 +360,12 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         }
         __syncwarp();
     } else if (warp < SCAN_WARP) {
-        // --------------------------------------------------------- tile readers
+        // -------------------------------------------------------- mask builders
         const int qt = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column group
-        uint32_t acount = 0, ph0 = 0, ph1 = 0;      // accumulators consumed; chunks seen per node slot
+        uint32_t acount = 0;
         int k = 0;
         for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
             const int sl = k & 1;
-            const uint32_t ph = sl ? ph1 : ph0;
             bool mine = mbar_wait(&S.meta_full[sl], (k >> 1) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
             NodeMeta &M = S.meta[sl];
@@ -398,173 +380,109 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                 if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
             }
             for (int J = 0; J < nch && ok; ++J) {
+                const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
+                const float n_t = M.nrm[t], td = M.pd[t];
                 for (int I = J; I < nch; ++I, ++acount) {
                     const int b = (int)(acount % NACC);
-                    if (I == J) {
-                        // ---- diagonal tile: words of O[t] for this warp's 32 rows and 32 columns
-                        const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
-                        const float n_t = M.nrm[t], td = M.pd[t];
-                        mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
-                        fence_after();
-                        const bool skip = CW * h + CW - 1 <= 32 * qt; // no column after any row of the warp
-                        uint32_t raw[CW];
-                        if (mine && !skip) {
-                            const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC + CW * h);
+                    mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
+                    fence_after();
+                    const bool skip = I == J && CW * h + CW - 1 <= 32 * qt; // no column after any row of the warp
+                    uint32_t raw[CW];
+                    if (mine && !skip) {
+                        const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC + CW * h);
 #pragma unroll
-                            for (int x = 0; x < CW / 16; ++x) tmem_ld16_async(ta + 16 * x, raw + 16 * x);
+                        for (int x = 0; x < CW / 16; ++x) tmem_ld16_async(ta + 16 * x, raw + 16 * x);
 #pragma unroll
-                            for (int x = 0; x < CW / 16; ++x) tmem_wait_ld16(raw + 16 * x);
-                        }
-                        // the accumulator is in registers: release it before the bit work
-                        fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&S.acc_empty[b]);
-                        if (!__all_sync(KCNA_FULL, mine)) {
-                            ok = false;
-                            break;
-                        }
+                        for (int x = 0; x < CW / 16; ++x) tmem_wait_ld16(raw + 16 * x);
+                    }
+                    // the accumulator is in registers: release it before the bit work
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.acc_empty[b]);
+                    if (!__all_sync(KCNA_FULL, mine)) {
+                        ok = false;
+                        break;
+                    }
 #pragma unroll
-                        for (int ww = 0; ww < WPT; ++ww) {
-                            const int p0 = I * PC + CW * h + 32 * ww; // first candidate of the word
-                            uint32_t word = 0;
-                            if (!skip) {
-                                const float4 *np4 = reinterpret_cast<const float4 *>(M.nrm + p0);
-                                const float4 *pd4 = reinterpret_cast<const float4 *>(M.pd + p0);
-                                // four chains of eight: candidate 8j+m ends in bit 7-m of wq[j]
-                                uint32_t wq[4] = {0u, 0u, 0u, 0u};
+                    for (int ww = 0; ww < WPT; ++ww) {
+                        const int p0 = I * PC + CW * h + 32 * ww; // first candidate of the word
+                        uint32_t word = 0;
+                        if (!skip) {
+                            const float4 *np4 = reinterpret_cast<const float4 *>(M.nrm + p0);
+                            const float4 *pd4 = reinterpret_cast<const float4 *>(M.pd + p0);
+                            // four chains of eight: candidate 8j+m ends in bit 7-m of wq[j]
+                            uint32_t wq[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-                                for (int u4 = 0; u4 < 8; ++u4) {
-                                    const float4 n4 = np4[u4], d4 = pd4[u4];
-                                    const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+                            for (int u4 = 0; u4 < 8; ++u4) {
+                                const float4 n4 = np4[u4], d4 = pd4[u4];
+                                const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
-                                    for (int v = 0; v < 4; ++v) {
-                                        const uint32_t sg = occl_sign<RULE>(__uint_as_float(raw[32 * ww + 4 * u4 + v]),
-                                                                            n_t, nn[v], dv[v], td, a.t3, a.thr);
-                                        wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
-                                    }
+                                for (int v = 0; v < 4; ++v) {
+                                    const uint32_t sg = occl_sign<RULE>(__uint_as_float(raw[32 * ww + 4 * u4 + v]),
+                                                                        n_t, nn[v], dv[v], td, a.t3, a.thr);
+                                    wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
                                 }
-                                word = __brev((wq[0] << 24) | (wq[1] << 16) | (wq[2] << 8) | wq[3]);
-                                const int r = t - p0; // only candidates after t
+                            }
+                            word = __brev((wq[0] << 24) | (wq[1] << 16) | (wq[2] << 8) | wq[3]);
+                            if (I == J) { // only candidates after t
+                                const int r = t - p0;
                                 word = r < 0 ? word : r >= 31 ? 0u : word & ~((2u << r) - 1u);
                             }
-                            mask[(4 * J + CW / 32 * h + ww) * MSTR + 32 * qt + lane] = word;
                         }
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&S.diag_full[sl]);
-                    } else {
-                        // ---- off-diagonal tile: chunk I's candidates against chunk J's kept ones
-                        if (I == J + 1) {
-                            mine = mbar_wait(&S.scan_done[sl], (ph + (uint32_t)J) & 1) && !S.abort_flag;
-                            if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
-                        }
-                        const int p = I * PC + 32 * qt + lane; // this lane's candidate (TMEM lane)
-                        const float n_p = M.nrm[p], pd_p = M.pd[p];
-                        const int kb = J ? (int)S.kept_end[sl][J - 1] : 0, ke = (int)S.kept_end[sl][J];
-                        mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
-                        fence_after();
-                        uint32_t rmin = NO_RANK;
-                        if (__all_sync(KCNA_FULL, mine)) {
-                            const uint32_t ta = tmem + ((uint32_t)(32 * qt) << 16) + (uint32_t)(b * PC);
-                            for (int e = kb + h; e < ke; e += 4) { // kept in order: the first hit is the lowest rank
-                                const int tt = S.kept[sl][e];
-                                const uint32_t g = tmem_ld1(ta + (uint32_t)(tt - J * PC));
-                                const uint32_t sg = occl_sign<RULE>(__uint_as_float(g), M.nrm[tt], n_p, pd_p, M.pd[tt],
-                                                                    a.t3, a.thr);
-                                if ((sg >> 31) && rmin == NO_RANK) rmin = (uint32_t)e + 1u;
-                            }
-                        }
-                        fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&S.acc_empty[b]);
-                        if (!__all_sync(KCNA_FULL, mine)) {
-                            ok = false;
-                            break;
-                        }
-                        const unsigned occ = __ballot_sync(KCNA_FULL, rmin != NO_RANK);
-                        if (occ) {
-                            if (lane == 0) atomicOr(&S.offdead[sl][4 * I + qt], occ);
-                            if (rmin != NO_RANK) atomicMin(&S.rank_min[sl][p], rmin);
-                        }
+                        mask[mask_base(4 * I + CW / 32 * h + ww) + t] = word;
                     }
                 }
             }
             if (!ok) break;
-            if (sl) ph1 += (uint32_t)nch;
-            else ph0 += (uint32_t)nch;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.mask_full[sl]);
         }
         if (!ok) S.abort_flag = 1;
     } else {
         // ----------------------------------------------------------------- scan
         unsigned long long cc = 0;
-        uint32_t ph0 = 0, ph1 = 0;
         int k = 0;
         for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
             const int sl = k & 1;
-            const uint32_t ph = sl ? ph1 : ph0;
-            bool mine = mbar_wait(&S.meta_full[sl], (k >> 1) & 1) && !S.abort_flag;
+            const bool mine = mbar_wait(&S.mask_full[sl], (k >> 1) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
             const NodeMeta &M = S.meta[sl];
             const uint32_t *mask = S.mask[sl];
             const uint64_t *keys = M.key + M.koff;
-            const int nch = (int)M.nch;
+            const int nc = (int)M.nc;
             uint32_t *gi = a.g_ids + (uint64_t)M.q * a.W;
             float *gd = a.g_dist + (uint64_t)M.q * a.W;
             int nk = 0;
-            bool done = false;
-            for (int J = 0; J < nch; ++J) {
-                mine = mbar_wait(&S.diag_full[sl], (ph + (uint32_t)J) & 1) && !S.abort_flag;
-                if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
-                // lanes 0-3: the chunk's four dead words
-                uint32_t dw = 0xFFFFFFFFu;
-                if (lane < 4) {
-                    const uint32_t d0 = M.dead[4 * J + lane], od = S.offdead[sl][4 * J + lane];
-                    dw = d0 | od;
-                    // occluded by an earlier chunk: tested against the kept list up to its first occluder
-                    for (uint32_t m = od & ~d0; m; m &= m - 1u) {
-                        const uint32_t r = S.rank_min[sl][PC * J + 32 * lane + __ffs(m) - 1];
-                        if (r < (uint32_t)a.range) cc += r;
-                    }
-                }
-                uint32_t alive = lane < 4 ? ~dw : 0u;
-                unsigned bal = done ? 0u : __ballot_sync(KCNA_FULL, alive != 0u);
-                while (bal) {
-                    const int L = __ffs(bal) - 1;
-                    const int tl = 32 * L + __ffs(__shfl_sync(KCNA_FULL, alive, L)) - 1; // chunk-local
-                    const int t = PC * J + tl;
+            if (nc > 0) {
+                uint32_t dead = lane < MW ? M.dead[lane] : 0xFFFFFFFFu;
+                int t = 0;
+                for (;;) {
                     if (lane == 0) {
                         gi[nk] = kcna_key_id(keys[t]);
                         gd[nk] = kcna_key_dist(keys[t]);
-                        S.kept[sl][nk] = (uint16_t)t;
                         cc += (unsigned long long)nk; // a kept candidate was tested against every earlier one
                     }
                     ++nk;
-                    if (nk >= a.range) {
-                        done = true;
-                        break;
-                    }
-                    const int tw = tl >> 5;
-                    const uint32_t o = lane < 4 ? mask[(4 * J + lane) * MSTR + tl] : 0u;
-                    const uint32_t above = lane > tw ? 0xFFFFFFFFu : lane < tw ? 0u : ~((2u << (tl & 31)) - 1u);
-                    cc += (unsigned long long)nk * __popc(o & ~dw & above); // dropped at the nk-th kept
-                    dw |= o;
-                    alive = lane < 4 ? ~dw & above : 0u;
-                    bal = __ballot_sync(KCNA_FULL, alive != 0u);
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    S.kept_end[sl][J] = (uint32_t)nk;
-                    mbar_arrive(&S.scan_done[sl]);
+                    if (nk >= a.range) break;
+                    const int tw = t >> 5;
+                    uint32_t o = 0;
+                    if (lane < MW && lane >= 4 * (t >> 7)) o = mask[mask_base(lane) + t];
+                    const uint32_t above = lane > tw ? 0xFFFFFFFFu : lane < tw ? 0u : ~((2u << (t & 31)) - 1u);
+                    cc += (unsigned long long)nk * __popc(o & ~dead & above); // dropped at the nk-th kept
+                    dead |= o;
+                    const uint32_t alive = ~dead & above;
+                    const unsigned bal = __ballot_sync(KCNA_FULL, alive != 0u);
+                    if (!bal) break;
+                    const int L = __ffs(bal) - 1;
+                    t = 32 * L + __ffs(__shfl_sync(KCNA_FULL, alive, L)) - 1;
                 }
             }
-            if (!ok) break;
             __syncwarp();
             for (int j = nk + lane; j < (int)a.W; j += 32) {
                 gi[j] = KCNA_NONE;
                 gd[j] = 0.f;
             }
             if (lane == 0) a.g_deg[M.q] = (uint32_t)nk;
-            if (sl) ph1 += (uint32_t)nch;
-            else ph0 += (uint32_t)nch;
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.node_empty[sl]);
         }

@@ -112,16 +112,6 @@ __device__ __forceinline__ void tmem_wait_ld16(uint32_t *r) {
                  : "memory");
 }
 
-// One accumulator column of this thread's TMEM lane (raw bits), waited for.
-__device__ __forceinline__ uint32_t tmem_ld1(uint32_t taddr) {
-    uint32_t r;
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n\ttcgen05.wait::ld.sync.aligned;"
-                 : "=r"(r)
-                 : "r"(taddr)
-                 : "memory");
-    return r;
-}
-
 // 16 consecutive FP32 accumulator columns of this thread's TMEM lane, waited for.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     uint32_t r[16];
