@@ -177,7 +177,7 @@ void kcna_log(kcna_ctx *c, const kcna_params *p, const char *fmt, ...) {
 static void free_state(kcna_ctx *c) {
     void *bufs[] = {c->pool, c->pool_cnt, c->radius, c->M, c->radiusM, c->found, c->fwd_new, c->fwd_new_cnt,
                     c->fwd_old, c->fwd_old_cnt, c->rnew, c->rnew_cnt, c->rold, c->rold_cnt, c->cand, c->cand_cnt,
-                    c->cand_src, c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
+                    c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
                     c->d_control_knn, c->big_list, c->big_cnt};
     for (void *b : bufs)
         if (b) kcna_release(c, b);
@@ -191,7 +191,6 @@ static void free_state(kcna_ctx *c) {
     c->rnew = c->rnew_cnt = c->rold = c->rold_cnt = nullptr;
     c->cand = nullptr;
     c->cand_cnt = nullptr;
-    c->cand_src = nullptr;
     c->big_list = c->big_cnt = nullptr;
     c->g_ids = c->g_deg = c->g_old = c->g_old_deg = nullptr;
     c->g_dist = nullptr;

@@ -38,6 +38,16 @@ __host__ __device__ __forceinline__ uint32_t kcna_key_id(uint64_t k) { return (u
 __host__ __device__ __forceinline__ uint32_t kcna_key_flags(uint64_t k) { return (uint32_t)(k & 3ull); }
 __host__ __device__ __forceinline__ uint64_t kcna_key_noflags(uint64_t k) { return k & ~3ull; }
 
+// Candidate buffers: slot s (s = node * CB + position) holds the candidate's
+// key in word 2 s and its joiner (the node whose join emitted it; low 32 bits)
+// in word 2 s + 1, so one 16-byte store writes both.
+__device__ __forceinline__ void kcna_cand_put(uint64_t *cand, uint64_t slot, uint64_t key, uint32_t joiner) {
+    *reinterpret_cast<ulonglong2 *>(cand + 2 * slot) = make_ulonglong2(key, (unsigned long long)joiner);
+}
+__device__ __forceinline__ uint32_t kcna_cand_joiner(const uint64_t *cand, uint64_t slot) {
+    return (uint32_t)cand[2 * slot + 1];
+}
+
 // ---------------------------------------------------------------------------
 // Canonical FP32 squared L2 distance: one fused multiply-add chain over the
 // dimensions in order, acc = fma(x_k - y_k, x_k - y_k, acc).  Every kernel that

@@ -65,7 +65,6 @@ struct kcna_ctx {
     uint32_t *rold = nullptr, *rold_cnt = nullptr;
     uint64_t *cand = nullptr;
     uint32_t *cand_cnt = nullptr;
-    uint32_t *cand_src = nullptr; // joiner of each candidate of an NN-descent join (found credit)
     uint32_t *big_list = nullptr, *big_cnt = nullptr; // merge queue of nodes with many candidates
     uint32_t merge_big_last = 0;                      // nodes the previous merge queued
     unsigned long long *counters = nullptr; // device scratch counters (64 slots)
@@ -171,7 +170,7 @@ kcna_status kcna_nnd_init(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_cand_alloc(kcna_ctx *c, const kcna_params *p);
 kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t *n_comps);  // iter 0: init lists
 // Merges every node's candidate buffer into its pool.  credit_found: the
-// candidates of an NN-descent join, whose joiners (cand_src) are credited with
+// candidates of an NN-descent join, whose joiners (stored beside their keys) are credited with
 // found flags for the entries they inserted below K.
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr, bool credit_found = false);

@@ -20,9 +20,8 @@ struct JoinArgs {
     uint32_t fwd_old_cap;
     const uint32_t *rnew, *rnew_cnt, *rold, *rold_cnt;
     const float *radius;
-    uint64_t *cand;
+    uint64_t *cand;     // key and joiner per slot (kcna_cand_put)
     uint32_t *cand_cnt;
-    uint32_t *cand_src; // the joiner of each candidate, beside its key (found credit in the merge)
     uint32_t CB;
     uint8_t *found;
     unsigned long long *counters; // [0] pairs evaluated, [5] rows gathered, [6] candidates emitted

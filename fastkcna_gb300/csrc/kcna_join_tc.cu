@@ -405,8 +405,7 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
             }
             emitted += (unsigned long long)(nr + nct);
             if (__any_sync(KCNA_FULL, nr > 0 || nct > 0)) { // write pass; the distances are read again from TMEM
-                uint64_t *dst = a.cand + (uint64_t)id_j * a.CB;
-                uint32_t *dsrc = a.cand_src + (uint64_t)id_j * a.CB;
+                const uint64_t s0 = (uint64_t)id_j * a.CB;
                 const uint32_t joiner = rowv ? M.row_node[r] : 0u; // the node whose join made this tile row
 #pragma unroll
                 for (int k = 0; k < GPW; ++k) {
@@ -428,18 +427,14 @@ __global__ void __launch_bounds__(JT_THREADS, 1) join_tc_kernel(JoinArgs a, cons
                             const float dd = fmaxf(
                                 __fsub_rn(__fadd_rn(n_j, M.col_nrm[i]), 2.f * __uint_as_float(raw[x])), 0.f);
                             if ((gm >> x) & 1u) {
-                                if (p < a.CB) {
-                                    dst[p] = kcna_key(dd, M.col_id[i], flags);
-                                    dsrc[p] = joiner;
-                                }
+                                if (p < a.CB) kcna_cand_put(a.cand, s0 + p, kcna_key(dd, M.col_id[i], flags), joiner);
                                 ++p;
                             }
                             if ((m >> lane) & 1u) {
                                 const uint32_t pc = cbx + __popc(m & kcna_lanemask_lt());
-                                if (pc < a.CB) {
-                                    a.cand[(uint64_t)M.col_id[i] * a.CB + pc] = kcna_key(dd, id_j, flags);
-                                    a.cand_src[(uint64_t)M.col_id[i] * a.CB + pc] = joiner;
-                                }
+                                if (pc < a.CB)
+                                    kcna_cand_put(a.cand, (uint64_t)M.col_id[i] * a.CB + pc, kcna_key(dd, id_j, flags),
+                                                  joiner);
                             }
                         }
                     }

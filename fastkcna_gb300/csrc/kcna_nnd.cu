@@ -198,21 +198,14 @@ __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, cons
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
             base = __shfl_sync(KCNA_FULL, base, 0);
-            uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
-            uint32_t *dsrc = a.cand_src + (uint64_t)tgt * a.CB;
+            const uint64_t s0 = (uint64_t)tgt * a.CB;
             if (ok[0]) {
                 uint32_t p = base + __popc(m0 & kcna_lanemask_lt());
-                if (p < a.CB) {
-                    dst[p] = keys[0];
-                    dsrc[p] = node;
-                }
+                if (p < a.CB) kcna_cand_put(a.cand, s0 + p, keys[0], node);
             }
             if (ok[1]) {
                 uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
-                if (p < a.CB) {
-                    dst[p] = keys[1];
-                    dsrc[p] = node;
-                }
+                if (p < a.CB) kcna_cand_put(a.cand, s0 + p, keys[1], node);
             }
             if (lane == 0) atomicAdd(s_emit, (unsigned)cnt);
         }
@@ -243,17 +236,13 @@ __device__ void join_tiles(const JoinArgs &a, const R &rows, uint32_t node, cons
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(a.cand_cnt + tgt, (uint32_t)cnt);
             base = __shfl_sync(KCNA_FULL, base, 0);
-            uint64_t *dst = a.cand + (uint64_t)tgt * a.CB;
-            uint32_t *dsrc = a.cand_src + (uint64_t)tgt * a.CB;
+            const uint64_t s0 = (uint64_t)tgt * a.CB;
             uint32_t run = base;
 #pragma unroll
             for (int h = 0; h < RI; ++h) {
                 if (mk[h] & (1u << lane)) {
                     uint32_t p = run + __popc(mk[h] & kcna_lanemask_lt());
-                    if (p < a.CB) {
-                        dst[p] = keys[h];
-                        dsrc[p] = node;
-                    }
+                    if (p < a.CB) kcna_cand_put(a.cand, s0 + p, keys[h], node);
                 }
                 run += __popc(mk[h]);
             }
@@ -315,7 +304,7 @@ struct MergeArgs {
     uint32_t *pool_cnt;
     uint32_t cap, limit, K;
     float *radius;
-    uint64_t *cand;
+    uint64_t *cand; // key and joiner per slot (kcna_cand_put)
     uint32_t *cand_cnt;
     uint32_t CB;
     unsigned long long *counters; // [1] flagged in top-K, [2] overflow, [3] inserted
@@ -330,7 +319,7 @@ struct MergeArgs {
     // emitter instead over-credits: NN-descent then converges measurably
     // faster than the reference's (200k C2 rows: recall 0.9968 after six
     // iterations against the reference's 0.9943).
-    const uint32_t *cand_src;
+    uint32_t credit; // credit joiners (NN-descent merges)
     uint8_t *found;
     uint32_t n_nodes;
 };
@@ -350,7 +339,7 @@ struct MergeArgs {
 // With CREDIT (NN-descent merges) every survivor also keeps the index of its
 // candidate slot (16 bits, CB <= 8192) and moves with its key through the
 // sort; before the survivors are deduplicated, each distinct survivor placed
-// at rank < K loads the joiners of its copies (MergeArgs.cand_src) and
+// at rank < K loads the joiners of its copies (beside their keys) and
 // credits the lowest.  Three blocks of eight warps still share an SM; with
 // 1024 survivor slots a block has seven warps so that two blocks share one.
 constexpr int MW_WARPS = 8;
@@ -379,7 +368,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
-        const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+        const uint64_t *gc = a.cand + 2 * (uint64_t)node * a.CB; // keys at even words
 #pragma unroll 4
         for (uint32_t i = lane; i < np; i += 32) s_pool[i] = gp[i];
         // candidates in groups of 128 (four per lane), the next group's loads in
@@ -389,7 +378,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
 #pragma unroll
         for (int u = 0; u < CG; ++u) {
             const uint32_t j = 32 * u + lane;
-            nxt[u] = j < nc ? gc[j] : KCNA_EMPTY_KEY;
+            nxt[u] = j < nc ? gc[2 * j] : KCNA_EMPTY_KEY;
         }
         __syncwarp();
         // survivors: not in the pool, landing below limit
@@ -400,7 +389,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
             for (int u = 0; u < CG; ++u) {
                 cur[u] = nxt[u];
                 const uint32_t j = b0 + 32 * CG + 32 * u + lane;
-                nxt[u] = j < nc ? gc[j] : KCNA_EMPTY_KEY;
+                nxt[u] = j < nc ? gc[2 * j] : KCNA_EMPTY_KEY;
             }
 #pragma unroll
             for (int u = 0; u < CG; ++u) {
@@ -436,7 +425,6 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                     // copies of one key are adjacent: each distinct survivor whose
                     // rank (distinct index + position in the pool) is below K
                     // credits the lowest joiner among its copies
-                    const uint32_t *gsrc = a.cand_src + (uint64_t)node * a.CB;
                     uint64_t carry = KCNA_EMPTY_KEY;
                     uint32_t q0 = 0;
                     for (uint32_t b0 = 0; b0 < ns; b0 += 32) {
@@ -450,7 +438,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                         if (start && q + (uint32_t)kcna_lower_bound(s_pool, (int)np, k) < a.K) {
                             uint32_t best = KCNA_NONE;
                             for (uint32_t x = j; x < ns && (s_sv[x] >> 2) == (k >> 2); ++x)
-                                best = min(best, gsrc[s_j[x]]);
+                                best = min(best, (uint32_t)gc[2 * s_j[x] + 1]);
                             if (best < a.n_nodes) a.found[best] = 1;
                         }
                         carry = __shfl_sync(KCNA_FULL, k, 31);
@@ -588,7 +576,7 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
     uint32_t *s_off = s_hist + a.cap + 2;                  // cap + 2
     uint32_t *s_giant = s_off + a.cap + 2;                 // cap + 2
     uint32_t *s_kept = reinterpret_cast<uint32_t *>(s_c);  // cbp + 1, once s_c's sorting is done
-    const bool credit = a.cand_src != nullptr;
+    const bool credit = a.credit != 0;
     __shared__ uint32_t s_warp[MT / 32];
     __shared__ uint32_t s_ngiant;
     __shared__ unsigned long long s_flagged;
@@ -599,7 +587,7 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
-        const uint64_t *gc = a.cand + (uint64_t)node * a.CB;
+        const uint64_t *gc = a.cand + 2 * (uint64_t)node * a.CB; // keys at even words
         if (threadIdx.x == 0) {
             s_flagged = 0;
             s_ngiant = 0;
@@ -609,7 +597,7 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
         __syncthreads();
         // bucket of every candidate
         for (uint32_t j = threadIdx.x; j < nc; j += MT) {
-            const uint64_t k = kcna_key_noflags(gc[j]);
+            const uint64_t k = kcna_key_noflags(gc[2 * j]);
             s_c[j] = k;
             const int b = kcna_lower_bound(s_pool, (int)np, k);
             const bool dup = b < (int)np && (s_pool[b] >> 2) == (k >> 2);
@@ -648,7 +636,7 @@ __global__ void __launch_bounds__(MT) merge_kernel(MergeArgs a, const uint32_t *
             if (b != KCNA_NONE) {
                 const uint32_t q = s_off[b] + atomicAdd(&s_hist[b], 1u);
                 s_sorted[q] = s_c[j];
-                s_ss[q] = credit ? a.cand_src[(uint64_t)node * a.CB + j] : 0u;
+                s_ss[q] = credit ? (uint32_t)gc[2 * j + 1] : 0u;
             }
         }
         __syncthreads();
@@ -926,11 +914,11 @@ __global__ void __launch_bounds__(256) rescore_kernel(const float *__restrict__ 
     __syncwarp();
     const uint32_t nc = min(cand_cnt[t], CB);
     const float rad = radius[t];
-    uint64_t *buf = cand + (uint64_t)t * CB;
+    uint64_t *buf = cand + 2 * (uint64_t)t * CB; // keys at even words
     const float4 *x4 = reinterpret_cast<const float4 *>(xt);
     unsigned long long n = 0, rep = 0;
     for (uint32_t j = lane; j < nc; j += 32) {
-        const uint64_t k = buf[j];
+        const uint64_t k = buf[2 * j];
         if (kcna_key_noflags(k) == KCNA_EMPTY_KEY_NOFLAGS) continue;
         const uint32_t id = kcna_key_id(k);
         bool in_pool = false;
@@ -943,14 +931,14 @@ __global__ void __launch_bounds__(256) rescore_kernel(const float *__restrict__ 
             }
         }
         if (in_pool) {
-            buf[j] = KCNA_EMPTY_KEY;
+            buf[2 * j] = KCNA_EMPTY_KEY;
             ++rep;
             continue;
         }
         const float4 *xc = reinterpret_cast<const float4 *>(X + (uint64_t)id * ld);
         float d = 0.f;
         for (int q = 0; q < (ld >> 2); ++q) d = kcna_acc4(d, x4[q], __ldg(xc + q));
-        buf[j] = d <= rad ? kcna_key(d, id, kcna_key_flags(k)) : KCNA_EMPTY_KEY;
+        buf[2 * j] = d <= rad ? kcna_key(d, id, kcna_key_flags(k)) : KCNA_EMPTY_KEY;
         ++n;
     }
     n = kcna_warp_sum(n);
@@ -1028,8 +1016,7 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     KCNA_TRY(kcna_alloc(c, &c->rnew_cnt, N, "rnew_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->rold, N * c->RB, "rold"));
     KCNA_TRY(kcna_alloc(c, &c->rold_cnt, N, "rold_cnt"));
-    KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
-    KCNA_TRY(kcna_alloc(c, &c->cand_src, N * c->CB, "candidate joiners"));
+    KCNA_TRY(kcna_alloc(c, &c->cand, 2 * N * c->CB, "candidate buffers"));
     KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->big_list, N, "merge queue"));
     KCNA_TRY(kcna_alloc(c, &c->big_cnt, 1, "merge queue count"));
@@ -1051,7 +1038,7 @@ kcna_status kcna_cand_alloc(kcna_ctx *c, const kcna_params *p) {
     uint32_t CB = cb ? (uint32_t)atoi(cb) : 4 * std::max<uint32_t>(p->L, 64);
     CB = std::min<uint32_t>(std::max<uint32_t>(CB, 64), 8192);
     c->CB = (uint32_t)kcna_pow2_ceil((int)CB);
-    KCNA_TRY(kcna_alloc(c, &c->cand, N * c->CB, "candidate buffers"));
+    KCNA_TRY(kcna_alloc(c, &c->cand, 2 * N * c->CB, "candidate buffers"));
     KCNA_TRY(kcna_alloc(c, &c->cand_cnt, N, "cand_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->big_list, N, "merge queue"));
     KCNA_TRY(kcna_alloc(c, &c->big_cnt, 1, "merge queue count"));
@@ -1099,7 +1086,6 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
     a.radius = c->radius;
     a.cand = c->cand;
     a.cand_cnt = c->cand_cnt;
-    a.cand_src = c->cand_src;
     a.CB = c->CB;
     a.found = c->found;
     a.counters = c->counters;
@@ -1169,7 +1155,7 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     a.cand_cnt = c->cand_cnt;
     a.CB = c->CB;
     a.counters = c->counters;
-    a.cand_src = credit_found ? c->cand_src : nullptr;
+    a.credit = credit_found ? 1u : 0u;
     a.found = c->found;
     a.n_nodes = c->n;
     size_t sm = merge_smem_bytes(c->cap, c->CB);

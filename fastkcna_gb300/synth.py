@@ -72,6 +72,11 @@ def _draw(name: str, n: int, seed: int, chunk: int = 1 << 17) -> np.ndarray:
     return out
 
 
+def centres(name: str) -> np.ndarray:
+    """The mixture centres the rows of a workload are drawn around."""
+    return _centres(name).copy()
+
+
 def base(name: str, n: int | None = None) -> np.ndarray:
     """Base rows (float32, C-contiguous)."""
     return _draw(name, SPECS[name]["n"] if n is None else n, SEED_BASE)

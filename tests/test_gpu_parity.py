@@ -151,8 +151,31 @@ def test_nndescent_recall_matches_oracle(index, oracle):
         assert np.all(np.diff(pd[i, : pc[i]]) >= 0)
 
 
+def _cluster_starts(X, Q, ep, L, name="c1"):
+    """Start nodes per query: the entry point and L - 1 seeded random rows of
+    the query's own cluster (nearest mixture centre)."""
+    cen = synth.centres(name).astype(np.float32)
+    lab_x = np.argmin(((X[:, None, :] - cen[None]) ** 2).sum(-1), axis=1)
+    lab_q = np.argmin(((Q[:, None, :] - cen[None]) ** 2).sum(-1), axis=1)
+    members = [np.flatnonzero(lab_x == c) for c in range(cen.shape[0])]
+    out = np.empty((Q.shape[0], L), np.uint32)
+    for qi in range(Q.shape[0]):
+        out[qi, 0] = ep
+        out[qi, 1:] = np.random.default_rng(qi).choice(members[lab_q[qi]], size=L - 1, replace=False)
+    return out
+
+
 @pytest.mark.parametrize("kind", ["nsg", "taumng", "alphapg"])
 def test_build_search_recall(index, oracle, kind):
+    """Search recall@10 of the GPU build against the oracle build of the same
+    rows and flags, both graphs searched by the same GPU searcher.  C1's 16
+    clusters hold 1,250 rows each against K = 100, so the graph is one island
+    per cluster joined only by tree_grow's links, and a search from the entry
+    point and random nodes reaches a query's cluster by chance: whole clusters
+    are found or missed per build (measured on both builders: recall 0.93 or
+    0.999 by seed).  Beams started inside the query's cluster measure the
+    graph itself; there the two builders agree to 0.0005 over three seeds at
+    L = 12 and 16 (recall 0.87-0.92), and the bar is 0.002."""
     X = synth.base("c1", 20000)
     Q = synth.queries("c1", 2000)
     kw = dict(K=100, L=100, S=10, R=100, iterations=6, search_L=40, nsg_R=32, search_K=100, massq_S=10,
@@ -176,12 +199,13 @@ def test_build_search_recall(index, oracle, kind):
         front = nxt
     assert seen.all()
     truth, _ = oracle.knn_queries(X, Q, 10)
-    gi, _ = index.search(Q, 64, 10)
-    r_gpu = recall_at(gi, truth, 10)
+    r_gpu = {L: recall_at(index.search(Q, L, 10, init_ids=_cluster_starts(X, Q, ep, L))[0], truth, 10)
+             for L in (12, 16)}
     # the oracle build of the same kind, searched by the same GPU searcher
     kid = {"nsg": 1, "taumng": 3, "alphapg": 4}[kind]
     og, odeg, ost = oracle.build(kid, X, oracle_py.params(**kw), width=g.shape[1], nthreads=8)
     index.set_graph(og, odeg, ost.ep)
-    oi, _ = index.search(Q, 64, 10)
-    r_orc = recall_at(oi, truth, 10)
-    assert abs(r_gpu - r_orc) <= 0.002, (r_gpu, r_orc, st)
+    r_orc = {L: recall_at(index.search(Q, L, 10, init_ids=_cluster_starts(X, Q, ost.ep, L))[0], truth, 10)
+             for L in (12, 16)}
+    for L in (12, 16):
+        assert abs(r_gpu[L] - r_orc[L]) <= 0.002, (L, r_gpu, r_orc, st)
