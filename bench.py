@@ -317,6 +317,33 @@ def roofline(st, hbm_gbs, ld, n, search_k):
                   "kernel": kernels[name], "phase": name, "launches_per_step": int(nl)}
 
 
+def cluster_starts(xlab, qlab, ep, L):
+    """Start nodes per query: the entry point and L - 1 seeded random rows of
+    the mixture component the query was drawn from."""
+    order = np.argsort(xlab, kind="stable")
+    bounds = np.searchsorted(xlab[order], np.arange(int(xlab.max()) + 2))
+    out = np.empty((len(qlab), L), np.uint32)
+    out[:, 0] = ep
+    for qi, c in enumerate(qlab):
+        members = order[bounds[c]:bounds[c + 1]] if c + 1 < len(bounds) else order[:0]
+        if len(members) == 0:
+            members = order
+        out[qi, 1:] = np.random.default_rng(qi).choice(members, size=L - 1, replace=len(members) < L - 1)
+    return out
+
+
+def search_recall10_in_cluster(ix, Q, truth, xlab, qlab, L=16):
+    """Search recall@10 with beams started inside each query's own cluster
+    (the entry point plus L - 1 seeded rows of the query's mixture
+    component).  C2's clusters are islands of the graph at 1M rows, so the
+    entry-point search above mostly measures whether a start lands in the
+    query's cluster; this one measures the graph."""
+    _, _, ep = ix.graph()
+    found, _ = ix.search(Q, L, 10, init_ids=cluster_starts(xlab, qlab, ep, L))
+    hit = sum(len(set(f.tolist()) & set(t.tolist())) for f, t in zip(found, truth))
+    return hit / (10.0 * Q.shape[0])
+
+
 def search_recall10(ix, Q, truth, n, L=100):
     """Index search recall@10 of the context's graph: beam of L from the entry
     point plus L-1 seeded random nodes (the same start for every query and
@@ -496,7 +523,7 @@ def run_gpu(args, ws, rank, local):
 
     torch.cuda.set_device(local)
     n = args.n
-    X = synth.base("c2", n)
+    X, xlab = synth.base_labels("c2", n)
     mode = dict(learned_seed=1, screen=1) if args.mode == "learned_bf16" else {}
     p = kcna.params(**FLAGS, **mode)
     p_plain = kcna.params(**FLAGS)
@@ -516,9 +543,10 @@ def run_gpu(args, ws, rank, local):
         e1.record(stream)
         e1.synchronize()
         plain_ms = e0.elapsed_time(e1) / args.steps
-        Q = synth.queries("c2", 10000)
+        Q, qlab = synth.query_labels("c2", 10000)
         truth, _ = ix.knn_queries(Q, 10)
         plain_rec10, plain_qps = search_recall10(ix, Q, truth, n)
+        plain_rec10_c = search_recall10_in_cluster(ix, Q, truth, xlab, qlab)
         ix.build("nsg", p)
     # timed region: device-resident rows, one build per step
     clock = ClockSampler(local)
@@ -564,10 +592,11 @@ def run_gpu(args, ws, rank, local):
     e2e_s = max_over_ranks(ws, statistics.median(e2e))
     st = stats[-1]
     if plain_ms is None:
-        Q = synth.queries("c2", 10000)
+        Q, qlab = synth.query_labels("c2", 10000)
         truth, _ = ix.knn_queries(Q, 10)
-        plain_rec10 = None
+        plain_rec10 = plain_rec10_c = None
     rec10, qps = search_recall10(ix, Q, truth, n)  # the graph of the last (end-to-end) build
+    rec10_c = search_recall10_in_cluster(ix, Q, truth, xlab, qlab)
     hbm, bf16, src = peaks()
     kname, roof = roofline(st, hbm, (X.shape[1] + 3) // 4 * 4, n, FLAGS["search_K"])
     roof["peak_source"] = f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s"
@@ -604,9 +633,13 @@ def run_gpu(args, ws, rank, local):
                     "learned_bf16_over_plain": round(ms / plain_ms, 4) if plain_ms else None,
                     "search_recall_at_10": round(rec10, 4),
                     "plain_fp32_search_recall_at_10": round(plain_rec10, 4) if plain_rec10 is not None else None,
+                    "search_recall_at_10_in_cluster": round(rec10_c, 4),
+                    "plain_fp32_search_recall_at_10_in_cluster":
+                        round(plain_rec10_c, 4) if plain_rec10_c is not None else None,
                     "search_qps": round(qps),
                     "plain_fp32_search_qps": round(plain_qps) if plain_ms else None,
-                    "search": "10,000 queries, beam 100 from the entry point + 99 seeded random nodes, exact 10-NN"},
+                    "search": "10,000 queries, beam 100 from the entry point + 99 seeded random nodes, exact 10-NN; "
+                              "in_cluster: beam 16 from the entry point + 15 seeded rows of the query's cluster"},
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e_s, 4), "unit": UNIT, "h2d_bytes_per_step": int(n * X.shape[1] * 4),
                 "d2h_bytes_per_step": int(n * W * 4 + n * 4 + 8)},

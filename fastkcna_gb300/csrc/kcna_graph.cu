@@ -983,14 +983,14 @@ __device__ void p2k_tile(const R &rows, int ld, uint32_t N, const uint32_t *s_u,
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(cand_cnt + u, (uint32_t)cnt);
         base = __shfl_sync(KCNA_FULL, base, 0);
-        uint64_t *dst = cand + 2 * (uint64_t)u * CB; // keys at even words (no joiner: no credit)
+        const uint64_t s0 = (uint64_t)u * CB; // whole slots, joiner 0 (no credit)
         if (ok[0]) {
             uint32_t p = base + __popc(m0 & kcna_lanemask_lt());
-            if (p < CB) dst[2 * p] = keys[0];
+            if (p < CB) kcna_cand_put(cand, s0 + p, keys[0], 0u);
         }
         if (ok[1]) {
             uint32_t p = base + __popc(m0) + __popc(m1 & kcna_lanemask_lt());
-            if (p < CB) dst[2 * p] = keys[1];
+            if (p < CB) kcna_cand_put(cand, s0 + p, keys[1], 0u);
         }
     }
     cc = kcna_warp_sum(cc);

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             }
             uint32_t p = cnt ? atomicAdd(a.cand_cnt + u, cnt) : 0u;
             if (__any_sync(KCNA_FULL, cnt != 0u)) { // write pass
-                uint64_t *dst = a.cand + 2 * (uint64_t)u * a.CB; // keys at even words (no joiner: no credit)
+                const uint64_t s0 = (uint64_t)u * a.CB; // whole slots, joiner 0 (no credit)
                 for (int g = gl + h; g <= gh; g += 4) {
                     uint32_t raw[16];
                     tmem_ld16_async(trow + 16 * g, raw);
@@ -333,7 +333,8 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
                                     __fsub_rn(__fadd_rn(nu2, M.col_nrm[col]), 2.f * __uint_as_float(raw[x]));
                                 if (dd <= rad) {
                                     if (p < a.CB)
-                                        dst[2 * p] = kcna_key(dd, w, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW));
+                                        kcna_cand_put(a.cand, s0 + p,
+                                                      kcna_key(dd, w, (uint32_t)(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW)), 0u);
                                     ++p;
                                 }
                             }

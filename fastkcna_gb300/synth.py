@@ -49,7 +49,7 @@ def _centres(name: str) -> np.ndarray:
     raise KeyError(name)
 
 
-def _draw(name: str, n: int, seed: int, chunk: int = 1 << 17) -> np.ndarray:
+def _draw(name: str, n: int, seed: int, chunk: int = 1 << 17, labels: np.ndarray | None = None) -> np.ndarray:
     d = SPECS[name]["d"]
     cen = _centres(name)
     rng = np.random.default_rng(seed)
@@ -58,6 +58,8 @@ def _draw(name: str, n: int, seed: int, chunk: int = 1 << 17) -> np.ndarray:
         e = min(n, s + chunk)
         m = e - s
         lab = rng.integers(0, cen.shape[0], size=m)
+        if labels is not None:
+            labels[s:e] = lab
         if name == "c1":
             x = cen[lab] + 0.1 * rng.standard_normal(size=(m, d))
         elif name in ("c2", "c5"):
@@ -85,6 +87,20 @@ def base(name: str, n: int | None = None) -> np.ndarray:
 def queries(name: str, q: int | None = None) -> np.ndarray:
     """Query rows drawn from the same mixture with the query seed."""
     return _draw(name, SPECS[name]["q"] if q is None else q, SEED_QUERY)
+
+
+def base_labels(name: str, n: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """Base rows (as base()) and the mixture component each was drawn from."""
+    n = SPECS[name]["n"] if n is None else n
+    lab = np.empty(n, np.int32)
+    return _draw(name, n, SEED_BASE, labels=lab), lab
+
+
+def query_labels(name: str, q: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """Query rows (as queries()) and the mixture component each was drawn from."""
+    q = SPECS[name]["q"] if q is None else q
+    lab = np.empty(q, np.int32)
+    return _draw(name, q, SEED_QUERY, labels=lab), lab
 
 
 def write_lshkit(path: str, x: np.ndarray) -> None:
