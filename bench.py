@@ -293,19 +293,28 @@ def run_reference(args, ws, rank):
 def roofline(st, hbm_gbs, ld, n, search_k):
     """Dominant device phase with its algorithmic bytes per launch.
 
-    join:  every gathered row once (BF16 or FP32) + every candidate key written once
+    join:  every gathered row once (BF16 or FP32) + every candidate's key and
+           joiner written once (12 bytes)
     merge: candidates read once, pool entries read and written once
     prune: every candidate row of every node read once (min(pool, search_K) rows)
+    None of the three runs at its memory roof; `limiter` names what the ncu
+    captures under profiles/ show binds each.
     """
     ph, launches = st["phase_ms"], st["phase_launches"]
     rb = 2 if st["bf16_rows"] else 4
     models = {
-        "join": st["join_rows"] * ld * rb + st["cand_emitted"] * 8,
+        "join": st["join_rows"] * ld * rb + st["cand_emitted"] * 12,
         "merge": st["cand_merged"] * 8 + st["pool_entries_merged"] * 16,
         "prune": launches["prune"] * n * min(search_k, st["maxl"]) * ld * rb,
     }
     kernels = {"join": "join_tc_kernel" if st["gram_tc"] else "join_kernel", "merge": "merge_warp_kernel",
                "prune": "prune_gram_kernel" if st.get("prune_tc") else "prune_kernel"}
+    limiters = {
+        "join": "scattered 16-byte candidate-slot stores and the TMEM re-read of the write pass (latency, LSU)",
+        "merge": "shared-memory latency: binary search of every candidate in the node's pool (bank conflicts)",
+        "prune": "issue slots of the mask-building warps; tensor pipe about 30 % busy" if st.get("prune_tc")
+        else "latency of the sequential occlusion scan",
+    }
     name = max(models, key=lambda k: ph.get(k, 0.0))
     ms, nl = ph[name], max(launches[name], 1)
     per_launch_bytes = models[name] / nl
@@ -314,7 +323,8 @@ def roofline(st, hbm_gbs, ld, n, search_k):
     return name, {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
                   "frac": round(achieved / hbm_gbs, 4), "traffic": None,
                   "traffic_note": "DRAM bytes are not measured by this run (ncu captures are separate)",
-                  "kernel": kernels[name], "phase": name, "launches_per_step": int(nl)}
+                  "kernel": kernels[name], "phase": name, "launches_per_step": int(nl),
+                  "limiter": limiters[name]}
 
 
 def cluster_starts(xlab, qlab, ep, L):
