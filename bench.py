@@ -439,9 +439,9 @@ def _search_from_entry(ix, Q, truth, n, ep, L, labels=None):
 def run_workload(args, local):
     """The other named workloads at full size, one JSON line each (not the
     headline measurement): c3 = the layered FastHNSW command line on 1M x 96
-    unit rows, FP32 and BF16-screened; c4 = FastTauMNG on 1M x 960 (FP32
-    kernels); c5 = FastAlphaPG on 2M x 128 integer rows, learned+BF16 and
-    plain FP32.  Times are one build each after the data is on the device
+    unit rows, FP32 and BF16-screened; c4 = FastTauMNG on 1M x 960, plain FP32
+    and with the FP8 E4M3-screened prune; c5 = FastAlphaPG on 2M x 128 integer
+    rows, learned+BF16 and plain FP32.  Times are one build each after the data is on the device
     (c3: the command line's own indexing time, file load excluded)."""
     import tempfile
 
@@ -501,16 +501,23 @@ def run_workload(args, local):
         with kcna.Index(local) as ix:
             ix.upload(X)
             truth, _ = ix.knn_queries(Q, 10)
-            t0 = time.perf_counter()
-            st = ix.build("taumng", kcna.params(**C4_FLAGS))
-            wall = time.perf_counter() - t0
-            _, deg, ep = ix.graph()
-            rec = {L: round(_search_from_entry(ix, Q, truth, X.shape[0], ep, L), 4) for L in (80, 160)}
-        out.update(build_s=round(st["total_time"], 3), wall_s=round(wall, 3), phase_ms={k: round(v, 1) for k, v in
-                   st["phase_ms"].items() if v}, nndescent_iterations=st["iterations"],
-                   knn_recall_at_K=round(st["loop_recall"][-1], 4), n_comps=st["n_comps"],
-                   cand_emitted=st["cand_emitted"], prune_comps=st["prune_comps"], bridge_comps=st["bridge_comps"],
-                   avg_degree=st["aod"], search_recall_at_10=rec, flags=C4_FLAGS, mode="plain FP32")
+            # plain FP32, then the FP8 E4M3-screened prune (BF16 mode at d >= 256)
+            for mode, extra in (("fp32", {}), ("fp8_screen", dict(screen=1))):
+                t0 = time.perf_counter()
+                st = ix.build("taumng", kcna.params(**C4_FLAGS, **extra))
+                wall = time.perf_counter() - t0
+                _, deg, ep = ix.graph()
+                rec = {L: round(_search_from_entry(ix, Q, truth, X.shape[0], ep, L), 4) for L in (80, 160)}
+                out[mode] = dict(build_s=round(st["total_time"], 3), wall_s=round(wall, 3),
+                                 phase_ms={k: round(v, 1) for k, v in st["phase_ms"].items() if v},
+                                 nndescent_iterations=st["iterations"],
+                                 knn_recall_at_K=round(st["loop_recall"][-1], 4), n_comps=st["n_comps"],
+                                 cand_emitted=st["cand_emitted"], prune_comps=st["prune_comps"],
+                                 bridge_comps=st["bridge_comps"], prune_tc=st["prune_tc"],
+                                 prune_exact_pairs=st["prune_exact"], avg_degree=st["aod"],
+                                 search_recall_at_10=rec)
+        out["ratio"] = round(out["fp8_screen"]["build_s"] / out["fp32"]["build_s"], 4)
+        out["flags"] = C4_FLAGS
     elif w == "c5":
         X = synth.base("c5", size)
         with kcna.Index(local) as ix:

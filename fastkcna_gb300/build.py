@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libkcna.so")
-SOURCES = ["kcna_api.cu", "kcna_knn.cu", "kcna_nnd.cu", "kcna_join_tc.cu", "kcna_p2k_tc.cu", "kcna_prune_tc.cu", "kcna_graph.cu", "kcna_noalloc.cu",
+SOURCES = ["kcna_api.cu", "kcna_knn.cu", "kcna_nnd.cu", "kcna_join_tc.cu", "kcna_p2k_tc.cu", "kcna_prune_tc.cu", "kcna_prune_fp8.cu", "kcna_graph.cu", "kcna_noalloc.cu",
            "kcna_tc.cu", "kcna_seed.cu", "kcna_cagra.cu",
            "kcna_pool_search.cu", "kcna_io.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -82,6 +82,7 @@ static void reset_phase_stats(kcna_ctx *c) {
         c->phase_launches[i] = 0;
     }
     c->join_rows = c->cand_emitted = c->cand_merged = c->pool_entries_merged = c->tree_attached = 0;
+    c->prune_exact = 0;
 }
 
 static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
@@ -94,6 +95,7 @@ static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
     st->cand_merged = c->cand_merged;
     st->pool_entries_merged = c->pool_entries_merged;
     st->tree_attached = c->tree_attached;
+    st->prune_exact = c->prune_exact;
 }
 
 kcna_status kcna_dev_malloc(kcna_ctx *c, size_t bytes, void **out, const char *what) {
@@ -246,9 +248,13 @@ __global__ void gram_check_kernel(const float *__restrict__ X, uint32_t n, uint3
 static void release_row_copies(kcna_ctx *c) {
     if (c->Xh) kcna_release(c, c->Xh);
     if (c->norms) kcna_release(c, c->norms);
+    if (c->Xq) kcna_release(c, c->Xq);
+    if (c->qmeta) kcna_release(c, c->qmeta);
     c->Xh = nullptr;
     c->norms = nullptr;
-    c->gram_exact = c->bf16_exact = c->bf16_screen = false;
+    c->Xq = nullptr;
+    c->qmeta = nullptr;
+    c->gram_exact = c->bf16_exact = c->bf16_screen = c->fp8_screen = false;
 }
 
 // BF16 copy rounded to nearest (even) and the squared norms of the rounded
@@ -288,6 +294,8 @@ static kcna_status prepare_rows(kcna_ctx *c, const kcna_params *p, uint32_t *use
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&bad, c->counters + 40, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "bf16 check"));
     if (bad) { // inexact data: FP32 rows everywhere; the join screens on a rounded copy
+        // high dimension: the tau-MNG prune screens on FP8 E4M3 codes instead
+        if (c->d >= 256) return kcna_fp8_rows(c);
         if ((c->ld & 7u) || c->ld > 128) return KCNA_OK;
         KCNA_TRY(kcna_alloc(c, &c->Xh, n, "bf16 rows (rounded)"));
         KCNA_TRY(kcna_alloc(c, &c->norms, c->n_total, "row norms"));
@@ -622,7 +630,8 @@ kcna_status kcna_build(kcna_ctx *c, const kcna_params *p, kcna_kind kind, kcna_s
     }
     st->loops = (uint32_t)loopcount;
     st->prune_tc = kcna_prune_tc_ok(c, kind == KCNA_HNSW_LAYER ? KCNA_NSG : kind, (int)P.nsg_R,
-                                    (int)std::min(P.search_K, c->cap)) ? 1u : 0u;
+                                    (int)std::min(P.search_K, c->cap), P.angle) ? 1u
+                   : kcna_prune_fp8_ok(c, kind, (int)P.nsg_R, (int)std::min(P.search_K, c->cap)) ? 2u : 0u;
     st->prune_comps = prune_comps;
     st->bridge_comps = bridge_comps;
     KCNA_TRY(degree_stats(c, st));
@@ -698,7 +707,9 @@ kcna_status kcna_set_pools(kcna_ctx *c, const kcna_params *p, const uint32_t *id
             keys[(size_t)i * maxl + j] = ((uint64_t)bits << 32) | ((uint64_t)id << 2);
         }
     }
-    KCNA_TRY(kcna_alloc(c, &c->pool, keys.size(), "pool"));
+    // two spare entries: the tile prunes copy pool prefixes from an even index
+    // in 16-byte units, which can reach one entry past the last row
+    KCNA_TRY(kcna_alloc(c, &c->pool, keys.size() + 2, "pool"));
     KCNA_TRY(kcna_alloc(c, &c->pool_cnt, c->n, "pool_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->radius, c->n, "radius"));
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->pool, keys.data(), keys.size() * 8, cudaMemcpyHostToDevice, c->stream), "h2d"));

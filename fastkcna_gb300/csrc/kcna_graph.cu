@@ -22,8 +22,6 @@
 
 namespace {
 
-constexpr double kPi = 3.14159265358979323846264;
-
 struct PruneRule {
     int kind;
     float t3;  // 3 * tau (FP32, src/kgraph.cpp:2859)
@@ -52,14 +50,17 @@ __device__ __forceinline__ bool occludes(const PruneRule &r, float td, float djk
 // at a time against kept[4..nk) with one lane per kept row; finally the batch
 // is resolved in candidate order (the first unoccluded lane is kept and tests
 // the later lanes).  Rows are read through R (FP32 or exact BF16 copy).
+// With nk0 > 0 the scan continues a kept list kid/kd[0, nk0) (from a prune
+// that covered the candidates before `first`) at candidate `first`.
 template <class R, typename GetFn>
 __device__ int warp_prune(const R &rows, uint32_t n_oracle, const PruneRule &rule, int first, int lim, int range,
-                          GetFn get, uint32_t *kid, float *kd, unsigned long long *comps) {
+                          GetFn get, uint32_t *kid, float *kd, unsigned long long *comps, int nk0 = 0) {
     const int lane = kcna_lane();
     const int nv = rows.ld >> 2;
-    if (first >= lim || range <= 0) return 0;
-    int nk = 0;
-    {
+    if (range <= 0) return 0;
+    if (first >= lim) return nk0;
+    int nk = nk0, start = first;
+    if (nk0 == 0) {
         uint32_t id0;
         float d0;
         get(first, id0, d0);
@@ -68,10 +69,11 @@ __device__ int warp_prune(const R &rows, uint32_t n_oracle, const PruneRule &rul
             kd[0] = d0;
         }
         nk = 1;
+        start = first + 1;
     }
     __syncwarp();
     unsigned long long cc = 0;
-    for (int base = first + 1; base < lim && nk < range; base += 32) {
+    for (int base = start; base < lim && nk < range; base += 32) {
         const int i = base + lane;
         uint32_t id = KCNA_NONE;
         float pd = 0.f;
@@ -201,6 +203,57 @@ __global__ void __launch_bounds__(PW * 32) prune_kernel(R rows, uint32_t N, cons
         g_dist[(uint64_t)q * W + j] = j < nk ? kd[j] : 0.f;
     }
     if (lane == 0) g_deg[q] = nk;
+}
+
+// Finishes the prunes a screened tile prune left at the end of its tile
+// (kcna_prune_fp8.cu): each listed item continues its node's kept list g_ids
+// / g_dist[0, g_deg) with the FP32 warp prune from candidate `skip` after the
+// first, the same scan as prune_kernel.  Items index the candidate rows of
+// `keys` (`stride` apart, cnt[row] candidates); with `nodes` the row of item
+// k is k and its node nodes[k] (the link's staged lists), else both are k
+// (the pools).
+template <class R>
+__global__ void __launch_bounds__(PW * 32) prune_resume_kernel(R rows, uint32_t n_oracle,
+                                                               const uint64_t *__restrict__ keys, uint64_t stride,
+                                                               const uint32_t *__restrict__ cnts,
+                                                               const uint32_t *__restrict__ nodes, PruneRule rule,
+                                                               int range, int maxc, int skip,
+                                                               const uint32_t *__restrict__ list,
+                                                               const uint32_t *__restrict__ list_cnt,
+                                                               uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
+                                                               uint32_t *__restrict__ g_deg, uint32_t W,
+                                                               unsigned long long *comps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = kcna_lane();
+    uint32_t *kid = reinterpret_cast<uint32_t *>(smem) + w * 2 * range;
+    float *kd = reinterpret_cast<float *>(kid + range);
+    const uint32_t nl = *list_cnt;
+    for (uint32_t i = blockIdx.x * PW + w; i < nl; i += gridDim.x * PW) {
+        const uint32_t item = list[i];
+        const uint32_t q = nodes ? nodes[item] : item;
+        const uint64_t *pr = keys + (uint64_t)item * stride;
+        const int cnt = (int)cnts[item];
+        const int first = cnt > 0 && kcna_key_id(pr[0]) == q ? 1 : 0;
+        const int lim = max(min(cnt, maxc), first + 1);
+        const int nk0 = (int)min(g_deg[q], (uint32_t)range);
+        for (int j = lane; j < nk0; j += 32) {
+            kid[j] = g_ids[(uint64_t)q * W + j];
+            kd[j] = g_dist[(uint64_t)q * W + j];
+        }
+        __syncwarp();
+        auto get = [&](int i2, uint32_t &id, float &dd) {
+            const uint64_t k = pr[i2];
+            id = kcna_key_id(k);
+            dd = kcna_key_dist(k);
+        };
+        const int nk = nk0 > 0 ? warp_prune(rows, n_oracle, rule, first + skip, lim, range, get, kid, kd, comps, nk0) : 0;
+        for (int j = lane; j < (int)W; j += 32) {
+            g_ids[(uint64_t)q * W + j] = j < nk ? kid[j] : KCNA_NONE;
+            g_dist[(uint64_t)q * W + j] = j < nk ? kd[j] : 0.f;
+        }
+        if (lane == 0) g_deg[q] = (uint32_t)nk;
+        __syncwarp();
+    }
 }
 
 // ---- link: reverse edges -------------------------------------------------
@@ -412,7 +465,9 @@ __global__ void __launch_bounds__(LW_WARPS * 32) link_warp_kernel(R rows, uint32
                                                                  const uint64_t *__restrict__ off,
                                                                  const uint64_t *__restrict__ rev,
                                                                  unsigned long long *comps, uint32_t *big_list,
-                                                                 uint32_t *big_cnt) {
+                                                                 uint32_t *big_cnt, uint64_t *stage,
+                                                                 uint32_t *stage_nodes, uint32_t *stage_cnt,
+                                                                 uint32_t *stage_n) {
     __shared__ uint64_t s_key[LW_WARPS][LW_CAP];
     __shared__ uint32_t s_id[LW_WARPS][LW_CAP];
     __shared__ float s_d[LW_WARPS][LW_CAP];
@@ -478,6 +533,22 @@ __global__ void __launch_bounds__(LW_WARPS * 32) link_warp_kernel(R rows, uint32
         for (int j = lane; j < tp; j += 32)
             key[j] = j < total ? (((uint64_t)__float_as_uint(ds[j]) << 32) | (uint32_t)j) : KCNA_EMPTY_KEY;
         kcna_warp_bitonic(key, tp);
+        if (stage) { // the FP8-screened tile prune takes the list (pool-format keys, LW_CAP apart)
+            uint32_t slot = 0;
+            if (lane == 0) slot = atomicAdd(stage_n, 1u);
+            slot = __shfl_sync(KCNA_FULL, slot, 0);
+            uint64_t *dst = stage + (uint64_t)slot * LW_CAP;
+            for (int j = lane; j < total; j += 32) {
+                const uint32_t p = (uint32_t)key[j];
+                dst[j] = ((uint64_t)__float_as_uint(ds[p]) << 32) | ((uint64_t)ids[p] << 2);
+            }
+            if (lane == 0) {
+                stage_nodes[slot] = q;
+                stage_cnt[slot] = (uint32_t)total;
+            }
+            __syncwarp();
+            continue;
+        }
         auto get = [&](int i, uint32_t &id, float &dd) {
             const uint32_t p = (uint32_t)key[i];
             id = ids[p];
@@ -1063,7 +1134,7 @@ PruneRule make_rule(const kcna_params *p, int kind) {
     PruneRule r;
     r.kind = kind;
     r.t3 = 3.0f * p->tau;
-    r.thr = (float)std::cos((double)(p->angle / 180.0f) * kPi);
+    r.thr = kcna_alpha_threshold(p->angle);
     return r;
 }
 
@@ -1117,8 +1188,24 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     const size_t sm = (size_t)PW * 2 * range * 4;
     const int maxc = (int)std::min(p->search_K, c->cap);
     KCNA_TRY(kcna_phase_begin(c));
-    if (kcna_prune_tc_ok(c, kind, (int)range, maxc)) { // Gram-exact rows: occlusion masks from tensor-core tiles
-        KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, rule.thr, (int)range, maxc, c->counters + 16));
+    if (kcna_prune_tc_ok(c, kind, (int)range, maxc, p->angle)) { // Gram-exact rows: occlusion masks from tensor-core tiles
+        KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, p->angle, (int)range, maxc, c->counters + 16));
+    } else if (kcna_prune_fp8_ok(c, kind, (int)range, maxc)) { // float rows, high d: FP8 screen, FP32 where undecided
+        uint32_t *resume = nullptr;
+        KCNA_TRY(kcna_scratch(c, (size_t)c->n * 4, reinterpret_cast<void **>(&resume)));
+        uint32_t *resume_cnt = reinterpret_cast<uint32_t *>(c->counters + 48);
+        KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 48, 0, 16, c->stream), "memset"));
+        KCNA_TRY(kcna_prune_fp8_launch(c, c->pool, c->cap, c->pool_cnt, nullptr, c->n, c->n, rule.t3, (int)range, maxc,
+                                       resume, resume_cnt, c->counters + 16, c->counters + 49));
+        prune_resume_kernel<<<std::max(1, c->num_sms) * 8, PW * 32, sm, c->stream>>>(
+            RowsF32{c->X, (int)c->ld}, c->n, c->pool, c->cap, c->pool_cnt, nullptr, rule, (int)range, maxc, 128,
+            resume, resume_cnt, c->g_ids, c->g_dist, c->g_deg, c->W, c->counters + 16);
+        KCNA_LAUNCHED(c);
+        KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_resume_kernel"));
+        unsigned long long ex = 0;
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&ex, c->counters + 49, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "prune sync"));
+        c->prune_exact += ex;
     } else {
         if (c->bf16_exact)
             prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
@@ -1177,6 +1264,21 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     if ((s = kcna_alloc(c, &blist, N + 1, "link big list")) != KCNA_OK) return cleanup(), s;
     bcnt = blist + N;
     cudaMemsetAsync(bcnt, 0, 4, c->stream);
+    // FP8 screen (float rows, high d): the warp kernel stages its sorted lists
+    // for the reversed prune, which the tile prune then takes
+    const bool fp8 = kcna_prune_fp8_ok(c, kind, (int)p->nsg_R, 1);
+    uint64_t *stage = nullptr;
+    uint32_t *stage_meta = nullptr; // nodes, counts, resume list (N each), staged count, resume count
+    if (fp8) {
+        if ((s = kcna_alloc(c, &stage, N * LW_CAP + 2, "link stage")) != KCNA_OK) return cleanup(), s;
+        if ((s = kcna_alloc(c, &stage_meta, 3 * N + 2, "link stage lists")) != KCNA_OK) {
+            kcna_release(c, stage);
+            return cleanup(), s;
+        }
+        cudaMemsetAsync(stage_meta + 3 * N, 0, 8, c->stream);
+    }
+    uint32_t *st_nodes = fp8 ? stage_meta : nullptr, *st_cnt = fp8 ? stage_meta + N : nullptr;
+    uint32_t *st_resume = fp8 ? stage_meta + 2 * N : nullptr, *st_n = fp8 ? stage_meta + 3 * N : nullptr;
     auto launch_link = [&](auto rows) -> kcna_status {
         int per_sm = 0;
         KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, link_warp_kernel<decltype(rows)>,
@@ -1186,15 +1288,31 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
                                                            (uint64_t)std::max(c->num_sms, 1) * std::max(per_sm, 1));
         link_warp_kernel<<<grid, LW_WARPS * 32, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids,
                                                                 c->g_dist, c->g_deg, W, off, rev, c->counters + 17,
-                                                                blist, bcnt);
+                                                                blist, bcnt, stage, st_nodes, st_cnt, st_n);
         KCNA_LAUNCHED(c);
-        uint32_t hb = 0;
-        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb, bcnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        uint32_t hb[2] = {0u, 0u};
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb[0], bcnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        if (fp8) KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb[1], st_n, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
         KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync"));
-        if (hb > 0) {
-            link_merge_kernel<<<hb, LT, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids, c->g_dist,
-                                                        c->g_deg, W, off, rev, c->counters + 17, c->d_err, blist);
+        if (hb[0] > 0) {
+            link_merge_kernel<<<hb[0], LT, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids, c->g_dist,
+                                                           c->g_deg, W, off, rev, c->counters + 17, c->d_err, blist);
             KCNA_LAUNCHED(c);
+        }
+        if (fp8 && hb[1] > 0) { // reversed prunes of the staged lists: FP8 tiles, FP32 where undecided or unfinished
+            KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 49, 0, 8, c->stream), "memset"));
+            KCNA_TRY(kcna_prune_fp8_launch(c, stage, LW_CAP, st_cnt, st_nodes, hb[1], 0xFFFFFFFFu, rule.t3,
+                                           (int)p->nsg_R, 0x7FFFFFFF, st_resume, st_n + 1, c->counters + 17,
+                                           c->counters + 49));
+            prune_resume_kernel<<<std::max(1, c->num_sms) * 8, PW * 32, (size_t)PW * 2 * p->nsg_R * 4, c->stream>>>(
+                rows, 0xFFFFFFFFu, stage, LW_CAP, st_cnt, st_nodes, rule, (int)p->nsg_R, 0x7FFFFFFF, 128, st_resume,
+                st_n + 1, c->g_ids, c->g_dist, c->g_deg, W, c->counters + 17);
+            KCNA_LAUNCHED(c);
+            unsigned long long ex = 0;
+            KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&ex, c->counters + 49, 8, cudaMemcpyDeviceToHost, c->stream),
+                                     "d2h"));
+            KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync"));
+            c->prune_exact += ex;
         }
         return kcna_cuda_check(c, cudaGetLastError(), "link kernels");
     };
@@ -1203,6 +1321,8 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     else
         s = launch_link(RowsF32{c->X, (int)c->ld});
     kcna_release(c, blist);
+    if (stage) kcna_release(c, stage);
+    if (stage_meta) kcna_release(c, stage_meta);
     unsigned long long h = 0;
     if (s == KCNA_OK)
         s = kcna_cuda_check(c, cudaMemcpyAsync(&h, c->counters + 17, 8, cudaMemcpyDeviceToHost, c->stream), "d2h");

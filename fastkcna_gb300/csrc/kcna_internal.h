@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <map>
 #include <string>
 #include <thread>
@@ -47,6 +48,15 @@ struct kcna_ctx {
     // screens pairs on Gram tiles of the rounded rows with a bound on the
     // rounding error, then recomputes every emitted pair in FP32 (rescore).
     bool bf16_exact = false, bf16_screen = false;
+    // fp8_screen (BF16 mode, rows inexact in BF16, d >= 256): the tau-MNG
+    // prune screens pairs on FP8 E4M3 Gram tiles (kcna_prune_fp8.cu).  Xq holds
+    // the codes (n_total x ldq bytes, ldq = d rounded up to 128, zero padded),
+    // qmeta per row {scale, squared norm of the decoded row, bound on the
+    // encoding error, 0}.
+    bool fp8_screen = false;
+    uint8_t *Xq = nullptr;
+    float4 *qmeta = nullptr;
+    uint32_t ldq = 0;
 
     // candidate pools: n x cap keys (kcna_common.cuh), counts, filter radius
     uint32_t cap = 0;
@@ -106,6 +116,7 @@ struct kcna_ctx {
     uint64_t phase_launches[KCNA_NUM_PHASES] = {};
     uint64_t launches_at_begin = 0;
     uint64_t join_rows = 0, cand_emitted = 0, cand_merged = 0, pool_entries_merged = 0, tree_attached = 0;
+    uint64_t prune_exact = 0; // undecided pairs of the FP8-screened prunes recomputed in FP32
 };
 
 // Brackets one phase with events on the context stream; end() waits for the
@@ -174,10 +185,28 @@ kcna_status kcna_nnd_join(kcna_ctx *c, const kcna_params *p, int iter, uint64_t 
 // found flags for the entries they inserted below K.
 kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overflow, uint64_t *flagged_topk,
                        uint64_t *merged = nullptr, uint64_t *inserted = nullptr, bool credit_found = false);
+// cos(angle) as the reference's alpha-PG prune computes it (src/kgraph.cpp:3160-3161:
+// the float angle / 180 times the double pi, cos in double, stored as float).
+inline float kcna_alpha_threshold(float angle) {
+    return (float)std::cos((double)(angle / 180.0f) * 3.14159265358979323846264);
+}
 // Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
-bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc);
-kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
+// alpha-PG takes it for angles up to 60 degrees only (angle: degrees).
+bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float angle);
+kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
                                  unsigned long long *comps);
+// tau-MNG prune of float rows on FP8 E4M3 Gram tiles (kcna_prune_fp8.cu);
+// requires c->fp8_screen.  The first 128 candidates of every item are pruned
+// on the tiles; items whose scan ran out of them with fewer than range kept
+// and more candidates left are appended to `resume` (item indices) for the
+// FP32 prune to finish.  keys: candidate keys, row = node (nodes null) or list
+// position, `stride` apart, cnt[row] of them.
+bool kcna_prune_fp8_ok(const kcna_ctx *c, int kind, int range, int maxc);
+kcna_status kcna_fp8_rows(kcna_ctx *c);
+kcna_status kcna_prune_fp8_launch(kcna_ctx *c, const uint64_t *keys, uint64_t stride, const uint32_t *cnt,
+                                  const uint32_t *nodes, uint32_t n_items, uint32_t n_oracle, float t3, int range,
+                                  int maxc, uint32_t *resume, uint32_t *resume_cnt, unsigned long long *comps,
+                                  unsigned long long *exact);
 // P2K join on tcgen05 Gram tiles (kcna_p2k_tc.cu); requires c->gram_exact.
 kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, unsigned long long *comps);
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);

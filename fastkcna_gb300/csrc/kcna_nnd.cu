@@ -1002,7 +1002,9 @@ kcna_status kcna_nnd_alloc(kcna_ctx *c, const kcna_params *p, uint32_t maxl) {
     c->CB = (uint32_t)kcna_pow2_ceil((int)CB);
     c->fwd_new_cap = (std::max<uint32_t>(2 * p->S, 64) + 3) & ~3u;
     c->fwd_old_cap = (std::max<uint32_t>(p->L, 1) + 3) & ~3u;
-    KCNA_TRY(kcna_alloc(c, &c->pool, N * c->cap, "pool"));
+    // two spare entries: the tile prunes copy pool prefixes from an even index
+    // in 16-byte units, which can reach one entry past the last row
+    KCNA_TRY(kcna_alloc(c, &c->pool, N * c->cap + 2, "pool"));
     KCNA_TRY(kcna_alloc(c, &c->pool_cnt, N, "pool_cnt"));
     KCNA_TRY(kcna_alloc(c, &c->radius, N, "radius"));
     KCNA_TRY(kcna_alloc(c, &c->M, N, "M"));

@@ -1,11 +1,12 @@
 // kcna_prune_tc.cu - occlusion prune on tcgen05 Gram tiles.
 //
 // Same result as prune_kernel (kcna_graph.cu; reference nsg_sync_prune
-// src/kgraph.cpp:1809-1851, taumg_sync_prune :2833-2876) for the RNG and
-// tau-MNG rules: the candidates of node q are pool[first .. lim) in order; the
-// first is kept; a later candidate p is dropped when an already kept t
-// occludes it (RNG: d(t,p) < d(q,p); tau-MNG: d(t,p) < d(q,p) - 3 tau), and
-// the scan stops at range kept.  The kernel runs only in Gram-exact mode (integer rows, squared norms
+// src/kgraph.cpp:1809-1851, taumg_sync_prune :2833-2876, alphapg_sync_prune
+// :3157-3203) for the RNG, tau-MNG and alpha-PG rules: the candidates of node
+// q are pool[first .. lim) in order; the first is kept; a later candidate p
+// is dropped when an already kept t occludes it (RNG: d(t,p) < d(q,p);
+// tau-MNG: d(t,p) < d(q,p) - 3 tau; alpha-PG: d(t,p) < d(q,p) and the angle
+// at t below the threshold angle), and the scan stops at range kept.  The kernel runs only in Gram-exact mode (integer rows, squared norms
 // below 2^23), where the tile distances (|x|^2 + |y|^2) - 2 <x, y> (BF16
 // rows, FP32 accumulation in TMEM) equal the canonical FMA-chain distances,
 // so the kept lists are identical.
@@ -99,7 +100,7 @@ struct PgArgs {
     const uint16_t *rows; // BF16 rows, ld elements apart
     const uint32_t *pool_cnt;
     const float *norms;
-    float t3, thr;
+    float aux, thr; // aux: 3 tau (tau-MNG) or the angle screen's margin 4m (alpha-PG)
     int range, maxc;
     uint32_t *g_ids;
     float *g_dist;
@@ -120,18 +121,58 @@ __device__ __forceinline__ void cp_async_wait_0() {
 // difference to the bound is the result of the FP32 comparison.  For RNG the
 // column value is pd - |p|^2 (an exact integer difference in Gram-exact mode:
 // pool distances are canonical distances of integer rows), one add fewer.
-template <int RULE>
-__device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float td, float t3, float thr) {
-    if (RULE == 0) return __float_as_uint(__fsub_rn(__fmaf_rn(-2.f, g, nt), pd)); // pd holds pd - |p|^2
-    const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
-    if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, t3))); // src/kgraph.cpp:2859
-    return __float_as_uint(__fsub_rn(dd, pd));
+// The alpha-PG angle test exactly as the FP32 prune and the reference evaluate
+// it (src/kgraph.cpp:3181-3183): cos = ((td + djk) - pd) / 2 / sqrt(td * djk),
+// IEEE operations in that order, compared with the FP32 threshold.
+__device__ __noinline__ bool alpha_angle_exact(float td, float djk, float pd, float thr) {
+    const float num = __fdiv_rn(__fsub_rn(__fadd_rn(td, djk), pd), 2.0f);
+    const float cs = __fdiv_rn(num, __fsqrt_rn(__fmul_rn(td, djk)));
+    return cs < thr;
 }
 
-// RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG.  alpha-PG is left to the FP32
-// prune: its angle test (two IEEE divisions and a square root) on every near
-// pair of the triangle made the tile version ten times slower than RNG (3.9 s
-// vs 0.37 s per 2M-row build, against 1.15 s for the sequential FP32 prune).
+// alpha-PG (RULE 2) without the angle arithmetic on almost every pair.  The
+// candidates are sorted by distance to the node, so a = d(q,t) <= c = d(q,p),
+// and the occlusion needs b = d(t,p) < c: qp is then the longest side of the
+// triangle q, t, p and the angle at t its largest, at least 60 degrees.  With
+// x = 1 - a/c, y = 1 - b/c and s = x + y = (2c - a - b) / c,
+//   cos(t) = (1 - s) / (2 sqrt((1 - x)(1 - y))),
+// and for s < 1 the root is at least sqrt(1 - s) ((1 - x)(1 - y) = 1 - s + xy),
+// so cos(t) <= sqrt(1 - s) / 2 <= 1/2 - s/4; for s >= 1, cos(t) <= 0.  With
+// the threshold thr = cos(angle) >= cos(60 degrees) and m = 1/2 - thr + 1e-5
+// (the 1e-5 covers the few-ulp error of the FP32 formula: Gram-exact distances
+// are integers, so a nonzero side is at least 1), s > 4m proves cos(t) < thr
+// and the pair is occluded as under RNG.  Only near-equilateral pairs
+// (2c - a - b <= 4m c + 8; rounding of the float differences of integers
+// below 2^25 is at most 4) and pairs with a zero side (the formula divides by
+// zero: -inf, or NaN for duplicate rows t, p) take the exact test.
+
+// A word whose sign bit says whether t occludes p, from the Gram entry g:
+// |t|^2 - 2g + |p|^2 is exact in Gram-exact mode, and the sign of its
+// difference to the bound is the result of the FP32 comparison.  For RNG the
+// column value is pd - |p|^2 (an exact integer difference in Gram-exact mode:
+// pool distances are canonical distances of integer rows), one add fewer.
+// For alpha-PG (RULE 2) the sign bit is set for the pairs the screen proves
+// occluded, and *amb receives whether the pair needs the exact test (RNG
+// holds but the screen cannot decide the angle); branch-free, so that the
+// 32 pairs of a word stay straight-line code.
+template <int RULE>
+__device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float td, float aux,
+                                              bool *amb) {
+    if (RULE == 0) return __float_as_uint(__fsub_rn(__fmaf_rn(-2.f, g, nt), pd)); // pd holds pd - |p|^2
+    const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
+    if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, aux))); // src/kgraph.cpp:2859
+    const float s = __fsub_rn(__fsub_rn(__fadd_rn(pd, pd), td), dd);
+    const bool rng = dd < pd;
+    const bool fast = td > 0.f && dd > 0.f && s > __fmaf_rn(aux, pd, 8.f);
+    *amb = rng && !fast;
+    return rng && fast ? 0x80000000u : 0u;
+}
+
+// RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG, 2 alpha-PG (angles up to 60
+// degrees; wider angles stay on the FP32 prune, whose per-pair angle test the
+// screen above cannot skip: evaluated on every near pair of the triangle it
+// made the tile version ten times slower than RNG, 3.9 s against 0.37 s per
+// 2M-row build).
 template <int RULE>
 __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -382,6 +423,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             for (int J = 0; J < nch && ok; ++J) {
                 const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
                 const float n_t = M.nrm[t], td = M.pd[t];
+                const uint32_t id_t = RULE == 2 ? kcna_key_id(M.key[M.koff + t]) : 0u;
                 for (int I = J; I < nch; ++I, ++acount) {
                     const int b = (int)(acount % NACC);
                     mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
@@ -412,21 +454,40 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                             const float4 *pd4 = reinterpret_cast<const float4 *>(M.pd + p0);
                             // four chains of eight: candidate 8j+m ends in bit 7-m of wq[j]
                             uint32_t wq[4] = {0u, 0u, 0u, 0u};
+                            uint32_t amb = 0u; // alpha-PG: pairs left to the exact angle test (bit = candidate - p0)
 #pragma unroll
                             for (int u4 = 0; u4 < 8; ++u4) {
                                 const float4 n4 = np4[u4], d4 = pd4[u4];
                                 const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
                                 for (int v = 0; v < 4; ++v) {
+                                    bool am = false;
                                     const uint32_t sg = occl_sign<RULE>(__uint_as_float(raw[32 * ww + 4 * u4 + v]),
-                                                                        n_t, nn[v], dv[v], td, a.t3, a.thr);
+                                                                        n_t, nn[v], dv[v], td, a.aux, &am);
                                     wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
+                                    if (RULE == 2) amb |= (am ? 1u : 0u) << (4 * u4 + v);
                                 }
                             }
                             word = __brev((wq[0] << 24) | (wq[1] << 16) | (wq[2] << 8) | wq[3]);
                             if (I == J) { // only candidates after t
                                 const int r = t - p0;
-                                word = r < 0 ? word : r >= 31 ? 0u : word & ~((2u << r) - 1u);
+                                const uint32_t after = r < 0 ? 0xFFFFFFFFu : r >= 31 ? 0u : ~((2u << r) - 1u);
+                                word &= after;
+                                amb &= after;
+                            }
+                            if (RULE == 2) { // near-equilateral pairs and zero sides: the exact test (rare)
+                                // only between candidates of this node: rows and columns beyond nc hold
+                                // stale keys (their bits are never read by the scan)
+                                const int nv = (int)M.nc - p0;
+                                amb &= t >= (int)M.nc || nv <= 0 ? 0u : nv >= 32 ? 0xFFFFFFFFu : (1u << nv) - 1u;
+                                while (amb) {
+                                    const int v = __ffs(amb) - 1;
+                                    amb &= amb - 1u;
+                                    const uint32_t id_p = kcna_key_id(M.key[M.koff + p0 + v]);
+                                    if (id_t >= a.N || id_p >= a.N) continue; // beyond the layer prefix: dead
+                                    const float djk = rows_l2(RowsB16{a.rows, (int)a.ld}, id_t, id_p);
+                                    if (alpha_angle_exact(td, djk, M.pd[p0 + v], a.thr)) word |= 1u << v;
+                                }
                             }
                         }
                         mask[mask_base(4 * I + CW / 32 * h + ww) + t] = word;
@@ -511,14 +572,17 @@ kcna_status launch_rule(kcna_ctx *c, const PgArgs &a, uint32_t grid) {
 
 } // namespace
 
-bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc) {
-    return kind != KCNA_ALPHAPG && c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range >= 1 && maxc >= 1 &&
+bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float angle) {
+    // alpha-PG: the angle screen proves the test for thresholds cos(angle) >= cos(60 degrees)
+    if (kind == KCNA_ALPHAPG && !(kcna_alpha_threshold(angle) >= kcna_alpha_threshold(60.f))) return false;
+    return c->gram_exact && c->Xh && c->norms && !(c->ld & 7u) && c->ld <= 128 && range >= 1 && maxc >= 1 &&
            maxc <= MAXC && prune_gram_smem() <= 227 * 1024;
 }
 
-kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int range, int maxc,
+kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
                                  unsigned long long *comps) {
-    if (!kcna_prune_tc_ok(c, kind, range, maxc)) return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
+    if (!kcna_prune_tc_ok(c, kind, range, maxc, angle))
+        return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
     PgArgs a;
     a.N = c->n;
     a.cap = c->cap;
@@ -528,8 +592,9 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int
     a.rows = c->Xh;
     a.pool_cnt = c->pool_cnt;
     a.norms = c->norms;
-    a.t3 = t3;
-    a.thr = thr;
+    a.thr = kcna_alpha_threshold(angle);
+    // tau-MNG: 3 tau; alpha-PG: 4m, m = 1/2 - thr + 1e-5 (the angle screen's margin)
+    a.aux = kind == KCNA_TAUMNG ? t3 : kind == KCNA_ALPHAPG ? (float)(4.0 * (0.5 - (double)a.thr + 1e-5)) : 0.f;
     a.range = range;
     a.maxc = maxc;
     a.g_ids = c->g_ids;
@@ -540,5 +605,6 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float thr, int
     const uint32_t grid = (uint32_t)std::min<uint64_t>(c->n, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
     if (kind == KCNA_TAUMNG) return launch_rule<1>(c, a, grid);
+    if (kind == KCNA_ALPHAPG) return launch_rule<2>(c, a, grid);
     return launch_rule<0>(c, a, grid);
 }

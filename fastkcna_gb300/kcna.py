@@ -68,7 +68,8 @@ class Stats(C.Structure):
         ("iter_cand", C.c_uint64 * MAX_ITERS), ("iter_inserted", C.c_uint64 * MAX_ITERS),
         ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
         ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
-        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32), ("prune_tc", C.c_uint32)]
+        ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32), ("prune_tc", C.c_uint32),
+        ("prune_exact", C.c_uint64)]
 
     def as_dict(self):
         it = self.iterations
@@ -92,7 +93,8 @@ class Stats(C.Structure):
                     seed_train_ms=self.seed_train_ms, seed_total_ms=self.seed_total_ms,
                     seed_loss_first=self.seed_loss_first, seed_loss_last=self.seed_loss_last,
                     seed_input_scale=self.seed_input_scale, seed_recall=self.seed_recall,
-                    seed_comps=self.seed_comps, bf16_rows=self.bf16_rows, gram_tc=self.gram_tc, prune_tc=self.prune_tc)
+                    seed_comps=self.seed_comps, bf16_rows=self.bf16_rows, gram_tc=self.gram_tc, prune_tc=self.prune_tc,
+                    prune_exact=self.prune_exact)
 
 
 _lib = None

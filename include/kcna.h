@@ -51,10 +51,12 @@ typedef enum {
     KCNA_REFINE_POOL_SEARCH = 1  /* per-node pool search, inSearch (:2340-2414, :3667-3688) */
 } kcna_refine;
 
-/* Distance screening forms for the local join and the P2K join. */
+/* Distance screening forms for the local join, the P2K join and the prune. */
 typedef enum {
     KCNA_SCREEN_FP32 = 0, /* plain FP32, the drop-in */
-    KCNA_SCREEN_BF16 = 1  /* BF16 tensor-core Gram screen + FP32 re-rank of survivors */
+    KCNA_SCREEN_BF16 = 1  /* BF16 tensor-core Gram screen + FP32 re-rank of survivors (d <= 128);
+                             at d >= 256 the tau-MNG prune screens on FP8 E4M3 Gram tiles with
+                             per-vector scales and recomputes undecided pairs in FP32 */
 } kcna_screen;
 
 /* Build parameters.  Field meaning and defaults follow kgraph::KGraph::IndexParams
@@ -161,7 +163,10 @@ typedef struct {
     uint32_t gram_tc;          /* local join on tensor-core Gram tiles: 1 exact (integer rows,
                                   squared norms < 2^23), 2 screening of rows rounded to BF16 with
                                   FP32 recompute of the emitted pairs; d <= 128, a multiple of 8 */
-    uint32_t prune_tc;         /* 1: the occlusion prunes ran on tensor-core Gram tiles (Gram-exact rows) */
+    uint32_t prune_tc;         /* 1: the occlusion prunes ran on tensor-core Gram tiles (Gram-exact rows);
+                                  2: the tau-MNG prunes screened float rows on FP8 E4M3 Gram tiles
+                                  (d >= 256), undecided pairs recomputed in FP32 */
+    uint64_t prune_exact;      /* pairs of the FP8-screened prunes recomputed in FP32 */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;

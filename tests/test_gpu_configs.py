@@ -1,8 +1,9 @@
 """The workload shapes beyond the headline build: C4's high dimension
 (d = 960, FastTauMNG, tau = 10) on the FP32 kernels, with the prune checked
-bit for bit against the oracle on the GPU's own pools, and C5's size
-(2M x 128 integer rows, FastAlphaPG, learned seed + BF16) against the plain
-FP32 build of the same rows."""
+bit for bit against the oracle on the GPU's own pools (the FP8-screened prune
+of the same rows is pinned in test_gpu_prune_fp8.py), and C5's size (2M x
+128 integer rows, FastAlphaPG, learned seed + BF16, the alpha-PG prune on Gram
+tiles) against the plain FP32 build of the same rows."""
 import numpy as np
 import pytest
 
@@ -61,11 +62,12 @@ def test_c5_two_million_alphapg_learned_bf16():
         g1, d1, _ = ix.graph()
         st0 = ix.build("alphapg", kcna.params(**kw))
         g0, d0, _ = ix.graph()
-    assert st["gram_tc"] == 1 and st["prune_tc"] == 0  # alpha-PG prunes on the FP32 kernel
+    assert st["gram_tc"] == 1 and st["prune_tc"] == 1  # alpha-PG (angle 60) prunes on the Gram tiles
     assert st["loop_recall"][-1] >= 0.99 and st0["loop_recall"][-1] >= 0.99
     assert st["iterations"] < st0["iterations"]  # the learned seed cuts NN-descent iterations
     assert d1.max() <= 50 and d0.max() <= 50
     assert abs(float(d1.mean()) - float(d0.mean())) < 0.5
+    assert st["phase_ms"]["prune"] < st0["phase_ms"]["prune"]
     print(f"\nC5 2M alpha-PG: learned+BF16 {st['total_time']:.2f} s ({st['iterations']} iterations), "
           f"plain FP32 {st0['total_time']:.2f} s ({st0['iterations']} iterations)")
 

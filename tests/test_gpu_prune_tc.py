@@ -2,7 +2,8 @@
 given the same pools, the kept lists equal the FP32 prune's and the oracle's
 (the reference's nsg_sync_prune / taumg / alphapg rules) exactly, for the
 three rules, with candidate lists spanning one to four 128-row chunks, range
-stops, repeated ids (also across a chunk boundary) and a layer prefix."""
+stops, repeated ids (also across a chunk boundary), duplicate rows (the
+alpha-PG angle formula's 0/0) and a layer prefix."""
 import numpy as np
 import pytest
 
@@ -79,3 +80,27 @@ def test_gram_prune_layer_prefix(index, c2_rows):
     g1, deg1, _ = _prune(index, ids, d, cnt, "hnsw", 1, **kw)
     assert g1.shape[0] == n
     assert np.array_equal(deg0, deg1) and np.array_equal(g0, g1)
+
+
+@pytest.mark.parametrize("angle", [45.0, 60.0, 75.0])
+def test_gram_alphapg_duplicate_rows(index, oracle, c2_rows, angle):
+    """alpha-PG on rows with exact duplicates (distinct ids, equal vectors).
+    Two duplicates t, p are at one distance from the node and at distance 0
+    from each other, where the reference's angle formula divides 0 by 0 (NaN:
+    not occluded); the tile path must take its exact test there.  Angles up to
+    60 degrees run on the tiles, 75 on the FP32 prune in both modes."""
+    X = c2_rows[:6000].copy()
+    X[1::9] = X[0::9][: len(X[1::9])]  # row 9i+1 repeats row 9i
+    ids, d, cnt = _pools(index, X, 400, dups=False)
+    kw = dict(K=400, L=400, search_K=400, nsg_R=50, angle=angle)
+    g0, deg0, _ = _prune(index, ids, d, cnt, "alphapg", 0, **kw)
+    g1, deg1, _ = _prune(index, ids, d, cnt, "alphapg", 1, **kw)
+    assert np.array_equal(deg0, deg1) and np.array_equal(g0, g1)
+    oi, od, odeg = oracle.prune(KIND_CODE["alphapg"], X, oracle_py.params(**kw), ids, d, cnt, g1.shape[1])
+    assert np.array_equal(deg1, odeg) and np.array_equal(g1, oi)
+    # duplicates stay side by side in the kept lists (neither occludes the other)
+    pairs = 0
+    for i in range(6000):
+        kept = set(g1[i, : deg1[i]].tolist())
+        pairs += sum(1 for j in kept if j % 9 == 0 and j + 1 in kept)
+    assert pairs > 0
