@@ -365,6 +365,10 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
     constexpr int NW = merge_warps(SURV, CREDIT);
     for (uint32_t node = blockIdx.x * NW + w; node < N; node += gridDim.x * NW) {
         const uint32_t raw = a.cand_cnt[node];
+        // a refinement round leaves most pools without candidates: their pool,
+        // count and radius stand (an NN-descent merge still counts every
+        // pool's flagged entries for its delta, so it visits them all)
+        if (!CREDIT && raw == 0) continue;
         const uint32_t nc = min(raw, a.CB);
         const uint32_t np = min(a.pool_cnt[node], a.limit);
         uint64_t *gp = a.pool + (uint64_t)node * a.cap;
@@ -414,14 +418,9 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
         } else {
             uint32_t nu = 0; // distinct survivors
             if (ns > 0) {
-                const int p2 = kcna_pow2_ceil_d((int)ns);
-                for (int i = (int)ns + lane; i < p2; i += 32) {
-                    s_sv[i] = KCNA_EMPTY_KEY;
-                    if (CREDIT) s_j[i] = 0xFFFFu;
-                }
                 __syncwarp();
                 if (CREDIT) {
-                    kcna_warp_bitonic_kv16(s_sv, s_j, p2);
+                    kcna_warp_sort_n<true>(s_sv, s_j, (int)ns);
                     // copies of one key are adjacent: each distinct survivor whose
                     // rank (distinct index + position in the pool) is below K
                     // credits the lowest joiner among its copies
@@ -446,7 +445,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                     }
                     __syncwarp();
                 } else {
-                    kcna_warp_bitonic(s_sv, p2);
+                    kcna_warp_sort_n<false>(s_sv, nullptr, (int)ns);
                 }
                 // drop repeats among survivors (same distance and id are adjacent);
                 // compaction moves entries down, so the previous key comes from

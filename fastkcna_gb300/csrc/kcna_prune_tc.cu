@@ -142,30 +142,38 @@ __device__ __noinline__ bool alpha_angle_exact(float td, float djk, float pd, fl
 // (the 1e-5 covers the few-ulp error of the FP32 formula: Gram-exact distances
 // are integers, so a nonzero side is at least 1), s > 4m proves cos(t) < thr
 // and the pair is occluded as under RNG.  Only near-equilateral pairs
-// (2c - a - b <= 4m c + 8; rounding of the float differences of integers
-// below 2^25 is at most 4) and pairs with a zero side (the formula divides by
-// zero: -inf, or NaN for duplicate rows t, p) take the exact test.
+// (2c - a - b within 4m c + 16 of zero, alpha_signs below) and pairs with
+// b = 0 (duplicate rows: the formula's 0/0 is NaN, not occluded) take the
+// exact test.
 
 // A word whose sign bit says whether t occludes p, from the Gram entry g:
 // |t|^2 - 2g + |p|^2 is exact in Gram-exact mode, and the sign of its
 // difference to the bound is the result of the FP32 comparison.  For RNG the
 // column value is pd - |p|^2 (an exact integer difference in Gram-exact mode:
 // pool distances are canonical distances of integer rows), one add fewer.
-// For alpha-PG (RULE 2) the sign bit is set for the pairs the screen proves
-// occluded, and *amb receives whether the pair needs the exact test (RNG
-// holds but the screen cannot decide the angle); branch-free, so that the
-// 32 pairs of a word stay straight-line code.
 template <int RULE>
-__device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float td, float aux,
-                                              bool *amb) {
+__device__ __forceinline__ uint32_t occl_sign(float g, float nt, float np, float pd, float aux) {
     if (RULE == 0) return __float_as_uint(__fsub_rn(__fmaf_rn(-2.f, g, nt), pd)); // pd holds pd - |p|^2
     const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
-    if (RULE == 1) return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, aux))); // src/kgraph.cpp:2859
-    const float s = __fsub_rn(__fsub_rn(__fadd_rn(pd, pd), td), dd);
-    const bool rng = dd < pd;
-    const bool fast = td > 0.f && dd > 0.f && s > __fmaf_rn(aux, pd, 8.f);
-    *amb = rng && !fast;
-    return rng && fast ? 0x80000000u : 0u;
+    return __float_as_uint(__fsub_rn(dd, __fsub_rn(pd, aux))); // src/kgraph.cpp:2859
+}
+
+// alpha-PG (RULE 2): three sign words per 32 pairs, branch-free.  With a =
+// td, c = pd and b = dd (integers in Gram-exact mode):
+//   r: b < c                                   (the RNG part of the rule)
+//   o: b < min(c, (2 - 4m) c - 16 - a)         (the screen: 2c - a - b > 4m c
+//      with room for the FMA's rounding, at most 4; m <= c, so o implies r)
+//   z: b > 1/2                                 (no zero side: the formula's 0/0)
+// o & z: proven occluded; r & ~(o & z): the exact test.  A zero a needs no
+// test: the formula then gives -inf, occluded whenever b < c.  k2 = 2 - 4m,
+// ctd = -16 - a (per row).
+__device__ __forceinline__ void alpha_signs(float g, float nt, float np, float pd, float k2, float ctd, uint32_t &r,
+                                            uint32_t &o, uint32_t &z) {
+    const float dd = __fadd_rn(__fmaf_rn(-2.f, g, nt), np);
+    const float m = fminf(pd, __fmaf_rn(k2, pd, ctd));
+    r = __float_as_uint(__fsub_rn(dd, pd));
+    o = __float_as_uint(__fsub_rn(dd, m));
+    z = __float_as_uint(__fsub_rn(0.5f, dd));
 }
 
 // RULE: 0 RNG (NSG, HNSW layers), 1 tau-MNG, 2 alpha-PG (angles up to 60
@@ -424,6 +432,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                 const int t = J * PC + 32 * qt + lane; // occluder candidate (TMEM lane)
                 const float n_t = M.nrm[t], td = M.pd[t];
                 const uint32_t id_t = RULE == 2 ? kcna_key_id(M.key[M.koff + t]) : 0u;
+                const float k2 = 2.f - a.aux, ctd = -16.f - td; // alpha-PG screen (alpha_signs)
                 for (int I = J; I < nch; ++I, ++acount) {
                     const int b = (int)(acount % NACC);
                     mine = mbar_wait(&S.acc_full[b], (acount / NACC) & 1);
@@ -454,21 +463,34 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                             const float4 *pd4 = reinterpret_cast<const float4 *>(M.pd + p0);
                             // four chains of eight: candidate 8j+m ends in bit 7-m of wq[j]
                             uint32_t wq[4] = {0u, 0u, 0u, 0u};
-                            uint32_t amb = 0u; // alpha-PG: pairs left to the exact angle test (bit = candidate - p0)
+                            uint32_t wo[4] = {0u, 0u, 0u, 0u}, wz[4] = {0u, 0u, 0u, 0u}; // alpha-PG
 #pragma unroll
                             for (int u4 = 0; u4 < 8; ++u4) {
                                 const float4 n4 = np4[u4], d4 = pd4[u4];
                                 const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
                                 for (int v = 0; v < 4; ++v) {
-                                    bool am = false;
-                                    const uint32_t sg = occl_sign<RULE>(__uint_as_float(raw[32 * ww + 4 * u4 + v]),
-                                                                        n_t, nn[v], dv[v], td, a.aux, &am);
-                                    wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
-                                    if (RULE == 2) amb |= (am ? 1u : 0u) << (4 * u4 + v);
+                                    const float g = __uint_as_float(raw[32 * ww + 4 * u4 + v]);
+                                    if (RULE == 2) {
+                                        uint32_t r, o, z;
+                                        alpha_signs(g, n_t, nn[v], dv[v], k2, ctd, r, o, z);
+                                        wq[u4 >> 1] = __funnelshift_l(r, wq[u4 >> 1], 1);
+                                        wo[u4 >> 1] = __funnelshift_l(o, wo[u4 >> 1], 1);
+                                        wz[u4 >> 1] = __funnelshift_l(z, wz[u4 >> 1], 1);
+                                    } else {
+                                        const uint32_t sg = occl_sign<RULE>(g, n_t, nn[v], dv[v], a.aux);
+                                        wq[u4 >> 1] = __funnelshift_l(sg, wq[u4 >> 1], 1); // shifts the sign bit in
+                                    }
                                 }
                             }
                             word = __brev((wq[0] << 24) | (wq[1] << 16) | (wq[2] << 8) | wq[3]);
+                            uint32_t amb = 0u; // alpha-PG: pairs left to the exact angle test (bit = candidate - p0)
+                            if (RULE == 2) {
+                                const uint32_t occ = __brev((wo[0] << 24) | (wo[1] << 16) | (wo[2] << 8) | wo[3]) &
+                                                     __brev((wz[0] << 24) | (wz[1] << 16) | (wz[2] << 8) | wz[3]);
+                                amb = word & ~occ;
+                                word = occ;
+                            }
                             if (I == J) { // only candidates after t
                                 const int r = t - p0;
                                 const uint32_t after = r < 0 ? 0xFFFFFFFFu : r >= 31 ? 0u : ~((2u << r) - 1u);

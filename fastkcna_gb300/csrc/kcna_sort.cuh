@@ -71,6 +71,43 @@ __device__ __forceinline__ void kcna_warp_bitonic_kv16(uint64_t *s, uint16_t *v,
     __syncwarp();
 }
 
+// Ascending sort of s[0, n), any n >= 1, by one warp in shared memory: the
+// bitonic network in its flip form (every comparator puts the smaller key at
+// the lower index), padded to the next power of two with virtual +infinite
+// keys.  A comparator that touches a virtual key leaves both in place, so
+// only the comparators inside [0, n) run and nothing beyond n is read or
+// written.  With KV every key carries a 16-bit value from v (values of equal
+// keys end in no particular order).
+template <bool KV>
+__device__ __forceinline__ void kcna_warp_sort_n(uint64_t *s, uint16_t *v, int n) {
+    const int lane = kcna_lane();
+    int p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (int size = 2; size <= p2; size <<= 1) {
+        const int half = size >> 1;
+        for (int stride = half; stride > 0; stride >>= 1) {
+            __syncwarp();
+            const bool flip = stride == half;
+            for (int t = lane; t < (p2 >> 1); t += 32) {
+                const int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                const int j = flip ? (i ^ (size - 1)) : i + stride;
+                if (j >= n) continue;
+                const uint64_t a = s[i], b = s[j];
+                if (b < a) {
+                    s[i] = b;
+                    s[j] = a;
+                    if (KV) {
+                        const uint16_t va = v[i];
+                        v[i] = v[j];
+                        v[j] = va;
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // Ascending bitonic sort of n (a power of two) (key, value) pairs in shared
 // memory by the whole thread block, ordered by key then value: among equal
 // keys the pair with the smallest value comes first.  Ends with a
