@@ -423,25 +423,35 @@ __global__ void __launch_bounds__(MW_WARPS * 32) merge_warp_kernel(MergeArgs a, 
                     kcna_warp_sort_n<true>(s_sv, s_j, (int)ns);
                     // copies of one key are adjacent: each distinct survivor whose
                     // rank (distinct index + position in the pool) is below K
-                    // credits the lowest joiner among its copies
-                    uint64_t carry = KCNA_EMPTY_KEY;
+                    // credits the lowest joiner among its copies.  Four batches of
+                    // 32 at a time: their first joiners are loaded together, so the
+                    // L2 round trips overlap.
                     uint32_t q0 = 0;
-                    for (uint32_t b0 = 0; b0 < ns; b0 += 32) {
-                        const uint32_t j = b0 + lane;
-                        const uint64_t k = j < ns ? s_sv[j] : KCNA_EMPTY_KEY;
-                        uint64_t prev = __shfl_up_sync(KCNA_FULL, k, 1);
-                        if (lane == 0) prev = carry;
-                        const bool start = j < ns && (j == 0 || (prev >> 2) != (k >> 2));
-                        const unsigned m = __ballot_sync(KCNA_FULL, start);
-                        const uint32_t q = q0 + __popc(m & kcna_lanemask_lt());
-                        if (start && q + (uint32_t)kcna_lower_bound(s_pool, (int)np, k) < a.K) {
-                            uint32_t best = KCNA_NONE;
-                            for (uint32_t x = j; x < ns && (s_sv[x] >> 2) == (k >> 2); ++x)
+                    for (uint32_t b0 = 0; b0 < ns; b0 += 128) {
+                        uint64_t kv[4];
+                        uint32_t bv[4];
+                        bool cr[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t j = b0 + 32 * u + lane;
+                            const uint64_t k = j < ns ? s_sv[j] : KCNA_EMPTY_KEY;
+                            const uint64_t prev = j > 0 && j < ns ? s_sv[j - 1] : KCNA_EMPTY_KEY;
+                            const bool start = j < ns && (j == 0 || (prev >> 2) != (k >> 2));
+                            const unsigned m = __ballot_sync(KCNA_FULL, start);
+                            const uint32_t q = q0 + __popc(m & kcna_lanemask_lt());
+                            q0 += __popc(m);
+                            cr[u] = start && q + (uint32_t)kcna_lower_bound(s_pool, (int)np, k) < a.K;
+                            kv[u] = k;
+                            bv[u] = cr[u] ? (uint32_t)gc[2 * s_j[j] + 1] : KCNA_NONE;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            if (!cr[u]) continue;
+                            uint32_t best = bv[u];
+                            for (uint32_t x = b0 + 32 * u + lane + 1; x < ns && (s_sv[x] >> 2) == (kv[u] >> 2); ++x)
                                 best = min(best, (uint32_t)gc[2 * s_j[x] + 1]);
                             if (best < a.n_nodes) a.found[best] = 1;
                         }
-                        carry = __shfl_sync(KCNA_FULL, k, 31);
-                        q0 += __popc(m);
                     }
                     __syncwarp();
                 } else {

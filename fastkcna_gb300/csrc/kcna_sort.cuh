@@ -88,7 +88,10 @@ __device__ __forceinline__ void kcna_warp_sort_n(uint64_t *s, uint16_t *v, int n
         for (int stride = half; stride > 0; stride >>= 1) {
             __syncwarp();
             const bool flip = stride == half;
-            for (int t = lane; t < (p2 >> 1); t += 32) {
+            // pairs are numbered in increasing order of their lower index i:
+            // those with i < n come first
+            const int tmax = (n / (2 * stride)) * stride + min(n % (2 * stride), stride);
+            for (int t = lane; t < tmax; t += 32) {
                 const int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
                 const int j = flip ? (i ^ (size - 1)) : i + stride;
                 if (j >= n) continue;
