@@ -948,18 +948,21 @@ __global__ void bridge_update_kernel(uint64_t *__restrict__ pool, const uint32_t
         unsigned mk = __ballot_sync(KCNA_FULL, f);
         uint32_t rank = taken + __popc(mk & kcna_lanemask_lt());
         bool take = f && (!capped || rank < S_);
-        if (take) {
-            uint32_t tgt = kcna_key_id(k);
-            if (!emit) {
-                atomicAdd(tcount + tgt, 1u);
-            } else {
-                unsigned long long p = atomicAdd(npush, 1ull);
+        const unsigned mt = __ballot_sync(KCNA_FULL, take);
+        if (!emit) {
+            if (take) atomicAdd(tcount + kcna_key_id(k), 1u);
+        } else if (mt) { // one reservation per warp and batch: the push list's counter is a single word
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(npush, (unsigned long long)__popc(mt));
+            base = __shfl_sync(KCNA_FULL, base, 0);
+            if (take) {
+                const unsigned long long p = base + __popc(mt & kcna_lanemask_lt());
                 if (p < push_cap)
-                    pushes[p] = ((uint64_t)tgt << 32) | i | ((k & KCNA_FLAG_ISNEW) ? 0x80000000ull : 0ull);
+                    pushes[p] = ((uint64_t)kcna_key_id(k) << 32) | i | ((k & KCNA_FLAG_ISNEW) ? 0x80000000ull : 0ull);
                 pr[j] = k & ~KCNA_FLAG_NEW;
             }
         }
-        taken += __popc(__ballot_sync(KCNA_FULL, take));
+        taken += __popc(mt);
     }
 }
 
