@@ -966,9 +966,10 @@ __global__ void bridge_update_kernel(uint64_t *__restrict__ pool, const uint32_t
     }
 }
 
+// groups the pushes by target; pnew (may be null) marks targets with a new pusher
 __global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint64_t np,
                                       const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
-                                      uint32_t *__restrict__ rnn, uint32_t N) {
+                                      uint32_t *__restrict__ rnn, uint32_t N, uint8_t *__restrict__ pnew) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= np) return;
     uint64_t v = pushes[t];
@@ -976,6 +977,20 @@ __global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint6
     if (tgt >= N) return;
     uint32_t p = atomicAdd(cursor + tgt, 1u);
     if (off[tgt] + p < off[tgt + 1]) rnn[off[tgt] + p] = (uint32_t)v;
+    if (pnew && (v & 0x80000000ull)) pnew[tgt] = 1;
+}
+
+// per node: graph neighbours whose edge is flagged new (UpdateNhoods); warp per node
+__global__ void count_new_edges_kernel(const uint8_t *__restrict__ g_isnew, const uint32_t *__restrict__ g_deg,
+                                       uint32_t N, uint32_t W, uint16_t *__restrict__ nnew) {
+    const uint32_t q = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = kcna_lane();
+    if (q >= N) return;
+    const uint32_t deg = min(g_deg[q], W);
+    uint32_t n = 0;
+    for (uint32_t j0 = 0; j0 < deg; j0 += 32)
+        n += __popc(__ballot_sync(KCNA_FULL, j0 + lane < deg && g_isnew[(uint64_t)q * W + j0 + lane]));
+    if (lane == 0) nnew[q] = (uint16_t)n;
 }
 
 // P2K join, tiled: one block per node q.  Rows = pushers u of q (rnn(q), up to
@@ -1096,6 +1111,7 @@ __global__ void __launch_bounds__(PJT) p2k_join_kernel(R rows, int ld, uint32_t 
     __shared__ uint32_t s_u[RMAX], s_w[PJC];
     __shared__ uint8_t s_unew[RMAX], s_wnew[PJC];
     __shared__ unsigned long long s_cc;
+    __shared__ int s_n;
     const uint32_t q = blockIdx.x;
     const uint64_t r0 = off[q], r1 = off[q + 1];
     const int deg = (int)min(g_deg[q], W);
@@ -1105,20 +1121,32 @@ __global__ void __launch_bounds__(PJT) p2k_join_kernel(R rows, int ld, uint32_t 
     for (int c0 = 0; c0 < deg; c0 += PJC) { // graph rows wider than 64: column chunks
         const int nw = min(PJC, deg - c0);
         __syncthreads();
+        int wn = 0;
         for (int j = threadIdx.x; j < nw; j += PJT) {
             s_w[j] = g_ids[(uint64_t)q * W + c0 + j];
             s_wnew[j] = g_isnew[(uint64_t)q * W + c0 + j];
+            wn |= s_wnew[j];
         }
+        // a pair of an old pusher and an old neighbour is skipped
+        // (src/kgraph.cpp:2639-2641): without a new neighbour in this chunk only
+        // the new pushers enter the tile, and a tile without pushers is skipped
+        const bool any_wnew = __syncthreads_or(wn) != 0;
         for (uint64_t t0 = r0; t0 < r1; t0 += RMAX) {
-            const int nu = (int)min((uint64_t)RMAX, r1 - t0);
+            const int nraw = (int)min((uint64_t)RMAX, r1 - t0);
             __syncthreads();
-            for (int i = threadIdx.x; i < nu; i += PJT) {
-                uint32_t v = rnn[t0 + i];
-                uint32_t u = v & 0x7FFFFFFFu;
-                s_u[i] = u < N ? u : 0;
-                s_unew[i] = (v & 0x80000000u) ? 1 : 0;
+            if (threadIdx.x == 0) s_n = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < nraw; i += PJT) {
+                const uint32_t v = rnn[t0 + i];
+                if (!any_wnew && !(v & 0x80000000u)) continue;
+                const uint32_t u = v & 0x7FFFFFFFu;
+                const int k = atomicAdd(&s_n, 1);
+                s_u[k] = u < N ? u : 0;
+                s_unew[k] = (v & 0x80000000u) ? 1 : 0;
             }
             __syncthreads();
+            const int nu = s_n;
+            if (nu == 0) continue;
             if (RMAX == 32 || nu <= 32)
                 p2k_tile<1>(rows, ld, N, s_u, s_unew, nu, s_w, s_wnew, nw, radius, cand, cand_cnt, CB, s_As, s_Bs, s_D,
                             &s_cc);
@@ -1548,6 +1576,8 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     KCNA_TRY(kcna_pools_set_radius(c, maxl));
     uint32_t *tcount = nullptr, *cursor = nullptr, *rnn = nullptr;
     uint64_t *off = nullptr, *pushes = nullptr;
+    uint16_t *nnew = nullptr; // Gram-tile join: new graph neighbours per node (fixed in this call)
+    uint8_t *pnew = nullptr;  // and whether a node has a new pusher (per round)
     kcna_status s = KCNA_OK;
     auto cleanup = [&]() {
         kcna_release(c, tcount);
@@ -1555,12 +1585,21 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         kcna_release(c, rnn);
         kcna_release(c, off);
         kcna_release(c, pushes);
+        kcna_release(c, nnew);
+        kcna_release(c, pnew);
     };
     if ((s = kcna_alloc(c, &tcount, N, "push counts")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &cursor, N, "cursor")) != KCNA_OK) return cleanup(), s;
     if ((s = kcna_alloc(c, &off, (uint64_t)N + 1, "offsets")) != KCNA_OK) return cleanup(), s;
     uint64_t total_comps = 0;
     const unsigned wblocks = kcna_div_up((uint64_t)N * 32, 256);
+    const bool tc = c->gram_exact && c->W <= 256;
+    if (tc) {
+        if ((s = kcna_alloc(c, &nnew, N, "new edges")) != KCNA_OK) return cleanup(), s;
+        if ((s = kcna_alloc(c, &pnew, N, "new pushers")) != KCNA_OK) return cleanup(), s;
+        count_new_edges_kernel<<<wblocks, 256, 0, c->stream>>>(c->g_isnew, c->g_deg, N, c->W, nnew);
+        KCNA_LAUNCHED(c);
+    }
     if ((s = kcna_cuda_check(c, cudaFuncSetAttribute(p2k_join_kernel<128, RowsF32>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)p2k_smem_bytes<128>()),
@@ -1614,12 +1653,13 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         }
         // group pushes by target (offsets already hold the right counts per target)
         cudaMemsetAsync(cursor, 0, (size_t)N * 4, c->stream);
+        if (tc) cudaMemsetAsync(pnew, 0, N, c->stream);
         bridge_scatter_kernel<<<kcna_div_up(std::max<uint64_t>(np_all, 1), 256), 256, 0, c->stream>>>(
-            pushes, np_all, off, cursor, rnn, N);
+            pushes, np_all, off, cursor, rnn, N, pnew);
         KCNA_LAUNCHED(c);
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
-        if (c->gram_exact && c->W <= 256) {
-            if ((s = kcna_p2k_tc_launch(c, off, rnn, c->counters + 21)) != KCNA_OK) return cleanup(), s;
+        if (tc) {
+            if ((s = kcna_p2k_tc_launch(c, off, rnn, nnew, pnew, c->counters + 21)) != KCNA_OK) return cleanup(), s;
         } else if (c->bf16_exact) {
             const RowsB16 rows{c->Xh, (int)c->ld};
             p2k_join_kernel<32><<<N, PJT, p2k_smem_bytes<32>(), c->stream>>>(
@@ -1637,7 +1677,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
                 rows, (int)c->ld, N, off, rnn, c->g_ids, c->g_deg, c->g_isnew, c->W, c->radius, c->cand, c->cand_cnt,
                 c->CB, c->counters + 21);
         }
-        if (!(c->gram_exact && c->W <= 256)) c->launches += 2; // the FP32 pair
+        if (!tc) c->launches += 2; // the FP32 pair
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, c->counters + 21, 8, cudaMemcpyDeviceToHost, c->stream);
         if ((s = kcna_phase_end(c, KCNA_PHASE_P2K)) != KCNA_OK) return cleanup(), s;

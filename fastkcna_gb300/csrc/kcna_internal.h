@@ -208,7 +208,9 @@ kcna_status kcna_prune_fp8_launch(kcna_ctx *c, const uint64_t *keys, uint64_t st
                                   int maxc, uint32_t *resume, uint32_t *resume_cnt, unsigned long long *comps,
                                   unsigned long long *exact);
 // P2K join on tcgen05 Gram tiles (kcna_p2k_tc.cu); requires c->gram_exact.
-kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, unsigned long long *comps);
+// nnew[q]: q's graph neighbours flagged new; pnew[q]: 1 when a pusher of q this round is new.
+kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, const uint16_t *nnew,
+                               const uint8_t *pnew, unsigned long long *comps);
 kcna_status kcna_nnd_sample(kcna_ctx *c, const kcna_params *p, int iter);
 kcna_status kcna_controls_setup(kcna_ctx *c, const kcna_params *p, uint32_t maxl);
 kcna_status kcna_control_recall(kcna_ctx *c, uint32_t K, float *recall);

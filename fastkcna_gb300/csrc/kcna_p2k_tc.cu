@@ -58,6 +58,7 @@ struct StageMeta {
     uint32_t row_id[PM];   // pusher id | isnew << 31
     uint32_t row_span[PM]; // column range of the row's node: begin | end << 16
     float row_rad[PM], row_nrm[PM];
+    uint16_t row_nn[PM];   // new neighbours of the row's node: an old pusher's row spans only them
     uint32_t col_id[PN];
     uint32_t col_gidx[PN]; // q * W + j: where the column's isnew flag lives
     float col_nrm[PN];
@@ -83,6 +84,8 @@ struct P2kArgs {
     uint64_t *cand;
     uint32_t *cand_cnt;
     uint32_t CB;
+    const uint16_t *nnew; // per node: graph neighbours flagged new
+    const uint8_t *pnew;  // per node: 1 when one of its pushers this round is new
     unsigned long long *comps;
     int *err;
 };
@@ -167,35 +170,67 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
         for (uint32_t qb = q0; ok && qb < q1; qb += 32) {
             const uint32_t ql = qb + lane;
             uint64_t o0 = 0, o1 = 0;
-            uint32_t dl = 0;
+            uint32_t dl = 0, nl = 0, al = 0;
             if (ql < q1) {
                 o0 = a.off[ql];
                 o1 = a.off[ql + 1];
                 dl = min(a.g_deg[ql], a.W);
+                nl = a.nnew[ql];
+                al = a.pnew[ql];
             }
             for (int jq = 0; jq < 32 && qb + jq < q1; ++jq) {
                 const uint32_t q = qb + jq;
                 const uint64_t ob = __shfl_sync(KCNA_FULL, o0, jq), oe = __shfl_sync(KCNA_FULL, o1, jq);
                 const uint32_t deg = __shfl_sync(KCNA_FULL, dl, jq);
+                const uint32_t nn = min(__shfl_sync(KCNA_FULL, nl, jq), deg);
+                const bool an = __shfl_sync(KCNA_FULL, al, jq) != 0u;
                 const uint32_t nu = (uint32_t)(oe - ob);
                 if (nu == 0 || deg == 0) continue;
+                // a pair of an old pusher and an old neighbour is skipped
+                // (src/kgraph.cpp:2639-2641): a node whose pushers and neighbours
+                // are all old has nothing to join; otherwise its new neighbours
+                // come first among its columns, an old pusher's row spans only
+                // them, and without new pushers only they are packed
+                if (!an && nn == 0) continue;
+                const uint32_t cl = an ? deg : nn; // columns the node needs
+                const bool reorder = nn > 0 && nn < deg;
                 for (uint32_t done = 0; done < nu;) {
-                    if (rows == PM || cols + deg > PN) {
+                    if (rows == PM || cols + cl > PN) {
                         close_tile();
                         if (!(ok = open_tile())) break;
                     }
                     const uint32_t take = min(nu - done, PM - rows);
-                    const uint32_t span = cols | ((cols + deg) << 16);
+                    const uint32_t span = cols | ((cols + cl) << 16);
                     for (uint32_t i = lane; i < take; i += 32) {
                         cp_async4(smem_u32(&M->row_id[rows + i]), a.rnn + ob + done + i);
                         M->row_span[rows + i] = span;
+                        M->row_nn[rows + i] = (uint16_t)nn;
                     }
-                    for (uint32_t j = lane; j < deg; j += 32) {
-                        cp_async4(smem_u32(&M->col_id[cols + j]), a.g_ids + (uint64_t)q * a.W + j);
-                        M->col_gidx[cols + j] = q * a.W + j;
+                    if (!reorder) { // all new, all old (new pushers only), or no reordering to do
+                        for (uint32_t j = lane; j < deg; j += 32) {
+                            cp_async4(smem_u32(&M->col_id[cols + j]), a.g_ids + (uint64_t)q * a.W + j);
+                            M->col_gidx[cols + j] = q * a.W + j;
+                        }
+                    } else {
+                        const uint8_t *fq = a.g_isnew + (uint64_t)q * a.W;
+                        uint32_t an_ = 0, ao = 0;
+                        for (uint32_t j0 = 0; j0 < deg; j0 += 32) {
+                            const uint32_t j = j0 + lane;
+                            const bool f = j < deg && fq[j];
+                            const unsigned mn = __ballot_sync(KCNA_FULL, f);
+                            const unsigned mo = __ballot_sync(KCNA_FULL, j < deg && !f);
+                            if (j < deg && (f || an)) {
+                                const uint32_t c = cols + (f ? an_ + __popc(mn & kcna_lanemask_lt())
+                                                             : nn + ao + __popc(mo & kcna_lanemask_lt()));
+                                cp_async4(smem_u32(&M->col_id[c]), a.g_ids + (uint64_t)q * a.W + j);
+                                M->col_gidx[c] = q * a.W + j;
+                            }
+                            an_ += __popc(mn);
+                            ao += __popc(mo);
+                        }
                     }
                     rows += take;
-                    cols += deg;
+                    cols += cl;
                     done += take;
                 }
             }
@@ -287,10 +322,13 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
             const uint32_t u = uw & 0x7FFFFFFFu;
             const bool unew = (uw >> 31) != 0u;
             const uint32_t span = rowv ? M.row_span[rr] : 0u;
-            const int cs = (int)(span & 0xFFFFu), ce = (int)(span >> 16);
+            const int cs = (int)(span & 0xFFFFu);
+            // an old pusher meets only its node's new neighbours (the first ones)
+            const int ce = unew ? (int)(span >> 16) : min((int)(span >> 16), cs + (rowv ? (int)M.row_nn[rr] : 0));
             const float rad = rowv ? M.row_rad[rr] : -1.f, nu2 = rowv ? M.row_nrm[rr] : 0.f;
             // 16-column groups this warp's rows touch
-            int gl = rowv ? cs >> 4 : 1 << 20, gh = rowv ? (ce - 1) >> 4 : -1;
+            const bool rowe = rowv && ce > cs;
+            int gl = rowe ? cs >> 4 : 1 << 20, gh = rowe ? (ce - 1) >> 4 : -1;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 gl = min(gl, __shfl_xor_sync(KCNA_FULL, gl, o));
@@ -361,7 +399,8 @@ __global__ void __launch_bounds__(PW_THREADS, 1) p2k_tc_kernel(P2kArgs a) {
 
 } // namespace
 
-kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, unsigned long long *comps) {
+kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t *rnn, const uint16_t *nnew,
+                               const uint8_t *pnew, unsigned long long *comps) {
     if (!c->gram_exact || !c->Xh || !c->norms || (c->ld & 7u) || c->ld > 128 || c->W > (uint32_t)PN)
         return kcna_fail(c, KCNA_E_STATE, "Gram-tile P2K needs exact BF16 rows with d <= 128 and width <= 256");
     P2kArgs a;
@@ -379,6 +418,8 @@ kcna_status kcna_p2k_tc_launch(kcna_ctx *c, const uint64_t *off, const uint32_t 
     a.cand = c->cand;
     a.cand_cnt = c->cand_cnt;
     a.CB = c->CB;
+    a.nnew = nnew;
+    a.pnew = pnew;
     a.comps = comps;
     a.err = c->d_err;
     const size_t sm = 1024 + (size_t)TS * STAGE + sizeof(PwShared);
