@@ -1295,12 +1295,15 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
     if ((s = kcna_alloc(c, &blist, N + 1, "link big list")) != KCNA_OK) return cleanup(), s;
     bcnt = blist + N;
     cudaMemsetAsync(bcnt, 0, 4, c->stream);
-    // FP8 screen (float rows, high d): the warp kernel stages its sorted lists
-    // for the reversed prune, which the tile prune then takes
-    const bool fp8 = kcna_prune_fp8_ok(c, kind, (int)p->nsg_R, 1);
+    // FP8 screen (float rows, high d) or Gram-exact rows: the warp kernel
+    // stages its sorted lists for the reversed prune, which a tile prune then
+    // takes (lists of at most LW_CAP entries; larger ones stay on the block kernel)
+    const bool gram = kcna_prune_tc_ok(c, kind, (int)p->nsg_R, LW_CAP, p->angle);
+    const bool fp8 = !gram && kcna_prune_fp8_ok(c, kind, (int)p->nsg_R, 1);
+    const bool staged = gram || fp8;
     uint64_t *stage = nullptr;
     uint32_t *stage_meta = nullptr; // nodes, counts, resume list (N each), staged count, resume count
-    if (fp8) {
+    if (staged) {
         if ((s = kcna_alloc(c, &stage, N * LW_CAP + 2, "link stage")) != KCNA_OK) return cleanup(), s;
         if ((s = kcna_alloc(c, &stage_meta, 3 * N + 2, "link stage lists")) != KCNA_OK) {
             kcna_release(c, stage);
@@ -1308,8 +1311,8 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
         }
         cudaMemsetAsync(stage_meta + 3 * N, 0, 8, c->stream);
     }
-    uint32_t *st_nodes = fp8 ? stage_meta : nullptr, *st_cnt = fp8 ? stage_meta + N : nullptr;
-    uint32_t *st_resume = fp8 ? stage_meta + 2 * N : nullptr, *st_n = fp8 ? stage_meta + 3 * N : nullptr;
+    uint32_t *st_nodes = staged ? stage_meta : nullptr, *st_cnt = staged ? stage_meta + N : nullptr;
+    uint32_t *st_resume = staged ? stage_meta + 2 * N : nullptr, *st_n = staged ? stage_meta + 3 * N : nullptr;
     auto launch_link = [&](auto rows) -> kcna_status {
         int per_sm = 0;
         KCNA_TRY(kcna_cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, link_warp_kernel<decltype(rows)>,
@@ -1323,13 +1326,17 @@ kcna_status kcna_link_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t 
         KCNA_LAUNCHED(c);
         uint32_t hb[2] = {0u, 0u};
         KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb[0], bcnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
-        if (fp8) KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb[1], st_n, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        if (staged)
+            KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&hb[1], st_n, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
         KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "link sync"));
         if (hb[0] > 0) {
             link_merge_kernel<<<hb[0], LT, 0, c->stream>>>(rows, (uint32_t)N, rule, (int)p->nsg_R, c->g_ids, c->g_dist,
                                                            c->g_deg, W, off, rev, c->counters + 17, c->d_err, blist);
             KCNA_LAUNCHED(c);
         }
+        if (gram && hb[1] > 0) // reversed prunes of the staged lists on Gram-exact tiles (no search_K cap)
+            KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, p->angle, (int)p->nsg_R, LW_CAP, c->counters + 17, stage,
+                                          LW_CAP, st_cnt, st_nodes, hb[1]));
         if (fp8 && hb[1] > 0) { // reversed prunes of the staged lists: FP8 tiles, FP32 where undecided or unfinished
             KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 49, 0, 8, c->stream), "memset"));
             KCNA_TRY(kcna_prune_fp8_launch(c, stage, LW_CAP, st_cnt, st_nodes, hb[1], 0xFFFFFFFFu, rule.t3,

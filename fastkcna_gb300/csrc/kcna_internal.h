@@ -193,8 +193,12 @@ inline float kcna_alpha_threshold(float angle) {
 // Occlusion prune on tcgen05 Gram tiles (kcna_prune_tc.cu); requires c->gram_exact.
 // alpha-PG takes it for angles up to 60 degrees only (angle: degrees).
 bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float angle);
+// Node mode (nodes null): each node's pool.  List mode: n_items staged
+// candidate lists (pool-format keys, `stride` apart, cnt[k] each) of nodes[k].
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
-                                 unsigned long long *comps);
+                                 unsigned long long *comps, const uint64_t *keys = nullptr, uint64_t stride = 0,
+                                 const uint32_t *cnt = nullptr, const uint32_t *nodes = nullptr,
+                                 uint32_t n_items = 0);
 // tau-MNG prune of float rows on FP8 E4M3 Gram tiles (kcna_prune_fp8.cu);
 // requires c->fp8_screen.  The first 128 candidates of every item are pruned
 // on the tiles; items whose scan ran out of them with fewer than range kept

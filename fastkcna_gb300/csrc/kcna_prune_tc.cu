@@ -95,10 +95,12 @@ struct PgShared {
 };
 
 struct PgArgs {
-    uint32_t N, cap, W, ld;
-    const uint64_t *pool;
-    const uint16_t *rows; // BF16 rows, ld elements apart
-    const uint32_t *pool_cnt;
+    uint32_t N, cap, W, ld; // N: ids at or beyond are skipped (the layer prefix); cap: candidate row stride
+    uint32_t n_items;       // nodes (or staged lists) to prune
+    const uint32_t *nodes;  // staged lists: node of list k (null: item k is node k)
+    const uint64_t *pool;   // candidate keys, row = node (or list), cap apart
+    const uint16_t *rows;   // BF16 rows, ld elements apart
+    const uint32_t *pool_cnt; // candidates of each row
     const float *norms;
     float aux, thr; // aux: 3 tau (tau-MNG) or the angle screen's margin 4m (alpha-PG)
     int range, maxc;
@@ -229,8 +231,8 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         uint32_t r_cnt0 = 0u, r_cnt1 = 0u, r_shift0 = 0u, r_shift1 = 0u;
         int pending = -1; // node whose key copy is requested and not yet waited for
         auto request = [&](int kk) {
-            const uint32_t q = blockIdx.x + (uint32_t)kk * gridDim.x;
-            if (q >= a.N) return;
+            const uint32_t q = blockIdx.x + (uint32_t)kk * gridDim.x; // item: node, or staged list
+            if (q >= a.n_items) return;
             const int b = kk & 1;
             pending = kk;
             const uint32_t cnt = min(a.pool_cnt[q], a.cap);
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         };
         request(0);
         int k = 0;
-        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+        for (uint32_t q = blockIdx.x; q < a.n_items; q += gridDim.x, ++k) {
             const int sl = k & 1;
             if (!mbar_wait(&S.keys_full[sl], (k >> 1) & 1)) { ok = false; break; }
             pending = -1;
@@ -265,8 +267,9 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             NodeMeta &M = S.meta[sl];
             const int cnt = (int)(sl ? r_cnt1 : r_cnt0);
             const uint32_t shift = sl ? r_shift1 : r_shift0;
+            const uint32_t node = a.nodes ? a.nodes[q] : q;
             int first = 0;
-            if (cnt > 0 && kcna_key_id(M.key[shift]) == q) first = 1;
+            if (cnt > 0 && kcna_key_id(M.key[shift]) == node) first = 1;
             const int nc = first < cnt ? max(min(cnt, a.maxc), first + 1) - first : 0;
             const int nch = (nc + PC - 1) / PC;
             const uint32_t koff = shift + (uint32_t)first;
@@ -294,7 +297,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
                 if (lane == 0) M.dead[i] = dm;
             }
             if (lane == 0) {
-                M.q = q;
+                M.q = node;
                 M.nc = (uint32_t)nc;
                 M.nch = (uint32_t)nch;
                 M.koff = koff;
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             mbar_arrive(&S.meta_full[sl]);          // this lane's stores
             // the next node's keys into the other buffer, once its node k-1 is done
             const uint32_t qn = q + gridDim.x;
-            if (qn < a.N) {
+            if (qn < a.n_items) {
                 if (k >= 1 && !mbar_wait(&S.node_empty[sl ^ 1], ((k - 1) >> 1) & 1)) { ok = false; break; }
                 request(k + 1);
             }
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         uint32_t gc = 0;
         int pend = -1; // slot whose copies are in flight, not yet announced
         int k = 0;
-        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+        for (uint32_t q = blockIdx.x; q < a.n_items; q += gridDim.x, ++k) {
             const int sl = k & 1;
             if (!mbar_wait(&S.ids_ready[sl], (k >> 1) & 1) || S.abort_flag) { ok = false; break; }
             const NodeMeta &M = S.meta[sl];
@@ -371,7 +374,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             uint32_t gc = 0, acount = 0;
             int k = 0;
             const uint32_t idesc = idesc_bf16(PC, PC);
-            for (uint32_t q = blockIdx.x; q < a.N && ok; q += gridDim.x, ++k) {
+            for (uint32_t q = blockIdx.x; q < a.n_items && ok; q += gridDim.x, ++k) {
                 const int sl = k & 1;
                 if (!mbar_wait(&S.ids_ready[sl], (k >> 1) & 1) || S.abort_flag) { ok = false; break; }
                 const int nch = (int)S.meta[sl].nch;
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         const int qt = warp & 3, h = (warp - 2) >> 2; // TMEM lane quarter, column group
         uint32_t acount = 0;
         int k = 0;
-        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+        for (uint32_t q = blockIdx.x; q < a.n_items; q += gridDim.x, ++k) {
             const int sl = k & 1;
             bool mine = mbar_wait(&S.meta_full[sl], (k >> 1) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
@@ -525,7 +528,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
         // ----------------------------------------------------------------- scan
         unsigned long long cc = 0;
         int k = 0;
-        for (uint32_t q = blockIdx.x; q < a.N; q += gridDim.x, ++k) {
+        for (uint32_t q = blockIdx.x; q < a.n_items; q += gridDim.x, ++k) {
             const int sl = k & 1;
             const bool mine = mbar_wait(&S.mask_full[sl], (k >> 1) & 1) && !S.abort_flag;
             if (!__all_sync(KCNA_FULL, mine)) { ok = false; break; }
@@ -602,17 +605,20 @@ bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float an
 }
 
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
-                                 unsigned long long *comps) {
+                                 unsigned long long *comps, const uint64_t *keys, uint64_t stride, const uint32_t *cnt,
+                                 const uint32_t *nodes, uint32_t n_items) {
     if (!kcna_prune_tc_ok(c, kind, range, maxc, angle))
         return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
     PgArgs a;
-    a.N = c->n;
-    a.cap = c->cap;
+    a.N = nodes ? 0xFFFFFFFFu : c->n; // staged lists carry no layer prefix
+    a.cap = nodes ? (uint32_t)stride : c->cap;
+    a.n_items = nodes ? n_items : c->n;
+    a.nodes = nodes;
     a.W = c->W;
     a.ld = c->ld;
-    a.pool = c->pool;
+    a.pool = nodes ? keys : c->pool;
     a.rows = c->Xh;
-    a.pool_cnt = c->pool_cnt;
+    a.pool_cnt = nodes ? cnt : c->pool_cnt;
     a.norms = c->norms;
     a.thr = kcna_alpha_threshold(angle);
     // tau-MNG: 3 tau; alpha-PG: 4m, m = 1/2 - thr + 1e-5 (the angle screen's margin)
@@ -624,7 +630,7 @@ kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, i
     a.g_deg = c->g_deg;
     a.comps = comps;
     a.err = c->d_err;
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(c->n, (uint64_t)std::max(c->num_sms, 1));
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(a.n_items, (uint64_t)std::max(c->num_sms, 1));
     if (grid == 0) return KCNA_OK;
     if (kind == KCNA_TAUMNG) return launch_rule<1>(c, a, grid);
     if (kind == KCNA_ALPHAPG) return launch_rule<2>(c, a, grid);
