@@ -408,6 +408,8 @@ kcna_status kcna_create(kcna_ctx **out, int device) {
 void kcna_destroy(kcna_ctx *c) {
     if (!c) return;
     if (c->writer.joinable()) c->writer.join();
+    if (c->seed_sub) kcna_destroy(c->seed_sub);
+    c->seed_sub = nullptr;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_state(c);

@@ -110,6 +110,10 @@ struct kcna_ctx {
     kcna_stats *stats = nullptr;
     double t0 = 0;
 
+    // the learned seed's subsample NN-descent runs in this context, kept
+    // across builds so that its buffers stay in its memory cache
+    kcna_ctx *seed_sub = nullptr;
+
     // phase timing with CUDA events on `stream`
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double phase_ms[KCNA_NUM_PHASES] = {};

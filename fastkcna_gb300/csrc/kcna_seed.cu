@@ -541,12 +541,11 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(d_sub, sub.data(), (size_t)ns * 4, cudaMemcpyHostToDevice, s), "h2d"));
     KCNA_TRY(kcna_gather_rows(c, d_sub, ns, Xs));
     KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(s), "subsample sync"));
-    kcna_ctx *sc = nullptr;
-    if (kcna_create(&sc, c->device) != KCNA_OK) return kcna_fail(c, KCNA_E_CUDA, "seed: no sub-context");
-    struct Closer {
-        kcna_ctx *p;
-        ~Closer() { kcna_destroy(p); }
-    } closer{sc};
+    if (!c->seed_sub && kcna_create(&c->seed_sub, c->device) != KCNA_OK) {
+        c->seed_sub = nullptr;
+        return kcna_fail(c, KCNA_E_CUDA, "seed: no sub-context");
+    }
+    kcna_ctx *sc = c->seed_sub;
     if (kcna_upload_device(sc, Xs, ns, ld, (uint64_t)ld * 4) != KCNA_OK)
         return kcna_fail(c, KCNA_E_CUDA, std::string("seed: ") + kcna_last_error(sc));
     kcna_params sp;
@@ -560,10 +559,12 @@ kcna_status kcna_seed_learned(kcna_ctx *c, const kcna_params *p, kcna_stats *st)
     sp.recall = 2.f; // run the iterations
     sp.delta = 0.f;
     sp.seed = p->seed + 17;
+    sp.screen = p->screen; // Gram-exact tiles give the FP32 join's pools bit for bit
     kcna_stats sst;
+    const uint64_t sub_launches0 = sc->launches;
     if (kcna_nndescent(sc, &sp, &sst) != KCNA_OK)
         return kcna_fail(c, KCNA_E_CUDA, std::string("seed subsample: ") + kcna_last_error(sc));
-    c->launches += sc->launches;
+    c->launches += sc->launches - sub_launches0;
     // --- 2. encoder training
     const int B = 2048, steps = 64, kp = 10;
     const float margin = 0.3f, lr = 2e-3f;
