@@ -930,11 +930,15 @@ __global__ void bridge_init_kernel(uint64_t *__restrict__ pool, const uint32_t *
     }
 }
 
-// count (pass 0) or emit (pass 1) the pushes of one update round
+// count (pass 0) or emit (pass 1) the pushes of one update round.  Emitting
+// writes each push straight into its target's bucket of rnn (offsets from the
+// count pass; the pusher's id with its isnew flag in bit 31) and, with pnew,
+// marks targets that receive a new pusher.
 __global__ void bridge_update_kernel(uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt, uint32_t cap,
                                      uint32_t N, uint32_t Lp, uint32_t S_, int capped, int emit,
-                                     uint32_t *__restrict__ tcount, uint64_t *__restrict__ pushes,
-                                     unsigned long long *__restrict__ npush, uint64_t push_cap) {
+                                     uint32_t *__restrict__ tcount, const uint64_t *__restrict__ off,
+                                     uint32_t *__restrict__ cursor, uint32_t *__restrict__ rnn,
+                                     uint8_t *__restrict__ pnew) {
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = kcna_lane();
     if (i >= N) return;
@@ -948,36 +952,20 @@ __global__ void bridge_update_kernel(uint64_t *__restrict__ pool, const uint32_t
         unsigned mk = __ballot_sync(KCNA_FULL, f);
         uint32_t rank = taken + __popc(mk & kcna_lanemask_lt());
         bool take = f && (!capped || rank < S_);
-        const unsigned mt = __ballot_sync(KCNA_FULL, take);
-        if (!emit) {
-            if (take) atomicAdd(tcount + kcna_key_id(k), 1u);
-        } else if (mt) { // one reservation per warp and batch: the push list's counter is a single word
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(npush, (unsigned long long)__popc(mt));
-            base = __shfl_sync(KCNA_FULL, base, 0);
-            if (take) {
-                const unsigned long long p = base + __popc(mt & kcna_lanemask_lt());
-                if (p < push_cap)
-                    pushes[p] = ((uint64_t)kcna_key_id(k) << 32) | i | ((k & KCNA_FLAG_ISNEW) ? 0x80000000ull : 0ull);
+        const uint32_t tgt = kcna_key_id(k);
+        if (take && tgt < N) {
+            if (!emit) {
+                atomicAdd(tcount + tgt, 1u);
+            } else {
+                const bool isnew = (k & KCNA_FLAG_ISNEW) != 0;
+                const uint32_t pos = atomicAdd(cursor + tgt, 1u);
+                if (off[tgt] + pos < off[tgt + 1]) rnn[off[tgt] + pos] = i | (isnew ? 0x80000000u : 0u);
+                if (pnew && isnew) pnew[tgt] = 1;
                 pr[j] = k & ~KCNA_FLAG_NEW;
             }
         }
-        taken += __popc(mt);
+        taken += __popc(__ballot_sync(KCNA_FULL, take));
     }
-}
-
-// groups the pushes by target; pnew (may be null) marks targets with a new pusher
-__global__ void bridge_scatter_kernel(const uint64_t *__restrict__ pushes, uint64_t np,
-                                      const uint64_t *__restrict__ off, uint32_t *__restrict__ cursor,
-                                      uint32_t *__restrict__ rnn, uint32_t N, uint8_t *__restrict__ pnew) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= np) return;
-    uint64_t v = pushes[t];
-    uint32_t tgt = (uint32_t)(v >> 32);
-    if (tgt >= N) return;
-    uint32_t p = atomicAdd(cursor + tgt, 1u);
-    if (off[tgt] + p < off[tgt + 1]) rnn[off[tgt] + p] = (uint32_t)v;
-    if (pnew && (v & 0x80000000ull)) pnew[tgt] = 1;
 }
 
 // per node: graph neighbours whose edge is flagged new (UpdateNhoods); warp per node
@@ -1582,7 +1570,8 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
     KCNA_LAUNCHED(c);
     KCNA_TRY(kcna_pools_set_radius(c, maxl));
     uint32_t *tcount = nullptr, *cursor = nullptr, *rnn = nullptr;
-    uint64_t *off = nullptr, *pushes = nullptr;
+    uint64_t *off = nullptr;
+    uint64_t rnn_cap = 0;
     uint16_t *nnew = nullptr; // Gram-tile join: new graph neighbours per node (fixed in this call)
     uint8_t *pnew = nullptr;  // and whether a node has a new pusher (per round)
     kcna_status s = KCNA_OK;
@@ -1591,7 +1580,6 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         kcna_release(c, cursor);
         kcna_release(c, rnn);
         kcna_release(c, off);
-        kcna_release(c, pushes);
         kcna_release(c, nnew);
         kcna_release(c, pnew);
     };
@@ -1623,7 +1611,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
         if ((s = kcna_phase_begin(c)) != KCNA_OK) return cleanup(), s;
         cudaMemsetAsync(tcount, 0, (size_t)N * 4, c->stream);
         bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 1, 0, tcount,
-                                                             nullptr, nullptr, 0);
+                                                             nullptr, nullptr, nullptr, nullptr);
         KCNA_LAUNCHED(c);
         uint64_t np = 0;
         if ((s = exclusive_scan(c, tcount, N, off, &np)) != KCNA_OK) return cleanup(), s;
@@ -1635,7 +1623,7 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             cudaMemsetAsync(tc2, 0, (size_t)N * 4, c->stream);
             // remainder = all flagged in the prefix minus the capped ones: count uncapped, subtract
             bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 0, 0, tc2,
-                                                                 nullptr, nullptr, 0);
+                                                                 nullptr, nullptr, nullptr, nullptr);
             KCNA_LAUNCHED(c);
             uint64_t np2 = 0;
             s = exclusive_scan(c, tc2, N, off, &np2);
@@ -1643,27 +1631,23 @@ kcna_status kcna_bridge_view(kcna_ctx *c, const kcna_params *p, uint32_t maxl, i
             if (s != KCNA_OK) return cleanup(), s;
             np_all = np2; // uncapped count covers the capped pushes too
         }
-        kcna_release(c, pushes);
-        pushes = nullptr;
-        kcna_release(c, rnn);
-        rnn = nullptr;
-        if ((s = kcna_alloc(c, &pushes, std::max<uint64_t>(np_all, 1), "pushes")) != KCNA_OK) return cleanup(), s;
-        if ((s = kcna_alloc(c, &rnn, std::max<uint64_t>(np_all, 1), "rnn")) != KCNA_OK) return cleanup(), s;
-        cudaMemsetAsync(c->counters + 20, 0, 8, c->stream);
+        // the pushes, grouped by target as they are taken (offsets hold the counts)
+        if (!rnn || np_all > rnn_cap) {
+            kcna_release(c, rnn);
+            rnn = nullptr;
+            rnn_cap = std::max<uint64_t>(np_all, (uint64_t)N * S_);
+            if ((s = kcna_alloc(c, &rnn, rnn_cap, "rnn")) != KCNA_OK) return cleanup(), s;
+        }
+        cudaMemsetAsync(cursor, 0, (size_t)N * 4, c->stream);
+        if (tc) cudaMemsetAsync(pnew, 0, N, c->stream);
         bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 1, 1, nullptr,
-                                                             pushes, c->counters + 20, np_all);
+                                                             off, cursor, rnn, pnew);
         KCNA_LAUNCHED(c);
         if (last) {
             bridge_update_kernel<<<wblocks, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, N, Lp, S_, 0, 1, nullptr,
-                                                                 pushes, c->counters + 20, np_all);
+                                                                 off, cursor, rnn, pnew);
             KCNA_LAUNCHED(c);
         }
-        // group pushes by target (offsets already hold the right counts per target)
-        cudaMemsetAsync(cursor, 0, (size_t)N * 4, c->stream);
-        if (tc) cudaMemsetAsync(pnew, 0, N, c->stream);
-        bridge_scatter_kernel<<<kcna_div_up(std::max<uint64_t>(np_all, 1), 256), 256, 0, c->stream>>>(
-            pushes, np_all, off, cursor, rnn, N, pnew);
-        KCNA_LAUNCHED(c);
         cudaMemsetAsync(c->counters + 21, 0, 8, c->stream);
         if (tc) {
             if ((s = kcna_p2k_tc_launch(c, off, rnn, nnew, pnew, c->counters + 21)) != KCNA_OK) return cleanup(), s;
