@@ -335,7 +335,8 @@ struct MergeArgs {
 // meets its barrier once at the end instead of waiting for its slowest node.
 // SURV is 512, or 1024 while the previous merge queued more than n/32 nodes
 // (the first iterations, when the pools are filling): twice the shared memory
-// per warp and fewer warps per SM, but fewer nodes left to the block merge.
+// per warp and fewer warps per SM, but fewer nodes left to the block merge;
+// refinement merges, with few survivors per node, take 128.
 // With CREDIT (NN-descent merges) every survivor also keeps the index of its
 // candidate slot (16 bits, CB <= 8192) and moves with its key through the
 // sort; before the survivors are deduplicated, each distinct survivor placed
@@ -1176,8 +1177,11 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     const char *wd = getenv("KCNA_MERGE_WIDE_DIV"); // tuning override of the threshold below
     const uint32_t wide_div = wd ? std::max(1, atoi(wd)) : 32; // 64 and 16 measured slower at C2 1M
     const bool wide = c->merge_big_last > c->n / wide_div; // many nodes overflowed the survivor buffer last time
-    const char *sv = getenv("KCNA_MERGE_SURV");   // tuning override: 512 or 1024
-    const int surv = sv ? (atoi(sv) >= 1024 ? 1024 : 512) : wide ? 1024 : 512;
+    const char *sv = getenv("KCNA_MERGE_SURV");   // tuning override: 128, 512 or 1024
+    // refinement merges (no credit) meet few survivors per node: 128 slots per
+    // warp, so that five blocks instead of three share an SM
+    const int surv = sv ? (atoi(sv) >= 1024 ? 1024 : atoi(sv) >= 512 ? 512 : 128)
+                        : wide ? 1024 : credit_found ? 512 : 128;
     const int nw = merge_warps(surv, credit_found);
     const size_t smw = merge_warp_bytes(c->cap, surv, credit_found) * nw;
     auto launch_warp = [&](auto kern) -> kcna_status {
@@ -1199,7 +1203,9 @@ kcna_status kcna_merge(kcna_ctx *c, uint32_t limit, uint32_t K, uint64_t *overfl
     if (credit_found)
         KCNA_TRY(surv == 1024 ? launch_warp(merge_warp_kernel<1024, true>) : launch_warp(merge_warp_kernel<512, true>));
     else
-        KCNA_TRY(surv == 1024 ? launch_warp(merge_warp_kernel<1024, false>) : launch_warp(merge_warp_kernel<512, false>));
+        KCNA_TRY(surv == 1024  ? launch_warp(merge_warp_kernel<1024, false>)
+                 : surv == 512 ? launch_warp(merge_warp_kernel<512, false>)
+                               : launch_warp(merge_warp_kernel<128, false>));
     merge_kernel<<<std::max(1, c->num_sms) * 4, MT, sm, c->stream>>>(a, c->big_list, c->big_cnt);
     c->launches += 2;
     KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "merge_kernel"));
