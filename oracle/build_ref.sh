@@ -13,8 +13,7 @@
 #
 # Where the sources are read from, in order:
 #   1. $KCNA_REF_SRC;
-#   2. <reference_path>/src, reference_path read from the benchmark spec at the
-#      repository root (the reference checkout, when this machine has one);
+#   2. /root/reference/src, the reference checkout, when this machine has one;
 #   3. oracle/_ref/src, a staging copy of the six source files the build uses.
 # When the sources come from 1 or 2, they are also staged into oracle/_ref/src
 # (git-ignored, never committed) so that a machine without the reference
@@ -25,13 +24,10 @@ HERE=$(cd "$(dirname "$0")" && pwd)
 STAGE="$HERE/_ref/src"
 FILES="kgraph.cpp kgraph.h kgraph-data.h metric.cpp neighbor.h fvec2lshit.cpp"
 SRC=${KCNA_REF_SRC:-}
-if [ -z "$SRC" ] && [ -f "$HERE/../BASELINE.json" ]; then
-    RP=$(sed -n 's/.*"reference_path"[[:space:]]*:[[:space:]]*"\([^"]*\)".*/\1/p' "$HERE/../BASELINE.json" | head -n 1)
-    if [ -n "$RP" ] && [ -f "$RP/src/kgraph.cpp" ]; then SRC="$RP/src"; fi
-fi
+if [ -z "$SRC" ] && [ -f /root/reference/src/kgraph.cpp ]; then SRC=/root/reference/src; fi
 if [ -z "$SRC" ] && [ -f "$STAGE/kgraph.cpp" ]; then SRC="$STAGE"; fi
 if [ -z "$SRC" ] || [ ! -f "$SRC/kgraph.cpp" ]; then
-    echo "build_ref.sh: reference sources not found (KCNA_REF_SRC, BASELINE.json reference_path, $STAGE)" >&2
+    echo "build_ref.sh: reference sources not found (KCNA_REF_SRC, /root/reference/src, $STAGE)" >&2
     exit 2
 fi
 mkdir -p "$HERE/_ref"
