@@ -294,9 +294,10 @@ void *kcna_stream(const kcna_ctx *ctx);
  * this host thread when the call began (it is left pending for its owner).
  * Runs on `stream` (a cudaStream_t, NULL = the legacy default stream) of the
  * current device, copies a 4-byte status word to a host stack variable and
- * synchronises the stream (cudaStreamSynchronize) before returning.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture.
+ * synchronises the stream (cudaStreamSynchronize) before returning, so no
+ * call may be made while a stream of the device is being captured into a CUDA
+ * graph.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current.
  * All calls share the one array: calls whose kernels overlap on the GPU (other
  * streams, other host threads) race and must be serialised by the caller.
  * Each call clears the array's error word itself. */
