@@ -170,7 +170,7 @@ def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
           "pool_entries_merged": 500_000, "maxl": 500}
     name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
     assert name == "join" and r["kernel"] == "join_tc_kernel" and r["launches_per_step"] == 6
-    per_launch = (6_000_000 * 128 * 2 + 1_000_000 * 8) / 6
+    per_launch = (6_000_000 * 128 * 2 + 1_000_000 * 12) / 6
     assert r["achieved"] == pytest.approx(per_launch / (0.3 / 6) / 1e9, abs=0.06)  # rounded to 0.1 GB/s
     assert r["frac"] == pytest.approx(r["achieved"] / 6782.4, abs=1e-4)
     st["phase_ms"]["prune"] = 400.0
@@ -178,6 +178,33 @@ def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
     name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
     assert name == "prune" and r["kernel"] == "prune_kernel"
     assert r["achieved"] == pytest.approx((3 * 1000 * 500 * 128 * 4 / 3) / (0.4 / 3) / 1e9, abs=0.06)
+    assert set(r["roofs"]) == {"hbm"}
+
+
+def test_bench_roofline_gram_prune_against_both_roofs():
+    import bench
+
+    # C2 1M, learned + BF16: prune 185 ms over 3 launches
+    st = {"phase_ms": {"join": 150.0, "merge": 180.0, "prune": 185.0},
+          "phase_launches": {"join": 6, "merge": 25, "prune": 3},
+          "bf16_rows": 1, "gram_tc": 1, "prune_tc": 1, "join_rows": 1, "cand_emitted": 1, "cand_merged": 1,
+          "pool_entries_merged": 1, "maxl": 500}
+    name, r = bench.roofline(st, 6774.6, 128, 1_000_000, 500, tensor_tflops=1713.4)
+    assert name == "prune" and r["kernel"] == "prune_gram_kernel"
+    t = r["roofs"]["tensor"]
+    pairs = 500 * 499 // 2
+    assert t["achieved"] == pytest.approx(1_000_000 * pairs * 2 * 128 / (0.185 / 3) / 1e12, abs=0.06)
+    h = r["roofs"]["hbm"]
+    assert h["achieved"] == pytest.approx(1_000_000 * 500 * 128 * 2 / (0.185 / 3) / 1e9, abs=0.06)
+    # 128 GB at 6.77 TB/s (18.9 ms) outlasts 31.9 TFLOP at 1.71 PFLOP/s (18.6 ms): HBM is the binding roof
+    assert r["bound"] == "hbm" and r["frac"] == h["frac"]
+    # at a lower tensor peak the tensor roof binds and becomes the headline
+    name, r = bench.roofline(st, 6774.6, 128, 1_000_000, 500, tensor_tflops=1000.0)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s" and r["frac"] == r["roofs"]["tensor"]["frac"]
+    # the FP32 prune has no tensor roof
+    st["prune_tc"] = 0
+    name, r = bench.roofline(st, 6774.6, 128, 1_000_000, 500, tensor_tflops=1713.4)
+    assert set(r["roofs"]) == {"hbm"} and r["kernel"] == "prune_kernel"
 
 
 C_CALLER = r"""
