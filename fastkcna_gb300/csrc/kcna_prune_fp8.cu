@@ -91,7 +91,7 @@ struct FShared {
     uint64_t slab_full[NS], slab_empty[NS], acc_full[NACC], acc_empty[NACC];
     uint64_t keys_full[2], ids_ready[2], meta_full[2], mask_full[2], node_empty[2];
     uint32_t tmem;
-    int abort_flag;
+    volatile int abort_flag;
     FMeta meta[2];
     uint32_t cm[2][MWD * PC]; // certain occlusion, word-major: word w of row t at w * PC + t
     uint32_t am[2][MWD * PC]; // undecided pairs
@@ -336,11 +336,13 @@ __global__ void __launch_bounds__(F8_THREADS, 1) prune_fp8_kernel(F8Args a) {
             }
             if (!ok) {
                 S.abort_flag = 1;
-                for (uint32_t b = 0; b < (uint32_t)NACC; ++b)
-                    if (kk > b) {
-                        const uint32_t last = b + (kk - 1 - b) / NACC * NACC;
-                        (void)mbar_wait(&S.acc_full[b], (last / NACC) & 1u, 1u << 16);
-                    }
+                // products still in flight finish before TMEM is released: every K block
+                // issued (of a node left half done too) was committed to its slab's
+                // barrier, and the last commit tracks every product issued before it
+                if (gsl > 0) {
+                    const uint32_t last = gsl - 1u;
+                    (void)mbar_wait(&S.slab_empty[last % NS], (last / NS) & 1u, 1u << 16);
+                }
             }
         }
         __syncwarp();

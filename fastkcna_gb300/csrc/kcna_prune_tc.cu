@@ -89,7 +89,7 @@ struct PgShared {
     uint64_t acc_full[NACC], acc_empty[NACC];
     uint64_t keys_full[2], ids_ready[2], meta_full[2], bound_ready[2], mask_full[2], node_empty[2];
     uint32_t tmem;
-    int abort_flag;
+    volatile int abort_flag;
     NodeMeta meta[2];
     uint32_t mask[2][MASK_WORDS];
 };
