@@ -296,7 +296,9 @@ def roofline(st, hbm_gbs, ld, n, search_k, tensor_tflops=None):
     join:  every gathered row once (BF16 or FP32) + every candidate's key and
            joiner written once (12 bytes)
     merge: candidates read once, pool entries read and written once
-    prune: every candidate row of every node read once (min(pool, search_K) rows)
+    prune: every candidate row of every pruned node read once (min(pool,
+           search_K) rows); the prunes after the first re-prune only the nodes
+           whose pool prefix changed (loops x n - prune_skipped nodes in all)
     The Gram-tile prune is also held against the tensor roof: its algorithmic
     work is one BF16 dot product of ld terms per unordered candidate pair,
     c (c - 1) / 2 pairs per node with c = min(pool, search_K) (the tiles it
@@ -308,10 +310,11 @@ def roofline(st, hbm_gbs, ld, n, search_k, tensor_tflops=None):
     ph, launches = st["phase_ms"], st["phase_launches"]
     rb = 2 if st["bf16_rows"] else 4
     c = min(search_k, st["maxl"])
+    pruned = max(st.get("loops", 1) * n - st.get("prune_skipped", 0), 0)  # node prunes run
     models = {
         "join": st["join_rows"] * ld * rb + st["cand_emitted"] * 12,
         "merge": st["cand_merged"] * 8 + st["pool_entries_merged"] * 16,
-        "prune": launches["prune"] * n * c * ld * rb,
+        "prune": pruned * c * ld * rb,
     }
     kernels = {"join": "join_tc_kernel" if st["gram_tc"] else "join_kernel", "merge": "merge_warp_kernel",
                "prune": "prune_gram_kernel" if st.get("prune_tc") else "prune_kernel"}
@@ -332,7 +335,7 @@ def roofline(st, hbm_gbs, ld, n, search_k, tensor_tflops=None):
     roofs = {"hbm": hbm}
     primary = hbm
     if name == "prune" and st.get("prune_tc") == 1 and tensor_tflops:
-        flops = n * (c * (c - 1) / 2) * 2.0 * ld  # per launch
+        flops = pruned * (c * (c - 1) / 2) * 2.0 * ld / nl  # per launch
         t_achieved = flops / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
         roofs["tensor"] = {"bound": "tensor", "achieved": round(t_achieved, 1), "peak": tensor_tflops,
                            "unit": "TFLOP/s", "frac": round(t_achieved / tensor_tflops, 4),

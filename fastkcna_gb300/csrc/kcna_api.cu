@@ -83,6 +83,7 @@ static void reset_phase_stats(kcna_ctx *c) {
     }
     c->join_rows = c->cand_emitted = c->cand_merged = c->pool_entries_merged = c->tree_attached = 0;
     c->prune_exact = 0;
+    c->prune_skipped = 0;
 }
 
 static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
@@ -96,6 +97,7 @@ static void copy_phase_stats(const kcna_ctx *c, kcna_stats *st) {
     st->pool_entries_merged = c->pool_entries_merged;
     st->tree_attached = c->tree_attached;
     st->prune_exact = c->prune_exact;
+    st->prune_skipped = c->prune_skipped;
 }
 
 kcna_status kcna_dev_malloc(kcna_ctx *c, size_t bytes, void **out, const char *what) {
@@ -180,7 +182,8 @@ static void free_state(kcna_ctx *c) {
     void *bufs[] = {c->pool, c->pool_cnt, c->radius, c->M, c->radiusM, c->found, c->fwd_new, c->fwd_new_cnt,
                     c->fwd_old, c->fwd_old_cnt, c->rnew, c->rnew_cnt, c->rold, c->rold_cnt, c->cand, c->cand_cnt,
                     c->g_ids, c->g_deg, c->g_old, c->g_old_deg, c->g_dist, c->g_isnew, c->d_controls,
-                    c->d_control_knn, c->big_list, c->big_cnt};
+                    c->d_control_knn, c->big_list, c->big_cnt, c->inc_snap, c->inc_cnt, c->inc_ids, c->inc_deg,
+                    c->inc_list, c->inc_dist};
     for (void *b : bufs)
         if (b) kcna_release(c, b);
     c->pool = nullptr;
@@ -198,6 +201,10 @@ static void free_state(kcna_ctx *c) {
     c->g_dist = nullptr;
     c->g_isnew = nullptr;
     c->d_controls = c->d_control_knn = nullptr;
+    c->inc_snap = nullptr;
+    c->inc_cnt = c->inc_ids = c->inc_deg = c->inc_list = nullptr;
+    c->inc_dist = nullptr;
+    c->inc_valid = false; // a build never reuses an earlier build's prune
     c->W = 0;
     c->cap = 0;
     c->has_graph = c->has_pools = false;

@@ -180,13 +180,15 @@ __global__ void __launch_bounds__(PW * 32) prune_kernel(R rows, uint32_t N, cons
                                                         PruneRule rule, int range, int maxc,
                                                         uint32_t *__restrict__ g_ids, float *__restrict__ g_dist,
                                                         uint32_t *__restrict__ g_deg, uint32_t W,
-                                                        unsigned long long *comps) {
+                                                        unsigned long long *comps, uint32_t n_items,
+                                                        const uint32_t *__restrict__ list) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = kcna_lane();
     uint32_t *kid = reinterpret_cast<uint32_t *>(smem) + w * 2 * range;
     float *kd = reinterpret_cast<float *>(kid + range);
-    const uint32_t q = blockIdx.x * PW + w;
-    if (q >= N) return;
+    const uint32_t item = blockIdx.x * PW + w; // node, or the item-th node of `list`
+    if (item >= n_items) return;
+    const uint32_t q = list ? list[item] : item;
     const uint64_t *pr = pool + (uint64_t)q * cap;
     const int cnt = (int)pool_cnt[q];
     int first = 0;
@@ -1181,6 +1183,39 @@ kcna_status kcna_exclusive_scan_u32(kcna_ctx *c, const uint32_t *in, uint64_t n,
     return exclusive_scan(c, in, n, out, total_h);
 }
 
+// ---- incremental prune -----------------------------------------------------
+// A node's kept list is a function of its first S = max(maxc, 2) pool entries
+// (ids and distances; the two flag bits of a key do not enter), of
+// min(count, S), of the rows and of the prune's parameters.  Within a build the
+// prune runs again after every pool refinement, and many pools come through a
+// refinement unchanged (C2 1M: a quarter of the nodes after the first
+// BridgeView round, three quarters after the second), so a later prune
+// compares every pool prefix with the snapshot of the previous prune, lists
+// the nodes whose prefix changed (and takes their new prefix into the
+// snapshot), restores the other rows from the graph that prune wrote, and
+// prunes the listed nodes only.  Warp per node; 8-byte keys read coalesced.
+__global__ void prune_diff_kernel(const uint64_t *__restrict__ pool, const uint32_t *__restrict__ pool_cnt,
+                                  uint32_t cap, uint32_t N, uint32_t S, uint64_t *__restrict__ snap,
+                                  uint32_t *__restrict__ snap_cnt, uint32_t *__restrict__ list,
+                                  uint32_t *__restrict__ list_cnt) {
+    const int lane = kcna_lane();
+    const uint32_t wpb = blockDim.x >> 5;
+    for (uint32_t q = blockIdx.x * wpb + (threadIdx.x >> 5); q < N; q += gridDim.x * wpb) {
+        const uint32_t cnt = pool_cnt[q];
+        const uint32_t m = min(cnt, S), ms = min(snap_cnt[q], S);
+        const uint64_t *pr = pool + (uint64_t)q * cap;
+        uint64_t *sr = snap + (uint64_t)q * S;
+        uint64_t d = 0;
+        for (uint32_t i = lane; i < m; i += 32) d |= (pr[i] ^ sr[i]) & ~(KCNA_FLAG_NEW | KCNA_FLAG_ISNEW);
+        if (!__any_sync(KCNA_FULL, d != 0) && m == ms) continue;
+        for (uint32_t i = lane; i < m; i += 32) sr[i] = pr[i];
+        if (lane == 0) {
+            snap_cnt[q] = cnt;
+            list[atomicAdd(list_cnt, 1u)] = q;
+        }
+    }
+}
+
 kcna_status kcna_graph_alloc(kcna_ctx *c, uint32_t W) {
     const uint64_t N = c->n;
     if (c->W == W && c->g_ids) return KCNA_OK;
@@ -1206,10 +1241,54 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
     KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(c->counters + 16, 0, 8, c->stream), "memset"));
     const size_t sm = (size_t)PW * 2 * range * 4;
     const int maxc = (int)std::min(p->search_K, c->cap);
+    const bool gram = kcna_prune_tc_ok(c, kind, (int)range, maxc, p->angle);
+    const bool fp8 = !gram && kcna_prune_fp8_ok(c, kind, (int)range, maxc);
+    // incremental prune (prune_diff_kernel) for the Gram-tile and FP32 prunes
+    const char *env = getenv("KCNA_PRUNE_INCREMENTAL");
+    const bool inc_on = !fp8 && !(env && env[0] == '0');
+    const uint64_t N = c->n, W = c->W;
+    const uint32_t S = std::min<uint32_t>(c->cap, (uint32_t)std::max(maxc, 2));
+    uint32_t sig[10] = {c->n, c->W, c->cap, S, (uint32_t)kind, range, (uint32_t)maxc,
+                        gram ? 2u : c->bf16_exact ? 1u : 0u, 0u, 0u};
+    memcpy(&sig[8], &rule.t3, 4);
+    memcpy(&sig[9], &p->angle, 4);
+    const bool inc = inc_on && c->inc_valid && memcmp(sig, c->inc_sig, sizeof sig) == 0;
     KCNA_TRY(kcna_phase_begin(c));
-    if (kcna_prune_tc_ok(c, kind, (int)range, maxc, p->angle)) { // Gram-exact rows: occlusion masks from tensor-core tiles
-        KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, p->angle, (int)range, maxc, c->counters + 16));
-    } else if (kcna_prune_fp8_ok(c, kind, (int)range, maxc)) { // float rows, high d: FP8 screen, FP32 where undecided
+    uint32_t n_items = c->n;
+    const uint32_t *list = nullptr;
+    if (!inc) {
+        int ds = 0;
+        while (ds < 10 && sig[ds] == c->inc_sig[ds]) ++ds;
+        kcna_log(c, p, "prune: all %u nodes (%s, parameter word %d)", c->n,
+                 !inc_on ? "incremental prune off" : c->inc_valid ? "new parameters" : "first prune", ds);
+    }
+    c->inc_valid = false; // until this prune's rows are saved
+    if (inc) {
+        uint32_t *list_cnt = reinterpret_cast<uint32_t *>(c->counters + 52);
+        KCNA_TRY(kcna_cuda_check(c, cudaMemsetAsync(list_cnt, 0, 4, c->stream), "memset"));
+        prune_diff_kernel<<<std::max(1, c->num_sms) * 8, 256, 0, c->stream>>>(c->pool, c->pool_cnt, c->cap, c->n, S,
+                                                                              c->inc_snap, c->inc_cnt, c->inc_list,
+                                                                              list_cnt);
+        KCNA_LAUNCHED(c);
+        KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_diff_kernel"));
+        // the previous prune's rows (the link has rewritten the graph since); the listed nodes are pruned over them
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->g_ids, c->inc_ids, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->g_dist, c->inc_dist, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->g_deg, c->inc_deg, N * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&n_items, list_cnt, 4, cudaMemcpyDeviceToHost, c->stream), "d2h"));
+        KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "prune diff sync"));
+        if (n_items > c->n) return kcna_fail(c, KCNA_E_CUDA, "prune: changed-node count out of range");
+        c->prune_skipped += c->n - n_items;
+        list = c->inc_list;
+        kcna_log(c, p, "prune: %u of %u pools changed since the previous prune", n_items, c->n);
+    }
+    if (gram) { // Gram-exact rows: occlusion masks from tensor-core tiles
+        if (list)
+            KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, p->angle, (int)range, maxc, c->counters + 16, nullptr, 0,
+                                          nullptr, list, n_items, true));
+        else
+            KCNA_TRY(kcna_prune_tc_launch(c, kind, rule.t3, p->angle, (int)range, maxc, c->counters + 16));
+    } else if (fp8) { // float rows, high d: FP8 screen, FP32 where undecided
         uint32_t *resume = nullptr;
         KCNA_TRY(kcna_scratch(c, (size_t)c->n * 4, reinterpret_cast<void **>(&resume)));
         uint32_t *resume_cnt = reinterpret_cast<uint32_t *>(c->counters + 48);
@@ -1225,17 +1304,37 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
         KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(&ex, c->counters + 49, 8, cudaMemcpyDeviceToHost, c->stream), "d2h"));
         KCNA_TRY(kcna_cuda_check(c, cudaStreamSynchronize(c->stream), "prune sync"));
         c->prune_exact += ex;
-    } else {
+    } else if (n_items > 0) {
         if (c->bf16_exact)
-            prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+            prune_kernel<<<kcna_div_up(n_items, PW), PW * 32, sm, c->stream>>>(
                 RowsB16{c->Xh, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
-                c->g_dist, c->g_deg, c->W, c->counters + 16);
+                c->g_dist, c->g_deg, c->W, c->counters + 16, n_items, list);
         else
-            prune_kernel<<<kcna_div_up(c->n, PW), PW * 32, sm, c->stream>>>(
+            prune_kernel<<<kcna_div_up(n_items, PW), PW * 32, sm, c->stream>>>(
                 RowsF32{c->X, (int)c->ld}, c->n, c->pool, c->pool_cnt, c->cap, rule, (int)range, maxc, c->g_ids,
-                c->g_dist, c->g_deg, c->W, c->counters + 16);
+                c->g_dist, c->g_deg, c->W, c->counters + 16, n_items, list);
         KCNA_LAUNCHED(c);
         KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
+    }
+    if (inc_on) {
+        if (!inc) { // first prune of the build (or new parameters): a fresh snapshot of every pool prefix
+            KCNA_TRY(kcna_alloc(c, &c->inc_snap, N * S, "prune snapshot"));
+            KCNA_TRY(kcna_alloc(c, &c->inc_cnt, N, "prune snapshot counts"));
+            KCNA_TRY(kcna_alloc(c, &c->inc_ids, N * W, "pruned ids"));
+            KCNA_TRY(kcna_alloc(c, &c->inc_dist, N * W, "pruned dists"));
+            KCNA_TRY(kcna_alloc(c, &c->inc_deg, N, "pruned degrees"));
+            KCNA_TRY(kcna_alloc(c, &c->inc_list, N, "changed nodes"));
+            KCNA_TRY(kcna_cuda_check(c, cudaMemcpy2DAsync(c->inc_snap, (size_t)S * 8, c->pool, (size_t)c->cap * 8,
+                                                          (size_t)S * 8, N, cudaMemcpyDeviceToDevice, c->stream),
+                                     "d2d"));
+            KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_cnt, c->pool_cnt, N * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        }
+        // this prune's rows, for the next prune of the build
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_ids, c->g_ids, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_dist, c->g_dist, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_deg, c->g_deg, N * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
+        memcpy(c->inc_sig, sig, sizeof sig);
+        c->inc_valid = true;
     }
     KCNA_TRY(kcna_phase_end(c, KCNA_PHASE_PRUNE));
     unsigned long long h = 0;

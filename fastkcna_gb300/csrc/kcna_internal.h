@@ -87,6 +87,19 @@ struct kcna_ctx {
     uint32_t ep = 0, width = 0;
     bool has_graph = false, has_pools = false;
 
+    // incremental prune (kcna_prune_all): the first S = min(cap, max(maxc, 2))
+    // keys and the count of every pool at the previous prune (inc_snap, n x S;
+    // inc_cnt), the graph rows that prune wrote (inc_ids / inc_dist, n x W;
+    // inc_deg), room for a list of n nodes, and what the kept lists depended on
+    // besides the pools (inc_sig).  Dropped with the pools (free_state: every
+    // build, upload and set_size), so a build never reuses an earlier build's.
+    uint64_t *inc_snap = nullptr;
+    uint32_t *inc_cnt = nullptr, *inc_ids = nullptr, *inc_deg = nullptr, *inc_list = nullptr;
+    float *inc_dist = nullptr;
+    bool inc_valid = false;
+    uint32_t inc_sig[10] = {};
+    uint64_t prune_skipped = 0; // nodes whose prune the snapshot showed unchanged
+
     // controls (exact MAXL-NN of sampled nodes) for the recall estimate
     std::vector<uint32_t> control_ids;
     std::vector<uint32_t> control_cache; // the reference's control order for control_cache_n rows
@@ -199,10 +212,12 @@ inline float kcna_alpha_threshold(float angle) {
 bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float angle);
 // Node mode (nodes null): each node's pool.  List mode: n_items staged
 // candidate lists (pool-format keys, `stride` apart, cnt[k] each) of nodes[k].
+// Pool-list mode (pool_list; keys, stride and cnt unused): the pools of the
+// n_items nodes nodes[k].
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
                                  unsigned long long *comps, const uint64_t *keys = nullptr, uint64_t stride = 0,
                                  const uint32_t *cnt = nullptr, const uint32_t *nodes = nullptr,
-                                 uint32_t n_items = 0);
+                                 uint32_t n_items = 0, bool pool_list = false);
 // tau-MNG prune of float rows on FP8 E4M3 Gram tiles (kcna_prune_fp8.cu);
 // requires c->fp8_screen.  The first 128 candidates of every item are pruned
 // on the tiles; items whose scan ran out of them with fewer than range kept

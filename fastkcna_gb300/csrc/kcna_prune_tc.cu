@@ -98,6 +98,7 @@ struct PgArgs {
     uint32_t N, cap, W, ld; // N: ids at or beyond are skipped (the layer prefix); cap: candidate row stride
     uint32_t n_items;       // nodes (or staged lists) to prune
     const uint32_t *nodes;  // staged lists: node of list k (null: item k is node k)
+    uint32_t by_node;       // 1: item k is the pool of node nodes[k] (candidate row nodes[k])
     const uint64_t *pool;   // candidate keys, row = node (or list), cap apart
     const uint16_t *rows;   // BF16 rows, ld elements apart
     const uint32_t *pool_cnt; // candidates of each row
@@ -235,8 +236,9 @@ __global__ void __launch_bounds__(PG_THREADS, 1) prune_gram_kernel(PgArgs a) {
             if (q >= a.n_items) return;
             const int b = kk & 1;
             pending = kk;
-            const uint32_t cnt = min(a.pool_cnt[q], a.cap);
-            const uint64_t base = (uint64_t)q * a.cap;
+            const uint32_t row = a.by_node ? a.nodes[q] : q;
+            const uint32_t cnt = min(a.pool_cnt[row], a.cap);
+            const uint64_t base = (uint64_t)row * a.cap;
             const uint32_t shift = (uint32_t)(base & 1u);
             const uint32_t ncopy = min(cnt, (uint32_t)max(a.maxc, 2));
             const uint32_t nent = (shift + ncopy + 1u) & ~1u;
@@ -606,19 +608,22 @@ bool kcna_prune_tc_ok(const kcna_ctx *c, int kind, int range, int maxc, float an
 
 kcna_status kcna_prune_tc_launch(kcna_ctx *c, int kind, float t3, float angle, int range, int maxc,
                                  unsigned long long *comps, const uint64_t *keys, uint64_t stride, const uint32_t *cnt,
-                                 const uint32_t *nodes, uint32_t n_items) {
+                                 const uint32_t *nodes, uint32_t n_items, bool pool_list) {
     if (!kcna_prune_tc_ok(c, kind, range, maxc, angle))
         return kcna_fail(c, KCNA_E_STATE, "Gram-tile prune needs Gram-exact rows");
+    if (pool_list && !nodes) return kcna_fail(c, KCNA_E_ARG, "Gram-tile prune: pool-list mode needs a node list");
+    const bool staged = nodes && !pool_list;
     PgArgs a;
-    a.N = nodes ? 0xFFFFFFFFu : c->n; // staged lists carry no layer prefix
-    a.cap = nodes ? (uint32_t)stride : c->cap;
+    a.N = staged ? 0xFFFFFFFFu : c->n; // staged lists carry no layer prefix
+    a.cap = staged ? (uint32_t)stride : c->cap;
     a.n_items = nodes ? n_items : c->n;
     a.nodes = nodes;
+    a.by_node = pool_list ? 1u : 0u;
     a.W = c->W;
     a.ld = c->ld;
-    a.pool = nodes ? keys : c->pool;
+    a.pool = staged ? keys : c->pool;
     a.rows = c->Xh;
-    a.pool_cnt = nodes ? cnt : c->pool_cnt;
+    a.pool_cnt = staged ? cnt : c->pool_cnt;
     a.norms = c->norms;
     a.thr = kcna_alpha_threshold(angle);
     // tau-MNG: 3 tau; alpha-PG: 4m, m = 1/2 - thr + 1e-5 (the angle screen's margin)

@@ -69,7 +69,7 @@ class Stats(C.Structure):
         ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
         ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
         ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32), ("prune_tc", C.c_uint32),
-        ("prune_exact", C.c_uint64)]
+        ("prune_exact", C.c_uint64), ("prune_skipped", C.c_uint64)]
 
     def as_dict(self):
         it = self.iterations
@@ -94,7 +94,7 @@ class Stats(C.Structure):
                     seed_loss_first=self.seed_loss_first, seed_loss_last=self.seed_loss_last,
                     seed_input_scale=self.seed_input_scale, seed_recall=self.seed_recall,
                     seed_comps=self.seed_comps, bf16_rows=self.bf16_rows, gram_tc=self.gram_tc, prune_tc=self.prune_tc,
-                    prune_exact=self.prune_exact)
+                    prune_exact=self.prune_exact, prune_skipped=self.prune_skipped)
 
 
 _lib = None

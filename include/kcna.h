@@ -167,6 +167,9 @@ typedef struct {
                                   2: the tau-MNG prunes screened float rows on FP8 E4M3 Gram tiles
                                   (d >= 256), undecided pairs recomputed in FP32 */
     uint64_t prune_exact;      /* pairs of the FP8-screened prunes recomputed in FP32 */
+    uint64_t prune_skipped;    /* node prunes skipped: the node's first search_K pool entries (ids,
+                                  distances) and their count were those of the previous prune of
+                                  the build, whose kept list was reused */
 } kcna_stats;
 
 typedef struct kcna_ctx kcna_ctx;

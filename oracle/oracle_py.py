@@ -55,7 +55,7 @@ class Stats(C.Structure):
         ("seed_train_ms", C.c_double), ("seed_total_ms", C.c_double), ("seed_loss_first", C.c_float),
         ("seed_loss_last", C.c_float), ("seed_input_scale", C.c_float), ("seed_recall", C.c_float),
         ("seed_comps", C.c_uint64), ("bf16_rows", C.c_uint32), ("gram_tc", C.c_uint32),
-        ("prune_tc", C.c_uint32),
+        ("prune_tc", C.c_uint32), ("prune_exact", C.c_uint64), ("prune_skipped", C.c_uint64),
     ]
 
 

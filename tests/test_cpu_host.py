@@ -32,6 +32,31 @@ def test_abi_exports_every_declared_function():
     assert not missing, missing
 
 
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    """kcna_params / kcna_stats as the C compiler lays them out, against the
+    ctypes mirrors of the product binding and of the oracle binding (a stats
+    struct shorter than the C one is overrun by the library's memset)."""
+    import ctypes
+
+    from fastkcna_gb300 import kcna
+
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "kcna.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu %zu %zu %zu\\n", sizeof(kcna_params), sizeof(kcna_stats),\n'
+        "         offsetof(kcna_stats, prune_tc), offsetof(kcna_stats, prune_skipped));\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)], check=True)
+    p_size, s_size, off_tc, off_skip = map(int, subprocess.run([str(exe)], capture_output=True, text=True,
+                                                               check=True).stdout.split())
+    for Params, Stats in ((kcna.Params, kcna.Stats), (oracle_py.Params, oracle_py.Stats)):
+        assert ctypes.sizeof(Params) == p_size
+        assert ctypes.sizeof(Stats) == s_size
+        assert Stats.prune_tc.offset == off_tc and Stats.prune_skipped.offset == off_skip
+
+
 def _model_pool(L, cap, entries):
     """Top-`cap` by (distance, insertion order) of unique ids: what the
     sequential try-insert keeps when no distance ties at the boundary."""
@@ -167,7 +192,7 @@ def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
 
     st = {"phase_ms": {"join": 300.0, "merge": 100.0, "prune": 200.0}, "phase_launches": {"join": 6, "merge": 10, "prune": 3},
           "bf16_rows": 1, "gram_tc": 1, "join_rows": 6_000_000, "cand_emitted": 1_000_000, "cand_merged": 2_000_000,
-          "pool_entries_merged": 500_000, "maxl": 500}
+          "pool_entries_merged": 500_000, "maxl": 500, "loops": 3, "prune_skipped": 0}
     name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
     assert name == "join" and r["kernel"] == "join_tc_kernel" and r["launches_per_step"] == 6
     per_launch = (6_000_000 * 128 * 2 + 1_000_000 * 12) / 6
@@ -179,6 +204,10 @@ def test_bench_roofline_picks_dominant_phase_and_counts_bf16_bytes():
     assert name == "prune" and r["kernel"] == "prune_kernel"
     assert r["achieved"] == pytest.approx((3 * 1000 * 500 * 128 * 4 / 3) / (0.4 / 3) / 1e9, abs=0.06)
     assert set(r["roofs"]) == {"hbm"}
+    # incremental prunes: only the node prunes that ran count
+    st["prune_skipped"] = 1200
+    name, r = bench.roofline(st, 6782.4, 128, 1000, 500)
+    assert r["achieved"] == pytest.approx((1800 * 500 * 128 * 4 / 3) / (0.4 / 3) / 1e9, abs=0.06)
 
 
 def test_bench_roofline_gram_prune_against_both_roofs():
@@ -188,7 +217,7 @@ def test_bench_roofline_gram_prune_against_both_roofs():
     st = {"phase_ms": {"join": 150.0, "merge": 180.0, "prune": 185.0},
           "phase_launches": {"join": 6, "merge": 25, "prune": 3},
           "bf16_rows": 1, "gram_tc": 1, "prune_tc": 1, "join_rows": 1, "cand_emitted": 1, "cand_merged": 1,
-          "pool_entries_merged": 1, "maxl": 500}
+          "pool_entries_merged": 1, "maxl": 500, "loops": 3, "prune_skipped": 0}
     name, r = bench.roofline(st, 6774.6, 128, 1_000_000, 500, tensor_tflops=1713.4)
     assert name == "prune" and r["kernel"] == "prune_gram_kernel"
     t = r["roofs"]["tensor"]
