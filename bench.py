@@ -657,6 +657,7 @@ def run_gpu(args, ws, rank, local):
                     "dist_evals_per_s": round((st["n_comps"] + st["prune_comps"] + st["bridge_comps"]) / (ms / 1000.0)),
                     "cand_overflow": sum(st["iter_cand_overflow"]), "cand_emitted": st["cand_emitted"],
                     "cand_merged": st["cand_merged"], "tree_attached": st["tree_attached"],
+                    "prune_skipped": st["prune_skipped"],
                     "avg_degree": st["aod"],
                     "iter_join_ms": [round(x, 1) for x in st["iter_join_ms"]],
                     "iter_merge_ms": [round(x, 1) for x in st["iter_merge_ms"]],
