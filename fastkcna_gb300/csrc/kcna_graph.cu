@@ -1316,20 +1316,33 @@ kcna_status kcna_prune_all(kcna_ctx *c, const kcna_params *p, int kind, uint64_t
         KCNA_LAUNCHED(c);
         KCNA_TRY(kcna_cuda_check(c, cudaGetLastError(), "prune_kernel"));
     }
-    if (inc_on) {
-        if (!inc) { // first prune of the build (or new parameters): a fresh snapshot of every pool prefix
-            KCNA_TRY(kcna_alloc(c, &c->inc_snap, N * S, "prune snapshot"));
-            KCNA_TRY(kcna_alloc(c, &c->inc_cnt, N, "prune snapshot counts"));
-            KCNA_TRY(kcna_alloc(c, &c->inc_ids, N * W, "pruned ids"));
-            KCNA_TRY(kcna_alloc(c, &c->inc_dist, N * W, "pruned dists"));
-            KCNA_TRY(kcna_alloc(c, &c->inc_deg, N, "pruned degrees"));
-            KCNA_TRY(kcna_alloc(c, &c->inc_list, N, "changed nodes"));
+    bool save = inc_on;
+    if (save && !inc) { // first prune of the build (or new parameters): a fresh snapshot of every pool prefix
+        kcna_status as = kcna_alloc(c, &c->inc_snap, N * S, "prune snapshot");
+        if (as == KCNA_OK) as = kcna_alloc(c, &c->inc_cnt, N, "prune snapshot counts");
+        if (as == KCNA_OK) as = kcna_alloc(c, &c->inc_ids, N * W, "pruned ids");
+        if (as == KCNA_OK) as = kcna_alloc(c, &c->inc_dist, N * W, "pruned dists");
+        if (as == KCNA_OK) as = kcna_alloc(c, &c->inc_deg, N, "pruned degrees");
+        if (as == KCNA_OK) as = kcna_alloc(c, &c->inc_list, N, "changed nodes");
+        if (as == KCNA_E_OOM) { // no room beside the build: every prune of this build prunes every node
+            void *bufs[] = {c->inc_snap, c->inc_cnt, c->inc_ids, c->inc_dist, c->inc_deg, c->inc_list};
+            for (void *b : bufs) kcna_release(c, b);
+            c->inc_snap = nullptr;
+            c->inc_cnt = c->inc_ids = c->inc_deg = c->inc_list = nullptr;
+            c->inc_dist = nullptr;
+            c->err.clear();
+            save = false;
+            kcna_log(c, p, "prune: no device memory for the incremental prune's snapshot; full prunes");
+        } else if (as != KCNA_OK) {
+            return as;
+        } else {
             KCNA_TRY(kcna_cuda_check(c, cudaMemcpy2DAsync(c->inc_snap, (size_t)S * 8, c->pool, (size_t)c->cap * 8,
                                                           (size_t)S * 8, N, cudaMemcpyDeviceToDevice, c->stream),
                                      "d2d"));
             KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_cnt, c->pool_cnt, N * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
         }
-        // this prune's rows, for the next prune of the build
+    }
+    if (save) { // this prune's rows, for the next prune of the build
         KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_ids, c->g_ids, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
         KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_dist, c->g_dist, N * W * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
         KCNA_TRY(kcna_cuda_check(c, cudaMemcpyAsync(c->inc_deg, c->g_deg, N * 4, cudaMemcpyDeviceToDevice, c->stream), "d2d"));
